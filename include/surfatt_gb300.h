@@ -1,0 +1,249 @@
+/*
+ * surfatt_gb300.h -- C ABI of the GB300 (sm_103a) SurfATT travel-time +
+ * adjoint library (libsurfatt_gb300.so).
+ *
+ * Three layers, all plain C types:
+ *
+ *  1. Link-time drop-ins for the reference's external Fortran procedures
+ *     (gfortran mangling: lower case + trailing underscore, every argument by
+ *     reference, default INTEGER = 4 bytes, no hidden arguments).  Arrays are
+ *     host memory, column-major (nx, ny), owned by the caller; outputs are
+ *     fully overwritten.  The reference has no error return: a source on the
+ *     grid boundary prints the reference's message and exits the process
+ *     (as its `stop` does); every other outcome is recorded in a per-thread
+ *     status readable with surfatt_last_status().
+ *
+ *  2. The measurement layer mirroring att_measadj (src/measadj.f90:25-114):
+ *     forward + receiver interpolation + misfit, adjoint + mask, density
+ *     adjoint, for one (source, period), on host buffers.
+ *
+ *  3. The batched engine: a whole gradient evaluation (every (period,
+ *     source) solve of a work list: forward, receiver interpolation, misfit,
+ *     adjoint source, one or two adjoint sweeps, mask and the per-period
+ *     kernel sum) with device-resident models, in plain FP64 or with the
+ *     factored unknown tau swept in FP32.
+ *
+ * All entry points are thread-safe; drop-in calls from different host
+ * threads use separate CUDA streams and scratch buffers.
+ */
+#ifndef SURFATT_GB300_H
+#define SURFATT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SURFATT_OK = 0,
+  SURFATT_SOURCE_ON_BOUNDARY = 1, /* reference: 'source on the boundary, mesh error', stop */
+  SURFATT_BAD_ARG = 2,            /* grid too small, point outside the grid, bad pointer */
+  SURFATT_NOT_CONVERGED = 3,      /* MaxIter reached; output is the last iterate */
+  SURFATT_OOM = 4,                /* device allocation failed / HBM budget exceeded */
+  SURFATT_CUDA_ERROR = 5,         /* a CUDA runtime call failed */
+  SURFATT_TIMEOUT = 6             /* a bounded wait gave up (serving loop) */
+} surfatt_status_t;
+
+typedef enum {
+  SURFATT_PREC_FP64 = 0, /* plain FP64, reference arithmetic */
+  SURFATT_PREC_FP32 = 1  /* tau swept in FP32; T0, misfit, kernels, convergence in FP64 */
+} surfatt_precision_t;
+
+typedef enum {
+  SURFATT_MODE_FORWARD = 0, /* forward + misfit + synthetic times only */
+  SURFATT_MODE_2D = 2,      /* tomo2d: adj_s += adj / svel^2 (src/tomo2d.f90:145-156) */
+  SURFATT_MODE_3D = 3       /* tomo: adj_s += adj / svel^3, adj_density += kden / svel^3
+                               (src/acqui.f90:307-316), two adjoint solves per source */
+} surfatt_mode_t;
+
+/* ---------------------------------------------------------------------------
+ * 1. Drop-in symbols (src/eikon_solver_2d.f90)
+ * ------------------------------------------------------------------------- */
+
+/* replaces FSM_UW_PS_lonlat_2d, src/eikon_solver_2d.f90:764-1126 (called at
+ * src/measadj.f90:68-70).  `u` is accepted and ignored, as in the reference
+ * (it only feeds an error monitor that is never reported). */
+void fsm_uw_ps_lonlat_2d_(const double* xx_deg, const double* yy_deg, const int* nx,
+                          const int* ny, const double* spha, const double* sphb,
+                          const double* sphc, double* T, const double* fun,
+                          const double* x0_deg, const double* y0_deg, const double* u);
+
+/* replaces FSM_UW_PS_cart_2d, src/eikon_solver_2d.f90:22-342 */
+void fsm_uw_ps_cart_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                        const double* a, const double* b, const double* c, double* T,
+                        const double* fun, const double* x0, const double* y0,
+                        const double* u);
+
+/* replaces FSM_WENO3_PS_2d (additive T = tau + T0), src/eikon_solver_2d.f90:344-548 */
+void fsm_weno3_ps_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                      const double* a, const double* b, const double* c, double* T,
+                      const double* fun, const double* x0, const double* y0, const double* u);
+
+/* replaces FSM_WENO3_PS_multi_2d (T = tau * T0), src/eikon_solver_2d.f90:552-761 */
+void fsm_weno3_ps_multi_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                            const double* a, const double* b, const double* c, double* T,
+                            const double* fun, const double* x0, const double* y0,
+                            const double* u);
+
+/* replaces FSM_O1_JSE_lonlat_2d, src/eikon_solver_2d.f90:1276-1446 (called at
+ * src/measadj.f90:85-88 and :99-102) */
+void fsm_o1_jse_lonlat_2d_(const double* xx_deg, const double* yy_deg, const int* nx,
+                           const int* ny, const double* spha, const double* sphb,
+                           const double* sphc, const double* T, double* Ta,
+                           const double* xrec_deg, const double* yrec_deg,
+                           const double* sourceAdj, const int* nr);
+
+/* replaces FSM_O1_JSE_2d, src/eikon_solver_2d.f90:1132-1273 */
+void fsm_o1_jse_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                    const double* a, const double* b, const double* c, const double* T,
+                    double* Ta, const double* xrec, const double* yrec,
+                    const double* sourceAdj, const int* nr);
+
+/* replaces mask, src/eikon_solver_2d.f90:1449-1467 (called at src/measadj.f90:89, :103) */
+void mask_(const double* xx, const double* yy, const int* nx, const int* ny, double* TableAdj,
+           const double* x0, const double* y0);
+
+/* Status and sweep-iteration count of the calling thread's last drop-in or
+ * measurement call (no counterpart in the reference, which has no status). */
+int surfatt_last_status(void);
+int surfatt_last_iterations(void);
+
+/* Behaviour of a drop-in call that finds the source on the grid boundary:
+ * 1 (default) prints the reference's message and exits the process like its
+ * `stop`; 0 records SURFATT_SOURCE_ON_BOUNDARY and returns. */
+void surfatt_set_exit_on_boundary(int enable);
+
+/* ---------------------------------------------------------------------------
+ * 2. Measurement layer (att_measadj, src/measadj.f90:62-114), host buffers
+ * ------------------------------------------------------------------------- */
+
+/* run_forward (src/measadj.f90:62-73): fun = 1/vel2d, FSM_UW_PS_lonlat_2d with
+ * (m11, m22, -m12), receiver times tekio by bilinear interpolation
+ * (interp2, src/shared/utils.f90:917-956), chi = 0.5*sum(w*(tekio-tt)^2).
+ * Fields (nx, ny) column-major; timetable is an (nx, ny) output. */
+surfatt_status_t surfatt_measadj_run_forward(const double* xgrids, const double* ygrids,
+                                             int nx, int ny, const double* vel2d,
+                                             const double* m11, const double* m22,
+                                             const double* m12, double srcx, double srcy,
+                                             int nrec, const double* recx, const double* recy,
+                                             const double* tt, const double* weight,
+                                             double* timetable, double* tekio, double* chi);
+
+/* run_adjoint (src/measadj.f90:75-90): zero weight where |tekio-tt|/tt > 0.5
+ * (weight updated in place), adjoint with sourceAdj = weight*(tekio-tt),
+ * then mask. */
+surfatt_status_t surfatt_measadj_run_adjoint(const double* xgrids, const double* ygrids,
+                                             int nx, int ny, const double* m11,
+                                             const double* m22, const double* m12,
+                                             double srcx, double srcy, int nrec,
+                                             const double* recx, const double* recy,
+                                             const double* tt, const double* tekio,
+                                             double* weight, const double* timetable,
+                                             double* adjtable);
+
+/* run_adjoint_density (src/measadj.f90:92-104): sourceAdj = -weight */
+surfatt_status_t surfatt_measadj_run_adjoint_density(
+    const double* xgrids, const double* ygrids, int nx, int ny, const double* m11,
+    const double* m22, const double* m12, double srcx, double srcy, int nrec,
+    const double* recx, const double* recy, const double* weight, const double* timetable,
+    double* density);
+
+/* ---------------------------------------------------------------------------
+ * 3. Batched gradient evaluation
+ * ------------------------------------------------------------------------- */
+
+/* A gradient evaluation's inputs.  Period p has its own lon/lat grid of
+ * nx[p] x ny[p] nodes (coordinates xgrid[xoff[p]..], ygrid[yoff[p]..],
+ * degrees, uniformly spaced and increasing) and fields svel (phase velocity),
+ * m11, m12, m22 (surface metric, src/grid.f90:142-145), each (nx, ny)
+ * column-major at cell offset goff[p].  Solve s = (period pidx[s], source
+ * srcx[s]/srcy[s]) owns receivers rec_off[s] .. rec_off[s]+nrec[s]-1 of the
+ * receiver table; path[r] is the receiver's index in the synthetic-time
+ * table tt_fwd (npath entries) -- the reference's SrcRec%isrcs work list and
+ * per-source gathers (src/src_rec.f90:252-283, 338-369).  All pointers are
+ * host memory. */
+typedef struct {
+  int nperiod;
+  const int* nx;
+  const int* ny;
+  const long long* xoff;
+  const long long* yoff;
+  const long long* goff;
+  const double* xgrid;
+  const double* ygrid;
+  const double* svel;
+  const double* m11;
+  const double* m12;
+  const double* m22;
+  int nsolve;
+  const int* pidx;
+  const double* srcx;
+  const double* srcy;
+  const int* rec_off;
+  const int* nrec;
+  const double* recx;
+  const double* recy;
+  const double* tt;
+  const double* weight;
+  const int* path;
+  int npath;
+} surfatt_problem_t;
+
+/* Outputs of one evaluation (host buffers, any may be NULL):
+ * adj_s / adj_density: ncell = goff[last] + nx*ny of the last period,
+ * period-slowest; chi: sum of the solves' misfits; tt_fwd: npath synthetic
+ * times; status / fwd_iters / adj_iters: per solve. */
+typedef struct {
+  double* adj_s;
+  double* adj_density;
+  double* chi;
+  double* tt_fwd;
+  int* status;
+  int* fwd_iters;
+  int* adj_iters;
+} surfatt_result_t;
+
+typedef struct surfatt_engine surfatt_engine_t;
+
+/* Create an engine on `device`.  hbm_budget_bytes bounds the engine's device
+ * allocations (0 = no bound beyond the device's free memory). */
+surfatt_status_t surfatt_engine_create(surfatt_engine_t** engine, int device,
+                                       size_t hbm_budget_bytes);
+void surfatt_engine_destroy(surfatt_engine_t* engine);
+
+/* Copy a problem to the device (grids, fields, work list, receivers) and size
+ * the engine's workspace.  Replaces any previously loaded problem. */
+surfatt_status_t surfatt_engine_load(surfatt_engine_t* engine, const surfatt_problem_t* pb);
+
+/* Replace the phase-velocity fields of the loaded problem (a line-search
+ * trial model or the next inversion iterate); same layout as pb->svel. */
+surfatt_status_t surfatt_engine_update_velocity(surfatt_engine_t* engine, const double* svel);
+
+/* Launch one gradient evaluation on the engine's stream (asynchronous). */
+surfatt_status_t surfatt_engine_run(surfatt_engine_t* engine, surfatt_mode_t mode,
+                                    surfatt_precision_t precision);
+
+/* Wait for the last run; returns its overall status (first failing solve). */
+surfatt_status_t surfatt_engine_sync(surfatt_engine_t* engine);
+
+/* Copy the last run's results to host buffers (synchronises first). */
+surfatt_status_t surfatt_engine_results(surfatt_engine_t* engine, surfatt_result_t* out);
+
+/* Device time of the last run (ms, CUDA events on the engine's stream) and of
+ * its solve kernel alone; number of kernel launches it issued. */
+surfatt_status_t surfatt_engine_timing(surfatt_engine_t* engine, double* total_ms,
+                                       double* solve_kernel_ms, int* launches);
+
+/* Total sweep cell visits of the last run (forward, adjoint), for the
+ * algorithmic roofline. */
+surfatt_status_t surfatt_engine_work(surfatt_engine_t* engine, double* fwd_cell_updates,
+                                     double* adj_cell_updates);
+
+/* Library version string. */
+const char* surfatt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,180 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+The oracle is a plain-C restatement of the reference Fortran (see
+``surfatt_oracle.c`` for the file:line map).  Only the test suite, the smoke
+check and the benchmark's CPU-baseline leg import this module; the product
+library never does.
+
+Parity status: unpinned by the reference's own tests (it has none for this
+path and cannot be built here); pinned by analytic known-answer,
+reciprocity and finite-difference tests in ``tests/``.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libsurfatt_oracle.so")
+_lib = None
+
+OK, SOURCE_ON_BOUNDARY, BAD_ARG, NOT_CONVERGED = 0, 1, 2, 3
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_llp = ctypes.POINTER(ctypes.c_longlong)
+
+
+def build():
+    """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+        _lib.orc_gradient_eval_range.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp,
+                                                 _ip, _ip, _ip]
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _fortran2d(a):
+    """(nx, ny) array -> column-major buffer (x fastest)."""
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def _solve(fn, xx, yy, a, b, c, fun, x0, y0):
+    xx, yy = _f64(xx), _f64(yy)
+    nx, ny = len(xx), len(yy)
+    a, b, c, fun = (_fortran2d(v) for v in (a, b, c, fun))
+    T = np.zeros((nx, ny), order="F")
+    it = ctypes.c_int(0)
+    st = fn(_d(xx), _d(yy), nx, ny, _d(a), _d(b), _d(c), _d(T), _d(fun), ctypes.c_double(x0),
+            ctypes.c_double(y0), ctypes.byref(it))
+    return T, st, it.value
+
+
+def fsm_uw_ps_lonlat_2d(xx_deg, yy_deg, spha, sphb, sphc, fun, x0_deg, y0_deg):
+    """Returns (T (nx, ny), status, iterations)."""
+    return _solve(lib().orc_fsm_uw_ps_lonlat_2d, xx_deg, yy_deg, spha, sphb, sphc, fun, x0_deg,
+                  y0_deg)
+
+
+def fsm_uw_ps_cart_2d(xx, yy, a, b, c, fun, x0, y0):
+    return _solve(lib().orc_fsm_uw_ps_cart_2d, xx, yy, a, b, c, fun, x0, y0)
+
+
+def fsm_weno3_ps_multi_2d(xx, yy, a, b, c, fun, x0, y0):
+    return _solve(lib().orc_fsm_weno3_ps_multi_2d, xx, yy, a, b, c, fun, x0, y0)
+
+
+def fsm_weno3_ps_2d(xx, yy, a, b, c, fun, x0, y0):
+    return _solve(lib().orc_fsm_weno3_ps_2d, xx, yy, a, b, c, fun, x0, y0)
+
+
+def _adjoint(fn, xx, yy, a, b, c, T, xrec, yrec, sadj):
+    xx, yy = _f64(xx), _f64(yy)
+    nx, ny = len(xx), len(yy)
+    a, b, c, T = (_fortran2d(v) for v in (a, b, c, T))
+    xrec, yrec, sadj = _f64(xrec), _f64(yrec), _f64(sadj)
+    Ta = np.zeros((nx, ny), order="F")
+    it = ctypes.c_int(0)
+    st = fn(_d(xx), _d(yy), nx, ny, _d(a), _d(b), _d(c), _d(T), _d(Ta), _d(xrec), _d(yrec),
+            _d(sadj), len(xrec), ctypes.byref(it))
+    return Ta, st, it.value
+
+
+def fsm_o1_jse_lonlat_2d(xx_deg, yy_deg, spha, sphb, sphc, T, xrec_deg, yrec_deg, sadj):
+    return _adjoint(lib().orc_fsm_o1_jse_lonlat_2d, xx_deg, yy_deg, spha, sphb, sphc, T,
+                    xrec_deg, yrec_deg, sadj)
+
+
+def fsm_o1_jse_2d(xx, yy, a, b, c, T, xrec, yrec, sadj):
+    return _adjoint(lib().orc_fsm_o1_jse_2d, xx, yy, a, b, c, T, xrec, yrec, sadj)
+
+
+def mask(xx, yy, table, x0, y0):
+    xx, yy = _f64(xx), _f64(yy)
+    t = _fortran2d(table).copy(order="F")
+    lib().orc_mask(_d(xx), _d(yy), len(xx), len(yy), _d(t), ctypes.c_double(x0),
+                   ctypes.c_double(y0))
+    return t
+
+
+def interp2(x, y, v, xq, yq):
+    x, y = _f64(x), _f64(y)
+    v = _fortran2d(v)
+    out = ctypes.c_double(0)
+    st = lib().orc_interp2(_d(x), len(x), _d(y), len(y), _d(v), ctypes.c_double(xq),
+                           ctypes.c_double(yq), ctypes.byref(out))
+    if st != OK:
+        raise ValueError("interp2: query point outside the grid")
+    return out.value
+
+
+class _Problem(ctypes.Structure):
+    _fields_ = [("nperiod", ctypes.c_int), ("nx", _ip), ("ny", _ip), ("xoff", _llp),
+                ("yoff", _llp), ("goff", _llp), ("xgrid", _dp), ("ygrid", _dp),
+                ("svel", _dp), ("m11", _dp), ("m12", _dp), ("m22", _dp),
+                ("nsolve", ctypes.c_int), ("pidx", _ip), ("srcx", _dp), ("srcy", _dp),
+                ("rec_off", _ip), ("nrec", _ip), ("recx", _dp), ("recy", _dp), ("tt", _dp),
+                ("weight", _dp), ("path", _ip), ("npath", ctypes.c_int)]
+
+
+def gradient_eval(pb, mode=2, nthreads=1, s_begin=0, s_end=None):
+    """One gradient evaluation of a packed problem (see surfatt_gb300.workloads.Problem).
+
+    mode 0: forward only; 2: tomo2d (adj/svel^2); 3: 3-D (adj and density /svel^3).
+    Returns dict(adj_s, adj_density, chi, tt_fwd, status, fwd_iters, adj_iters, rc).
+    """
+    if s_end is None:
+        s_end = pb.nsolve
+    keep = []
+
+    def P(a, kind):
+        a = np.ascontiguousarray(a, dtype={"d": np.float64, "i": np.int32, "q": np.int64}[kind])
+        keep.append(a)
+        return a.ctypes.data_as({"d": _dp, "i": _ip, "q": _llp}[kind])
+
+    s = _Problem(pb.nperiod, P(pb.nx, "i"), P(pb.ny, "i"), P(pb.xoff, "q"), P(pb.yoff, "q"),
+                 P(pb.goff, "q"), P(pb.xgrid, "d"), P(pb.ygrid, "d"), P(pb.svel, "d"),
+                 P(pb.m11, "d"), P(pb.m12, "d"), P(pb.m22, "d"), pb.nsolve, P(pb.pidx, "i"),
+                 P(pb.srcx, "d"), P(pb.srcy, "d"), P(pb.rec_off, "i"), P(pb.nrec, "i"),
+                 P(pb.recx, "d"), P(pb.recy, "d"), P(pb.tt, "d"), P(pb.weight, "d"),
+                 P(pb.path, "i"), pb.npath)
+    ncell = pb.ncell
+    adj_s = np.zeros(ncell)
+    adj_d = np.zeros(ncell)
+    chi = ctypes.c_double(0)
+    tt_fwd = np.zeros(max(pb.npath, 1))
+    status = np.zeros(pb.nsolve, np.int32)
+    fit = np.zeros(pb.nsolve, np.int32)
+    ait = np.zeros(pb.nsolve, np.int32)
+    rc = lib().orc_gradient_eval_range(ctypes.byref(s), mode, nthreads, s_begin, s_end,
+                                       _d(adj_s), _d(adj_d), ctypes.byref(chi), _d(tt_fwd),
+                                       _i(status), _i(fit), _i(ait))
+    return dict(adj_s=adj_s, adj_density=adj_d, chi=chi.value, tt_fwd=tt_fwd[:pb.npath],
+                status=status, fwd_iters=fit, adj_iters=ait, rc=rc)
+
+
+def scatter_all_i(countval, size, rank):
+    a, b = ctypes.c_int(0), ctypes.c_int(0)
+    lib().orc_scatter_all_i(countval, size, rank, ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value

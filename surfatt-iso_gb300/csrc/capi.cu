@@ -1,0 +1,854 @@
+// capi.cu -- host side of libsurfatt_gb300.so: the drop-in Fortran symbols,
+// the att_measadj mirror and the batched gradient-evaluation engine.
+//
+// There is no CPU path here: every solve runs on the GPU, and a missing or
+// failing device is reported as SURFATT_CUDA_ERROR.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <vector>
+
+#include "../../include/surfatt_gb300.h"
+#include "kernels.cuh"
+
+using namespace sgb;
+
+namespace {
+
+thread_local int g_last_status = SURFATT_OK;
+thread_local int g_last_iters = 0;
+int g_exit_on_boundary = 1;
+
+#define CK(call)                                                                 \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      std::fprintf(stderr, "surfatt_gb300: %s failed: %s (%s:%d)\n", #call,       \
+                   cudaGetErrorString(e_), __FILE__, __LINE__);                  \
+      return SURFATT_CUDA_ERROR;                                                 \
+    }                                                                            \
+  } while (0)
+
+// Grow-only device buffer.
+struct DBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  size_t* counter = nullptr;  // engine allocation counter (budget), may be null
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return SURFATT_OK;
+    release();
+    size_t want = bytes < 256 ? 256 : bytes;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      p = nullptr;
+      cap = 0;
+      cudaGetLastError();
+      return SURFATT_OOM;
+    }
+    cap = want;
+    if (counter) *counter += cap;
+    return SURFATT_OK;
+  }
+  void release() {
+    if (p) {
+      cudaFree(p);
+      if (counter) *counter -= cap;
+    }
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// Per-thread drop-in context: one stream and grow-only scratch per host
+// thread (the reference runs one solver per MPI rank; several ranks or
+// threads may share a GPU).
+// ---------------------------------------------------------------------------
+struct PeriodBufs {
+  DBuf xdeg, ydeg, xs, ys, cosy, siny, a, b, c, fun, f2, disx, disy, A, B, C, V;
+  int ensure(int nx, int ny) {
+    const size_t N = (size_t)nx * ny * sizeof(double);
+    const size_t X = nx * sizeof(double), Y = ny * sizeof(double);
+    int e = 0;
+    e |= xdeg.ensure(X) | ydeg.ensure(Y) | xs.ensure(X) | ys.ensure(Y) | cosy.ensure(Y) |
+         siny.ensure(Y);
+    e |= a.ensure(N) | b.ensure(N) | c.ensure(N) | fun.ensure(N) | f2.ensure(N) |
+         disx.ensure(N) | disy.ensure(N) | A.ensure(N) | B.ensure(N) | C.ensure(N) |
+         V.ensure(N);
+    return e ? SURFATT_OOM : SURFATT_OK;
+  }
+  void release() {
+    for (DBuf* d : {&xdeg, &ydeg, &xs, &ys, &cosy, &siny, &a, &b, &c, &fun, &f2, &disx, &disy,
+                    &A, &B, &C, &V})
+      d->release();
+  }
+  PrepOut out() {
+    return PrepOut{xs.as<double>(), ys.as<double>(), cosy.as<double>(), siny.as<double>(),
+                   a.as<double>(), b.as<double>(), c.as<double>(), fun.as<double>(),
+                   f2.as<double>(), disx.as<double>(), disy.as<double>()};
+  }
+  PeriodDev dev(int nx, int ny, int lonlat, double dx, double dy, const double* svel) {
+    PeriodDev P;
+    P.nx = nx;
+    P.ny = ny;
+    P.lonlat = lonlat;
+    P.dx = dx;
+    P.dy = dy;
+    P.xs = xs.as<double>();
+    P.ys = ys.as<double>();
+    P.xdeg = xdeg.as<double>();
+    P.ydeg = ydeg.as<double>();
+    P.cosy = cosy.as<double>();
+    P.siny = siny.as<double>();
+    P.a = a.as<double>();
+    P.b = b.as<double>();
+    P.c = c.as<double>();
+    P.fun = fun.as<double>();
+    P.f2 = f2.as<double>();
+    P.disx = disx.as<double>();
+    P.disy = disy.as<double>();
+    P.svel = svel;
+    P.goff = 0;
+    return P;
+  }
+};
+
+struct ThreadCtx {
+  bool init = false;
+  cudaStream_t st = nullptr;
+  PeriodBufs pb;
+  DBuf ws, T, Ta, rx, ry, sa, out, si;
+  int* si_host = nullptr;  // pinned {status, iters}
+  ~ThreadCtx() {
+    if (!init) return;
+    pb.release();
+    for (DBuf* d : {&ws, &T, &Ta, &rx, &ry, &sa, &out, &si}) d->release();
+    if (si_host) cudaFreeHost(si_host);
+    if (st) cudaStreamDestroy(st);
+  }
+  int setup() {
+    if (init) return SURFATT_OK;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SURFATT_CUDA_ERROR;
+    if (cudaMallocHost(&si_host, 4 * sizeof(int)) != cudaSuccess) return SURFATT_CUDA_ERROR;
+    init = true;
+    return SURFATT_OK;
+  }
+};
+
+thread_local ThreadCtx g_ctx;
+
+int record(int st, int iters) {
+  g_last_status = st;
+  g_last_iters = iters;
+  return st;
+}
+
+// Upload one grid + fields and run the per-period precompute.
+// conv: coordinates are degrees on a sphere (lon/lat) or Cartesian.
+int prep_single(ThreadCtx& c, const double* xx, const double* yy, int nx, int ny, const double* A,
+                const double* B, const double* C, const double* V, int lonlat, int from_model,
+                PeriodDev* P) {
+  const size_t N = (size_t)nx * ny;
+  if (c.pb.ensure(nx, ny)) return SURFATT_OOM;
+  CK(cudaMemcpyAsync(c.pb.xdeg.p, xx, nx * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.pb.ydeg.p, yy, ny * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.pb.A.p, A, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.pb.B.p, B, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.pb.C.p, C, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  if (V) CK(cudaMemcpyAsync(c.pb.V.p, V, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  else CK(cudaMemsetAsync(c.pb.V.p, 0, N * sizeof(double), c.st));
+  PrepIn in{nx, ny, lonlat, c.pb.xdeg.as<double>(), c.pb.ydeg.as<double>(), c.pb.A.as<double>(),
+            c.pb.B.as<double>(), c.pb.C.as<double>(), c.pb.V.as<double>(), from_model};
+  launch_prep(in, c.pb.out(), c.st);
+  CK(cudaGetLastError());
+  // dx, dy in sweep units: xx(2)-xx(1) after the same conversion as the device
+  double dx, dy;
+  if (lonlat) {
+    dx = xx[1] / 180.0 * PI_S - xx[0] / 180.0 * PI_S;
+    dy = yy[1] / 180.0 * PI_S - yy[0] / 180.0 * PI_S;
+  } else {
+    dx = xx[1] - xx[0];
+    dy = yy[1] - yy[0];
+  }
+  *P = c.pb.dev(nx, ny, lonlat, dx, dy, nullptr);
+  return SURFATT_OK;
+}
+
+int finish_single(ThreadCtx& c, double* out_host, size_t n, const DBuf& out_dev) {
+  CK(cudaMemcpyAsync(c.si_host, c.si.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  if (out_host)
+    CK(cudaMemcpyAsync(out_host, out_dev.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  return SURFATT_OK;
+}
+
+void boundary_stop(double x0, double y0) {
+  if (!g_exit_on_boundary) return;
+  // src/eikon_solver_2d.f90:863-867: print and `stop`
+  std::printf(" source on the boundary, mesh error\n");
+  std::printf(" %24.16E %24.16E\n", x0, y0);
+  std::fflush(stdout);
+  std::exit(0);
+}
+
+int uw_dropin(const double* xx, const double* yy, int nx, int ny, const double* A,
+              const double* B, const double* C, double* T, const double* fun, double x0,
+              double y0, int lonlat, int weno, int multi) {
+  if (!xx || !yy || !A || !B || !C || !T || !fun || nx < (weno ? 4 : 2) || ny < (weno ? 4 : 2))
+    return record(SURFATT_BAD_ARG, 0);
+  ThreadCtx& c = g_ctx;
+  int e = c.setup();
+  if (e) return record(e, 0);
+  PeriodDev P;
+  e = prep_single(c, xx, yy, nx, ny, A, B, C, fun, lonlat, 0, &P);
+  if (e) return record(e, 0);
+  const size_t N = (size_t)nx * ny;
+  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.out.ensure(N * sizeof(double)) ||
+      c.si.ensure(4 * sizeof(int)))
+    return record(SURFATT_OOM, 0);
+  const double xs0 = lonlat ? x0 / 180.0 * PI_S : x0;
+  const double ys0 = lonlat ? y0 / 180.0 * PI_S : y0;
+  if (weno)
+    launch_weno_single(P, xs0, ys0, multi, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+  else
+    launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+  if (cudaGetLastError() != cudaSuccess) return record(SURFATT_CUDA_ERROR, 0);
+  e = finish_single(c, nullptr, 0, c.out);
+  if (e) return record(e, 0);
+  const int st = c.si_host[0], it = c.si_host[1];
+  if (st == SURFATT_SOURCE_ON_BOUNDARY) {
+    boundary_stop(xs0, ys0);
+    return record(st, 0);
+  }
+  if (st == SURFATT_OK || st == SURFATT_NOT_CONVERGED) {
+    if (cudaMemcpy(T, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return record(SURFATT_CUDA_ERROR, 0);
+  }
+  return record(st, it);
+}
+
+int jse_dropin(const double* xx, const double* yy, int nx, int ny, const double* A,
+               const double* B, const double* C, const double* T, double* Ta, const double* xr,
+               const double* yr, const double* sadj, int nr, int lonlat) {
+  if (!xx || !yy || !A || !B || !C || !T || !Ta || nx < 3 || ny < 3 || nr < 0 ||
+      (nr > 0 && (!xr || !yr || !sadj)))
+    return record(SURFATT_BAD_ARG, 0);
+  ThreadCtx& c = g_ctx;
+  int e = c.setup();
+  if (e) return record(e, 0);
+  PeriodDev P;
+  e = prep_single(c, xx, yy, nx, ny, A, B, C, nullptr, lonlat, 0, &P);
+  if (e) return record(e, 0);
+  const size_t N = (size_t)nx * ny;
+  const size_t R = (size_t)(nr > 0 ? nr : 1) * sizeof(double);
+  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.T.ensure(N * sizeof(double)) ||
+      c.out.ensure(N * sizeof(double)) || c.rx.ensure(R) || c.ry.ensure(R) || c.sa.ensure(R) ||
+      c.si.ensure(4 * sizeof(int)))
+    return record(SURFATT_OOM, 0);
+  if (cudaMemcpyAsync(c.T.p, T, N * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
+      (nr > 0 && (cudaMemcpyAsync(c.rx.p, xr, nr * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
+                  cudaMemcpyAsync(c.ry.p, yr, nr * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
+                  cudaMemcpyAsync(c.sa.p, sadj, nr * sizeof(double), cudaMemcpyHostToDevice, c.st))))
+    return record(SURFATT_CUDA_ERROR, 0);
+  launch_jse_single(P, c.T.as<double>(), c.rx.as<double>(), c.ry.as<double>(), c.sa.as<double>(),
+                    nr, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+  if (cudaGetLastError() != cudaSuccess) return record(SURFATT_CUDA_ERROR, 0);
+  e = finish_single(c, nullptr, 0, c.out);
+  if (e) return record(e, 0);
+  const int st = c.si_host[0], it = c.si_host[1];
+  if (st == SURFATT_OK || st == SURFATT_NOT_CONVERGED)
+    if (cudaMemcpy(Ta, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return record(SURFATT_CUDA_ERROR, 0);
+  return record(st, it);
+}
+
+int mask_dropin(const double* xx, const double* yy, int nx, int ny, double* tab, double x0,
+                double y0) {
+  if (!xx || !yy || !tab || nx < 2 || ny < 2) return record(SURFATT_BAD_ARG, 0);
+  ThreadCtx& c = g_ctx;
+  int e = c.setup();
+  if (e) return record(e, 0);
+  const size_t N = (size_t)nx * ny;
+  if (c.pb.ensure(nx, ny) || c.out.ensure(N * sizeof(double))) return record(SURFATT_OOM, 0);
+  if (cudaMemcpyAsync(c.pb.xdeg.p, xx, nx * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
+      cudaMemcpyAsync(c.pb.ydeg.p, yy, ny * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
+      cudaMemcpyAsync(c.out.p, tab, N * sizeof(double), cudaMemcpyHostToDevice, c.st))
+    return record(SURFATT_CUDA_ERROR, 0);
+  PeriodDev P = c.pb.dev(nx, ny, 0, 0, 0, nullptr);
+  launch_mask_single(P, c.out.as<double>(), x0, y0, c.st);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(tab, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
+      cudaStreamSynchronize(c.st))
+    return record(SURFATT_CUDA_ERROR, 0);
+  return record(SURFATT_OK, 0);
+}
+
+}  // namespace
+
+// ===========================================================================
+// 1. Drop-in symbols
+// ===========================================================================
+extern "C" {
+
+void fsm_uw_ps_lonlat_2d_(const double* xx_deg, const double* yy_deg, const int* nx,
+                          const int* ny, const double* spha, const double* sphb,
+                          const double* sphc, double* T, const double* fun,
+                          const double* x0_deg, const double* y0_deg, const double* /*u*/) {
+  uw_dropin(xx_deg, yy_deg, *nx, *ny, spha, sphb, sphc, T, fun, *x0_deg, *y0_deg, 1, 0, 0);
+}
+
+void fsm_uw_ps_cart_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                        const double* a, const double* b, const double* c, double* T,
+                        const double* fun, const double* x0, const double* y0,
+                        const double* /*u*/) {
+  uw_dropin(xx, yy, *nx, *ny, a, b, c, T, fun, *x0, *y0, 0, 0, 0);
+}
+
+void fsm_weno3_ps_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                      const double* a, const double* b, const double* c, double* T,
+                      const double* fun, const double* x0, const double* y0, const double* /*u*/) {
+  uw_dropin(xx, yy, *nx, *ny, a, b, c, T, fun, *x0, *y0, 0, 1, 0);
+}
+
+void fsm_weno3_ps_multi_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                            const double* a, const double* b, const double* c, double* T,
+                            const double* fun, const double* x0, const double* y0,
+                            const double* /*u*/) {
+  uw_dropin(xx, yy, *nx, *ny, a, b, c, T, fun, *x0, *y0, 0, 1, 1);
+}
+
+void fsm_o1_jse_lonlat_2d_(const double* xx_deg, const double* yy_deg, const int* nx,
+                           const int* ny, const double* spha, const double* sphb,
+                           const double* sphc, const double* T, double* Ta,
+                           const double* xrec_deg, const double* yrec_deg,
+                           const double* sourceAdj, const int* nr) {
+  jse_dropin(xx_deg, yy_deg, *nx, *ny, spha, sphb, sphc, T, Ta, xrec_deg, yrec_deg, sourceAdj,
+             *nr, 1);
+}
+
+void fsm_o1_jse_2d_(const double* xx, const double* yy, const int* nx, const int* ny,
+                    const double* a, const double* b, const double* c, const double* T,
+                    double* Ta, const double* xrec, const double* yrec,
+                    const double* sourceAdj, const int* nr) {
+  jse_dropin(xx, yy, *nx, *ny, a, b, c, T, Ta, xrec, yrec, sourceAdj, *nr, 0);
+}
+
+void mask_(const double* xx, const double* yy, const int* nx, const int* ny, double* TableAdj,
+           const double* x0, const double* y0) {
+  mask_dropin(xx, yy, *nx, *ny, TableAdj, *x0, *y0);
+}
+
+int surfatt_last_status(void) { return g_last_status; }
+int surfatt_last_iterations(void) { return g_last_iters; }
+void surfatt_set_exit_on_boundary(int enable) { g_exit_on_boundary = enable; }
+const char* surfatt_version(void) { return "surfatt_gb300 0.1 (sm_103a)"; }
+
+// ===========================================================================
+// 2. Measurement layer (src/measadj.f90)
+// ===========================================================================
+surfatt_status_t surfatt_measadj_run_forward(const double* xgrids, const double* ygrids,
+                                             int nx, int ny, const double* vel2d,
+                                             const double* m11, const double* m22,
+                                             const double* m12, double srcx, double srcy,
+                                             int nrec, const double* recx, const double* recy,
+                                             const double* tt, const double* weight,
+                                             double* timetable, double* tekio, double* chi) {
+  if (!vel2d || !m11 || !m22 || !m12 || !timetable || nrec < 0 ||
+      (nrec > 0 && (!recx || !recy || !tt || !weight || !tekio)) || !chi || nx < 2 || ny < 2)
+    return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+  ThreadCtx& c = g_ctx;
+  int e = c.setup();
+  if (e) return (surfatt_status_t)record(e, 0);
+  PeriodDev P;
+  e = prep_single(c, xgrids, ygrids, nx, ny, m11, m22, m12, vel2d, 1, 1, &P);
+  if (e) return (surfatt_status_t)record(e, 0);
+  const size_t N = (size_t)nx * ny;
+  const size_t R = (size_t)(nrec > 0 ? nrec : 1) * sizeof(double);
+  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.out.ensure(N * sizeof(double)) ||
+      c.si.ensure(4 * sizeof(int)) || c.rx.ensure(R) || c.ry.ensure(R) || c.sa.ensure(R))
+    return (surfatt_status_t)record(SURFATT_OOM, 0);
+  const double xs0 = srcx / 180.0 * PI_S, ys0 = srcy / 180.0 * PI_S;
+  launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+  if (cudaMemsetAsync(c.si.as<int>() + 2, 0, sizeof(int), c.st) != cudaSuccess)
+    return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
+  if (nrec > 0) {
+    if (cudaMemcpyAsync(c.rx.p, recx, nrec * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
+        cudaMemcpyAsync(c.ry.p, recy, nrec * sizeof(double), cudaMemcpyHostToDevice, c.st))
+      return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
+    launch_interp(P, c.out.as<double>(), nrec, c.rx.as<double>(), c.ry.as<double>(),
+                  c.sa.as<double>(), c.si.as<int>() + 2, c.st);
+  }
+  if (cudaGetLastError() != cudaSuccess) return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
+  if (cudaMemcpyAsync(c.si_host, c.si.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, c.st) ||
+      cudaMemcpyAsync(timetable, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
+      (nrec > 0 && cudaMemcpyAsync(tekio, c.sa.p, nrec * sizeof(double), cudaMemcpyDeviceToHost, c.st)) ||
+      cudaStreamSynchronize(c.st))
+    return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
+  int st = c.si_host[0];
+  if (st == SURFATT_SOURCE_ON_BOUNDARY) return (surfatt_status_t)record(st, 0);
+  if (nrec > 0 && c.si_host[2] != 0 && st == SURFATT_OK) st = SURFATT_BAD_ARG;
+  // chi = 0.5*sum(weight*(tekio-tt)**2): a scalar of the receivers, summed in
+  // receiver order on the host side of the call, as the reference does
+  double s = 0;
+  for (int i = 0; i < nrec; ++i) {
+    const double d = tekio[i] - tt[i];
+    s = s + weight[i] * (d * d);
+  }
+  *chi = 0.5 * s;
+  return (surfatt_status_t)record(st, c.si_host[1]);
+}
+
+surfatt_status_t surfatt_measadj_run_adjoint(const double* xgrids, const double* ygrids,
+                                             int nx, int ny, const double* m11,
+                                             const double* m22, const double* m12,
+                                             double srcx, double srcy, int nrec,
+                                             const double* recx, const double* recy,
+                                             const double* tt, const double* tekio,
+                                             double* weight, const double* timetable,
+                                             double* adjtable) {
+  if (nrec < 0 || (nrec > 0 && (!tt || !tekio || !weight)) || !m12)
+    return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+  std::vector<double> sadj((size_t)(nrec > 0 ? nrec : 1)), nm12((size_t)nx * ny);
+  for (int i = 0; i < nrec; ++i)
+    if (std::fabs(tekio[i] - tt[i]) / tt[i] > 0.5) weight[i] = 0.;
+  for (int i = 0; i < nrec; ++i) sadj[i] = weight[i] * (tekio[i] - tt[i]);
+  for (size_t k = 0; k < nm12.size(); ++k) nm12[k] = -m12[k];
+  int st = jse_dropin(xgrids, ygrids, nx, ny, m11, m22, nm12.data(), timetable, adjtable, recx,
+                      recy, sadj.data(), nrec, 1);
+  if (st != SURFATT_OK && st != SURFATT_NOT_CONVERGED) return (surfatt_status_t)st;
+  const int it = g_last_iters;
+  int sm = mask_dropin(xgrids, ygrids, nx, ny, adjtable, srcx, srcy);
+  if (sm != SURFATT_OK) return (surfatt_status_t)sm;
+  return (surfatt_status_t)record(st, it);
+}
+
+surfatt_status_t surfatt_measadj_run_adjoint_density(
+    const double* xgrids, const double* ygrids, int nx, int ny, const double* m11,
+    const double* m22, const double* m12, double srcx, double srcy, int nrec,
+    const double* recx, const double* recy, const double* weight, const double* timetable,
+    double* density) {
+  if (nrec < 0 || (nrec > 0 && !weight) || !m12) return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+  std::vector<double> sadj((size_t)(nrec > 0 ? nrec : 1)), nm12((size_t)nx * ny);
+  for (int i = 0; i < nrec; ++i) sadj[i] = -1.0 * weight[i];
+  for (size_t k = 0; k < nm12.size(); ++k) nm12[k] = -m12[k];
+  int st = jse_dropin(xgrids, ygrids, nx, ny, m11, m22, nm12.data(), timetable, density, recx,
+                      recy, sadj.data(), nrec, 1);
+  if (st != SURFATT_OK && st != SURFATT_NOT_CONVERGED) return (surfatt_status_t)st;
+  const int it = g_last_iters;
+  int sm = mask_dropin(xgrids, ygrids, nx, ny, density, srcx, srcy);
+  if (sm != SURFATT_OK) return (surfatt_status_t)sm;
+  return (surfatt_status_t)record(st, it);
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// 3. Batched engine
+// ===========================================================================
+struct surfatt_engine {
+  int device = 0;
+  size_t budget = 0;
+  size_t allocated = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  bool loaded = false, ran = false;
+  int last_mode = 0, launches = 0;
+  // problem shape (host)
+  int nperiod = 0, nsolve = 0, npath = 0, nrec_total = 0;
+  long long ncell = 0, kslot_total = 0, max_cells = 0;
+  std::vector<int> nx, ny, pidx, nrec;
+  std::vector<long long> goff, xoff, yoff;
+  std::vector<PeriodDev> periods;
+  std::vector<int> order, plist_off, plist;
+  std::vector<long long> kslot;
+  // device buffers
+  DBuf d_periods, d_xdeg, d_ydeg, d_xs, d_ys, d_cosy, d_siny, d_A, d_B, d_C, d_V, d_a, d_b, d_c,
+      d_fun, d_f2, d_disx, d_disy, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
+      d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
+  DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
+      d_fupd, d_aupd, d_ws, d_queue;
+  int grid = 0, block = 128;
+  std::vector<DBuf*> all() {
+    return {&d_periods, &d_xdeg, &d_ydeg, &d_xs, &d_ys, &d_cosy, &d_siny, &d_A, &d_B, &d_C,
+            &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_pidx, &d_srcx, &d_srcy,
+            &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
+            &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
+            &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
+            &d_aupd, &d_ws, &d_queue};
+  }
+};
+
+namespace {
+
+int eng_ensure(surfatt_engine* e, DBuf& b, size_t bytes) {
+  b.counter = &e->allocated;
+  if (bytes <= b.cap) return SURFATT_OK;
+  if (e->budget && e->allocated - b.cap + bytes > e->budget) return SURFATT_OOM;
+  return b.ensure(bytes);
+}
+
+template <class T>
+int up(surfatt_engine* e, DBuf& b, const T* src, size_t n) {
+  int r = eng_ensure(e, b, (n ? n : 1) * sizeof(T));
+  if (r) return r;
+  if (n && src) CK(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, e->st));
+  return SURFATT_OK;
+}
+
+int run_prep_all(surfatt_engine* e) {
+  for (int p = 0; p < e->nperiod; ++p) {
+    const long long g = e->goff[p];
+    PrepIn in{e->nx[p], e->ny[p], 1, e->d_xdeg.as<double>() + e->xoff[p],
+              e->d_ydeg.as<double>() + e->yoff[p], e->d_A.as<double>() + g,
+              e->d_B.as<double>() + g, e->d_C.as<double>() + g, e->d_V.as<double>() + g, 1};
+    PrepOut out{e->d_xs.as<double>() + e->xoff[p], e->d_ys.as<double>() + e->yoff[p],
+                e->d_cosy.as<double>() + e->yoff[p], e->d_siny.as<double>() + e->yoff[p],
+                e->d_a.as<double>() + g, e->d_b.as<double>() + g, e->d_c.as<double>() + g,
+                e->d_fun.as<double>() + g, e->d_f2.as<double>() + g,
+                e->d_disx.as<double>() + g, e->d_disy.as<double>() + g};
+    launch_prep(in, out, e->st);
+  }
+  CK(cudaGetLastError());
+  return SURFATT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+surfatt_status_t surfatt_engine_create(surfatt_engine_t** out, int device, size_t budget) {
+  if (!out) return SURFATT_BAD_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return SURFATT_CUDA_ERROR;
+  }
+  CK(cudaSetDevice(device));
+  auto* e = new surfatt_engine();
+  e->device = device;
+  e->budget = budget;
+  if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess ||
+      cudaEventCreate(&e->evk0) != cudaSuccess || cudaEventCreate(&e->evk1) != cudaSuccess) {
+    delete e;
+    return SURFATT_CUDA_ERROR;
+  }
+  *out = e;
+  return SURFATT_OK;
+}
+
+void surfatt_engine_destroy(surfatt_engine_t* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  cudaStreamSynchronize(e->st);
+  for (DBuf* b : e->all()) b->release();
+  cudaEventDestroy(e->ev0);
+  cudaEventDestroy(e->ev1);
+  cudaEventDestroy(e->evk0);
+  cudaEventDestroy(e->evk1);
+  cudaStreamDestroy(e->st);
+  delete e;
+}
+
+surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_t* pb) {
+  if (!e || !pb || pb->nperiod < 1 || pb->nsolve < 0) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  e->loaded = false;
+  e->ran = false;
+  const int np = pb->nperiod, ns = pb->nsolve;
+  e->nperiod = np;
+  e->nsolve = ns;
+  e->npath = pb->npath;
+  e->nx.assign(pb->nx, pb->nx + np);
+  e->ny.assign(pb->ny, pb->ny + np);
+  e->goff.assign(pb->goff, pb->goff + np);
+  e->xoff.assign(pb->xoff, pb->xoff + np);
+  e->yoff.assign(pb->yoff, pb->yoff + np);
+  e->pidx.assign(pb->pidx, pb->pidx + ns);
+  e->nrec.assign(pb->nrec, pb->nrec + ns);
+  long long nxs = 0, nys = 0;
+  e->ncell = 0;
+  e->max_cells = 0;
+  for (int p = 0; p < np; ++p) {
+    if (e->nx[p] < 3 || e->ny[p] < 3) return SURFATT_BAD_ARG;
+    const long long N = (long long)e->nx[p] * e->ny[p];
+    e->ncell = std::max(e->ncell, e->goff[p] + N);
+    e->max_cells = std::max(e->max_cells, N);
+    nxs = std::max(nxs, e->xoff[p] + e->nx[p]);
+    nys = std::max(nys, e->yoff[p] + e->ny[p]);
+  }
+  int nrec_total = 0;
+  for (int s = 0; s < ns; ++s) {
+    if (e->pidx[s] < 0 || e->pidx[s] >= np || e->nrec[s] < 0) return SURFATT_BAD_ARG;
+    nrec_total = std::max(nrec_total, pb->rec_off[s] + e->nrec[s]);
+  }
+  for (int r = 0; r < nrec_total; ++r)
+    if (pb->path[r] < 0 || pb->path[r] >= pb->npath) return SURFATT_BAD_ARG;
+  e->nrec_total = nrec_total;
+  // processing order: largest grids first (longest-processing-time first)
+  e->order.resize(ns);
+  std::iota(e->order.begin(), e->order.end(), 0);
+  std::stable_sort(e->order.begin(), e->order.end(), [&](int a, int b) {
+    return (long long)e->nx[e->pidx[a]] * e->ny[e->pidx[a]] >
+           (long long)e->nx[e->pidx[b]] * e->ny[e->pidx[b]];
+  });
+  // per-period solve lists in work-list order, kernel slots per solve
+  e->plist_off.assign(np + 1, 0);
+  for (int s = 0; s < ns; ++s) e->plist_off[e->pidx[s] + 1]++;
+  for (int p = 0; p < np; ++p) e->plist_off[p + 1] += e->plist_off[p];
+  e->plist.assign(ns, 0);
+  {
+    std::vector<int> fill(e->plist_off.begin(), e->plist_off.end() - 1);
+    for (int s = 0; s < ns; ++s) e->plist[fill[e->pidx[s]]++] = s;
+  }
+  e->kslot.assign(ns, 0);
+  long long acc = 0;
+  for (int s = 0; s < ns; ++s) {
+    e->kslot[s] = acc;
+    acc += (long long)e->nx[e->pidx[s]] * e->ny[e->pidx[s]];
+  }
+  e->kslot_total = acc;
+  const size_t NC = (size_t)e->ncell;
+  int r = 0;
+  r |= up(e, e->d_xdeg, pb->xgrid, nxs) | up(e, e->d_ydeg, pb->ygrid, nys);
+  r |= up(e, e->d_xs, (double*)nullptr, nxs) | up(e, e->d_ys, (double*)nullptr, nys);
+  r |= up(e, e->d_cosy, (double*)nullptr, nys) | up(e, e->d_siny, (double*)nullptr, nys);
+  r |= up(e, e->d_A, pb->m11, NC) | up(e, e->d_B, pb->m22, NC) | up(e, e->d_C, pb->m12, NC) |
+       up(e, e->d_V, pb->svel, NC);
+  for (DBuf* b : {&e->d_a, &e->d_b, &e->d_c, &e->d_fun, &e->d_f2, &e->d_disx, &e->d_disy})
+    r |= up(e, *b, (double*)nullptr, NC);
+  r |= up(e, e->d_pidx, pb->pidx, ns) | up(e, e->d_srcx, pb->srcx, ns) |
+       up(e, e->d_srcy, pb->srcy, ns) | up(e, e->d_rec_off, pb->rec_off, ns) |
+       up(e, e->d_nrec, pb->nrec, ns);
+  r |= up(e, e->d_recx, pb->recx, nrec_total) | up(e, e->d_recy, pb->recy, nrec_total) |
+       up(e, e->d_tt, pb->tt, nrec_total) | up(e, e->d_weight, pb->weight, nrec_total) |
+       up(e, e->d_path, pb->path, nrec_total);
+  r |= up(e, e->d_order, e->order.data(), ns) | up(e, e->d_plist_off, e->plist_off.data(), np + 1) |
+       up(e, e->d_plist, e->plist.data(), ns) | up(e, e->d_kslot, e->kslot.data(), ns) |
+       up(e, e->d_goff, e->goff.data(), np) | up(e, e->d_nx, e->nx.data(), np) |
+       up(e, e->d_ny, e->ny.data(), np);
+  // outputs
+  r |= up(e, e->d_tekio, (double*)nullptr, nrec_total) | up(e, e->d_wgt, (double*)nullptr, nrec_total) |
+       up(e, e->d_ttfwd, (double*)nullptr, std::max(1, pb->npath)) |
+       up(e, e->d_chis, (double*)nullptr, ns) | up(e, e->d_chi, (double*)nullptr, 1) |
+       up(e, e->d_kc, (double*)nullptr, e->kslot_total) |
+       up(e, e->d_kcd, (double*)nullptr, e->kslot_total) | up(e, e->d_adj, (double*)nullptr, NC) |
+       up(e, e->d_adjd, (double*)nullptr, NC) | up(e, e->d_status, (int*)nullptr, ns) |
+       up(e, e->d_fit, (int*)nullptr, ns) | up(e, e->d_ait, (int*)nullptr, ns) |
+       up(e, e->d_fupd, (double*)nullptr, ns) | up(e, e->d_aupd, (double*)nullptr, ns) |
+       up(e, e->d_queue, (int*)nullptr, 1);
+  if (r & SURFATT_CUDA_ERROR) return SURFATT_CUDA_ERROR;
+  if (r) return SURFATT_OOM;
+  // per-period descriptors
+  e->periods.resize(np);
+  for (int p = 0; p < np; ++p) {
+    PeriodDev& P = e->periods[p];
+    const long long g = e->goff[p];
+    P.nx = e->nx[p];
+    P.ny = e->ny[p];
+    P.lonlat = 1;
+    const double* xg = pb->xgrid + e->xoff[p];
+    const double* yg = pb->ygrid + e->yoff[p];
+    P.dx = xg[1] / 180.0 * PI_S - xg[0] / 180.0 * PI_S;
+    P.dy = yg[1] / 180.0 * PI_S - yg[0] / 180.0 * PI_S;
+    P.xs = e->d_xs.as<double>() + e->xoff[p];
+    P.ys = e->d_ys.as<double>() + e->yoff[p];
+    P.xdeg = e->d_xdeg.as<double>() + e->xoff[p];
+    P.ydeg = e->d_ydeg.as<double>() + e->yoff[p];
+    P.cosy = e->d_cosy.as<double>() + e->yoff[p];
+    P.siny = e->d_siny.as<double>() + e->yoff[p];
+    P.a = e->d_a.as<double>() + g;
+    P.b = e->d_b.as<double>() + g;
+    P.c = e->d_c.as<double>() + g;
+    P.fun = e->d_fun.as<double>() + g;
+    P.f2 = e->d_f2.as<double>() + g;
+    P.disx = e->d_disx.as<double>() + g;
+    P.disy = e->d_disy.as<double>() + g;
+    P.svel = e->d_V.as<double>() + g;
+    P.goff = g;
+  }
+  r = up(e, e->d_periods, e->periods.data(), np);
+  if (r) return (surfatt_status_t)r;
+  r = run_prep_all(e);
+  if (r) return (surfatt_status_t)r;
+  e->loaded = true;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_update_velocity(surfatt_engine_t* e, const double* svel) {
+  if (!e || !e->loaded || !svel) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaMemcpyAsync(e->d_V.p, svel, (size_t)e->ncell * sizeof(double), cudaMemcpyHostToDevice,
+                     e->st));
+  return (surfatt_status_t)run_prep_all(e);
+}
+
+surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
+                                    surfatt_precision_t prec) {
+  if (!e || !e->loaded) return SURFATT_BAD_ARG;
+  if (mode != SURFATT_MODE_FORWARD && mode != SURFATT_MODE_2D && mode != SURFATT_MODE_3D)
+    return SURFATT_BAD_ARG;
+  if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, e->device));
+  const int block = e->block;
+  int per_sm = prec == SURFATT_PREC_FP64 ? batch_fp64_max_blocks_per_sm(block)
+                                         : batch_fp32_max_blocks_per_sm(block);
+  if (per_sm < 1) per_sm = 1;
+  int grid = prop.multiProcessorCount * per_sm;
+  if (grid > e->nsolve) grid = std::max(1, e->nsolve);
+  const long long wsd = prec == SURFATT_PREC_FP64 ? batch_fp64_ws_doubles(e->max_cells)
+                                                 : batch_fp32_ws_doubles(e->max_cells);
+  int r = eng_ensure(e, e->d_ws, (size_t)grid * wsd * sizeof(double));
+  if (r) return (surfatt_status_t)r;
+  e->grid = grid;
+  BatchArgs A;
+  A.periods = e->d_periods.as<PeriodDev>();
+  A.nsolve = e->nsolve;
+  A.order = e->d_order.as<int>();
+  A.pidx = e->d_pidx.as<int>();
+  A.srcx = e->d_srcx.as<double>();
+  A.srcy = e->d_srcy.as<double>();
+  A.rec_off = e->d_rec_off.as<int>();
+  A.nrec = e->d_nrec.as<int>();
+  A.recx = e->d_recx.as<double>();
+  A.recy = e->d_recy.as<double>();
+  A.tt = e->d_tt.as<double>();
+  A.weight = e->d_weight.as<double>();
+  A.path = e->d_path.as<int>();
+  A.kslot = e->d_kslot.as<long long>();
+  A.mode = mode;
+  A.tekio = e->d_tekio.as<double>();
+  A.wgt_eff = e->d_wgt.as<double>();
+  A.tt_fwd = e->d_ttfwd.as<double>();
+  A.chi = e->d_chis.as<double>();
+  A.kcontrib = e->d_kc.as<double>();
+  A.kcontrib_den = e->d_kcd.as<double>();
+  A.status = e->d_status.as<int>();
+  A.fwd_iters = e->d_fit.as<int>();
+  A.adj_iters = e->d_ait.as<int>();
+  A.fwd_updates = e->d_fupd.as<double>();
+  A.adj_updates = e->d_aupd.as<double>();
+  A.Tout = nullptr;
+  A.ws = e->d_ws.as<double>();
+  A.ws_doubles = wsd;
+  A.queue = e->d_queue.as<int>();
+  A.block = block;
+  e->launches = 0;
+  CK(cudaEventRecord(e->ev0, e->st));
+  CK(cudaMemsetAsync(e->d_queue.p, 0, sizeof(int), e->st));
+  CK(cudaMemsetAsync(e->d_ttfwd.p, 0, std::max(1, e->npath) * sizeof(double), e->st));
+  CK(cudaMemsetAsync(e->d_aupd.p, 0, std::max(1, e->nsolve) * sizeof(double), e->st));
+  CK(cudaEventRecord(e->evk0, e->st));
+  if (e->nsolve > 0) {
+    if (prec == SURFATT_PREC_FP64) launch_batch_fp64(A, grid, block, e->st);
+    else launch_batch_fp32(A, grid, block, e->st);
+    e->launches++;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(e->evk1, e->st));
+  if (mode >= 2) {
+    launch_kernel_reduce(nullptr, e->nperiod, e->d_plist_off.as<int>(), e->d_plist.as<int>(),
+                         e->d_kslot.as<long long>(), e->d_kc.as<double>(), e->d_adj.as<double>(),
+                         e->ncell, e->d_goff.as<long long>(), e->d_nx.as<int>(),
+                         e->d_ny.as<int>(), e->st);
+    e->launches++;
+    if (mode == 3) {
+      launch_kernel_reduce(nullptr, e->nperiod, e->d_plist_off.as<int>(), e->d_plist.as<int>(),
+                           e->d_kslot.as<long long>(), e->d_kcd.as<double>(),
+                           e->d_adjd.as<double>(), e->ncell, e->d_goff.as<long long>(),
+                           e->d_nx.as<int>(), e->d_ny.as<int>(), e->st);
+      e->launches++;
+    }
+  }
+  launch_chi_reduce(e->d_chis.as<double>(), e->nsolve, e->d_chi.as<double>(), e->st);
+  e->launches++;
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(e->ev1, e->st));
+  e->ran = true;
+  e->last_mode = mode;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_sync(surfatt_engine_t* e) {
+  if (!e || !e->ran) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->st));
+  std::vector<int> st(std::max(1, e->nsolve));
+  if (e->nsolve)
+    CK(cudaMemcpy(st.data(), e->d_status.p, e->nsolve * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int s = 0; s < e->nsolve; ++s)
+    if (st[s] != SURFATT_OK) return (surfatt_status_t)st[s];
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_results(surfatt_engine_t* e, surfatt_result_t* out) {
+  if (!e || !e->ran || !out) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  const size_t NC = (size_t)e->ncell;
+  if (out->adj_s) {
+    if (e->last_mode >= 2)
+      CK(cudaMemcpyAsync(out->adj_s, e->d_adj.p, NC * sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    else
+      std::memset(out->adj_s, 0, NC * sizeof(double));
+  }
+  if (out->adj_density) {
+    if (e->last_mode == 3)
+      CK(cudaMemcpyAsync(out->adj_density, e->d_adjd.p, NC * sizeof(double),
+                         cudaMemcpyDeviceToHost, e->st));
+    else
+      std::memset(out->adj_density, 0, NC * sizeof(double));
+  }
+  if (out->chi) CK(cudaMemcpyAsync(out->chi, e->d_chi.p, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+  if (out->tt_fwd && e->npath)
+    CK(cudaMemcpyAsync(out->tt_fwd, e->d_ttfwd.p, e->npath * sizeof(double), cudaMemcpyDeviceToHost, e->st));
+  if (out->status && e->nsolve)
+    CK(cudaMemcpyAsync(out->status, e->d_status.p, e->nsolve * sizeof(int), cudaMemcpyDeviceToHost, e->st));
+  if (out->fwd_iters && e->nsolve)
+    CK(cudaMemcpyAsync(out->fwd_iters, e->d_fit.p, e->nsolve * sizeof(int), cudaMemcpyDeviceToHost, e->st));
+  if (out->adj_iters && e->nsolve)
+    CK(cudaMemcpyAsync(out->adj_iters, e->d_ait.p, e->nsolve * sizeof(int), cudaMemcpyDeviceToHost, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_timing(surfatt_engine_t* e, double* total_ms,
+                                       double* solve_kernel_ms, int* launches) {
+  if (!e || !e->ran) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaEventSynchronize(e->ev1));
+  float a = 0, b = 0;
+  CK(cudaEventElapsedTime(&a, e->ev0, e->ev1));
+  CK(cudaEventElapsedTime(&b, e->evk0, e->evk1));
+  if (total_ms) *total_ms = a;
+  if (solve_kernel_ms) *solve_kernel_ms = b;
+  if (launches) *launches = e->launches;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_work(surfatt_engine_t* e, double* fwd, double* adj) {
+  if (!e || !e->ran) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->st));
+  std::vector<double> f(std::max(1, e->nsolve)), a(std::max(1, e->nsolve));
+  if (e->nsolve) {
+    CK(cudaMemcpy(f.data(), e->d_fupd.p, e->nsolve * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(a.data(), e->d_aupd.p, e->nsolve * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  double sf = 0, sa = 0;
+  for (int s = 0; s < e->nsolve; ++s) {
+    sf += f[s];
+    sa += a[s];
+  }
+  if (fwd) *fwd = sf;
+  if (adj) *adj = sa;
+  return SURFATT_OK;
+}
+
+}  // extern "C"

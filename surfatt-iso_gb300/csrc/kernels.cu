@@ -1,0 +1,414 @@
+// kernels.cu -- FP64 kernels: per-period precompute, the fused batched
+// (period, source) solve, ordered kernel / misfit reductions, and the
+// single-solve kernels behind the drop-in symbols.
+#include <cstdio>
+
+#include "kernels.cuh"
+#include "solver_fp64.cuh"
+#include "batch_tail.cuh"
+
+namespace sgb {
+
+// ---------------------------------------------------------------------------
+// Per-period precompute (one block row per period field).
+// lon/lat: xx = xx_deg/180.0*pi (:801-804); a = spha/(R^2 cos^2 y),
+// b = sphb/R^2, c = sphc/(R^2 cos y) (:817-821).  The one-sided `dis` terms
+// (:1014, :1055) are loop invariant and evaluated here exactly as written.
+// ---------------------------------------------------------------------------
+__global__ void k_prep(PrepIn in, PrepOut out) {
+  const int nx = in.nx, ny = in.ny;
+  const size_t N = (size_t)nx * ny;
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nthr = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = tid; i < (size_t)nx; i += nthr)
+    out.xs[i] = in.lonlat ? in.xdeg[i] / 180.0 * PI_S : in.xdeg[i];
+  for (size_t j = tid; j < (size_t)ny; j += nthr) {
+    const double y = in.lonlat ? in.ydeg[j] / 180.0 * PI_S : in.ydeg[j];
+    out.ys[j] = y;
+    if (in.lonlat) {
+      out.cosy[j] = cos(y);
+      out.siny[j] = sin(y);
+    }
+  }
+  for (size_t k = tid; k < N; k += nthr) {
+    const int j = (int)(k / nx);
+    double A = in.A[k], B = in.B[k], C = in.C[k], f;
+    if (in.from_model) {
+      C = -C;
+      f = 1. / in.V[k];
+    } else {
+      f = in.V[k];
+    }
+    double a = A, b = B, c = C;
+    if (in.lonlat) {
+      const double y = in.ydeg[j] / 180.0 * PI_S;
+      const double cy = cos(y);
+      a = A / (R_EARTH * R_EARTH * (cy * cy));
+      b = B / (R_EARTH * R_EARTH);
+      c = C / (R_EARTH * R_EARTH * cy);
+    }
+    out.a[k] = a;
+    out.b[k] = b;
+    out.c[k] = c;
+    out.fun[k] = f;
+    out.f2[k] = f * f;
+    out.disx[k] = sqrt(f * f * (b / (a * b - c * c)));
+    out.disy[k] = sqrt(f * f * (a / (a * b - c * c)));
+  }
+}
+
+void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st) {
+  const size_t N = (size_t)in.nx * in.ny;
+  int grid = (int)((N + 255) / 256);
+  if (grid < 1) grid = 1;
+  if (grid > 4096) grid = 4096;
+  k_prep<<<grid, 256, 0, st>>>(in, out);
+}
+
+// ---------------------------------------------------------------------------
+// Fused batched solve (FP64).  Persistent blocks pull solves from a device
+// work queue; each runs forward -> interp2 -> misfit -> adjoint(s) -> mask
+// -> kernel contribution for one (period, source).
+// ---------------------------------------------------------------------------
+long long batch_fp64_ws_doubles(long long N) {
+  // tau, tau_old, T0, T + max(forward constants, adjoint constants + 6 fields)
+  const long long fwd = (long long)KC_COUNT, adj = (long long)KA_COUNT + 6;
+  return (4 + (fwd > adj ? fwd : adj)) * N;
+}
+
+struct SolveLayout {
+  FwdWs fw;
+  AdjWs aw;
+  double* T;
+};
+
+__device__ inline SolveLayout carve(double* base, size_t N) {
+  SolveLayout L;
+  L.fw.tau = base;
+  L.fw.tau_old = base + N;
+  L.fw.T0 = base + 2 * N;
+  L.T = base + 3 * N;
+  L.fw.K = base + 4 * N;
+  L.aw.T = L.T;
+  L.aw.K = base + 4 * N;  // aliases the forward constants (dead by then)
+  double* f = base + 4 * N + KA_COUNT * N;
+  L.aw.delta[0] = f;
+  L.aw.delta[1] = f + N;
+  L.aw.Ta[0] = f + 2 * N;
+  L.aw.Ta[1] = f + 3 * N;
+  L.aw.old[0] = f + 4 * N;
+  L.aw.old[1] = f + 5 * N;
+  return L;
+}
+
+__global__ void __launch_bounds__(128) k_batch_fp64(BatchArgs A) {
+  __shared__ SolveShared sh;
+  __shared__ int next;
+  double* base = A.ws + (size_t)blockIdx.x * (size_t)A.ws_doubles;
+  for (;;) {
+    if (threadIdx.x == 0) next = atomicAdd(A.queue, 1);
+    __syncthreads();
+    const int q = next;
+    __syncthreads();
+    if (q >= A.nsolve) break;
+    const int s = A.order[q];
+    const PeriodDev P = A.periods[A.pidx[s]];
+    const size_t N = (size_t)P.nx * P.ny;
+    if (threadIdx.x == 0) sh.flag = ST_OK;
+    SolveLayout L = carve(base, N);
+    double x0 = A.srcx[s], y0 = A.srcy[s];
+    if (P.lonlat) {
+      x0 = x0 / 180.0 * PI_S;
+      y0 = y0 / 180.0 * PI_S;
+    }
+    fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, L.fw, true, sh);
+    if (sh.status != ST_OK) {
+      const int st = sh.status;
+      __syncthreads();
+      solve_fail(A, P, s, st);
+      continue;
+    }
+    uw_sweeps(P, L.fw, sh, MAXITER_UW);
+    const int fst = sh.status, fit = sh.iters;
+    for (size_t k = threadIdx.x; k < N; k += blockDim.x) L.T[k] = L.fw.tau[k] * L.fw.T0[k];
+    if (A.fwd_updates && threadIdx.x == 0) {
+      const Box b = sh.box;
+      const double frozen = (double)(b.i1 - b.i0 + 1) * (b.j1 - b.j0 + 1);
+      A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
+    }
+    __syncthreads();
+    solve_tail(A, P, s, L.T, L.aw, sh, fst, fit);
+  }
+}
+
+void launch_batch_fp64(const BatchArgs& a, int grid, int block, cudaStream_t st) {
+  k_batch_fp64<<<grid, block, 0, st>>>(a);
+}
+
+int batch_fp64_max_blocks_per_sm(int block) {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp64, block, 0);
+  return n;
+}
+
+// ---------------------------------------------------------------------------
+// Ordered reductions
+// ---------------------------------------------------------------------------
+__global__ void k_kernel_reduce(int nperiod, const int* plist_off, const int* plist,
+                                const long long* kslot, const double* contrib, double* out,
+                                const long long* goff, const int* nxs, const int* nys) {
+  const int p = blockIdx.y;
+  if (p >= nperiod) return;
+  const long long N = (long long)nxs[p] * nys[p];
+  const int s0 = plist_off[p], s1 = plist_off[p + 1];
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < N;
+       k += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int q = s0; q < s1; ++q) acc = acc + contrib[kslot[plist[q]] + k];
+    out[goff[p] + k] = acc;
+  }
+}
+
+void launch_kernel_reduce(const PeriodDev* /*periods_host*/, int nperiod, const int* plist_off,
+                          const int* plist, const long long* kslot, const double* contrib,
+                          double* out, long long /*ncell*/, const long long* goff_dev,
+                          const int* nx_dev, const int* ny_dev, cudaStream_t st) {
+  dim3 grid(64, nperiod);
+  k_kernel_reduce<<<grid, 256, 0, st>>>(nperiod, plist_off, plist, kslot, contrib, out,
+                                        goff_dev, nx_dev, ny_dev);
+}
+
+__global__ void k_chi_reduce(const double* chi_s, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double acc = 0.0;
+    for (int s = 0; s < n; ++s) acc = acc + chi_s[s];
+    *out = acc;
+  }
+}
+
+void launch_chi_reduce(const double* chi_s, int nsolve, double* chi_out, cudaStream_t st) {
+  k_chi_reduce<<<1, 32, 0, st>>>(chi_s, nsolve, chi_out);
+}
+
+// ---------------------------------------------------------------------------
+// WENO3 sweeps (FSM_WENO3_PS_2d :344-548, FSM_WENO3_PS_multi_2d :552-761)
+// ---------------------------------------------------------------------------
+__device__ inline double weno_w(double u, double v) {
+  const double r = (EPS14 + u * u) / (EPS14 + v * v);
+  return 1.0 / (1 + 2 * (r * r));
+}
+
+__device__ inline void weno_pair(const double* tau, size_t k, size_t s, int i, int n, double h,
+                                 double* p1, double* p2) {
+  const double tm1 = tau[k - s], t0 = tau[k], tp1 = tau[k + s];
+  if (i == 1) {
+    const double tp2 = tau[k + 2 * s];
+    *p1 = (t0 - tm1) / h;
+    const double w2 = weno_w(t0 - 2 * tp1 + tp2, tm1 - 2 * t0 + tp1);
+    *p2 = (1 - w2) * (tp1 - tm1) / 2 / h + w2 * (-3 * t0 + 4 * tp1 - tp2) / 2 / h;
+  } else if (i == n - 2) {
+    const double tm2 = tau[k - 2 * s];
+    const double w1 = weno_w(t0 - 2 * tm1 + tm2, tp1 - 2 * t0 + tm1);
+    *p1 = (1 - w1) * (tp1 - tm1) / 2 / h + w1 * (3 * t0 - 4 * tm1 + tm2) / 2 / h;
+    *p2 = (tp1 - t0) / h;
+  } else {
+    const double tm2 = tau[k - 2 * s], tp2 = tau[k + 2 * s];
+    const double w1 = weno_w(t0 - 2 * tm1 + tm2, tp1 - 2 * t0 + tm1);
+    *p1 = (1.0 - w1) * (tp1 - tm1) / 2 / h + w1 * (3 * t0 - 4 * tm1 + tm2) / 2 / h;
+    const double w2 = weno_w(t0 - 2 * tp1 + tp2, tm1 - 2 * t0 + tp1);
+    *p2 = (1.0 - w2) * (tp1 - tm1) / 2 / h + w2 * (-3 * t0 + 4 * tp1 - tp2) / 2 / h;
+  }
+}
+
+__device__ inline void weno_sweeps(const PeriodDev& P, const FwdWs& W, SolveShared& sh, int multi) {
+  const int nx = P.nx, ny = P.ny;
+  const size_t N = (size_t)nx * ny;
+  const Box box = sh.box;
+  double* tau = W.tau;
+  double* tau_old = W.tau_old;
+  const double* T0 = W.T0;
+  const double* T0x = W.K;
+  const double* T0y = W.K + N;
+  const double dx = P.dx, dy = P.dy;
+  int iter, status = ST_NOT_CONVERGED;
+  for (iter = 1; iter <= MAXITER_WENO; ++iter) {
+    for (size_t k = threadIdx.x; k < N; k += blockDim.x) tau_old[k] = tau[k];
+    __syncthreads();
+    for (int s = 0; s < 4; ++s) {
+      SweepGeom g;
+      g.ilo = 1; g.ihi = nx - 2; g.jlo = 1; g.jhi = ny - 2;
+      sweep_dirs(s, g.xdir, g.ydir);
+      const int nd = g.ndiag();
+      for (int d = 0; d < nd; ++d) {
+        for (int v = g.vmin(d) + (int)threadIdx.x; v <= g.vmax(d); v += blockDim.x) {
+          int i, j;
+          g.cell(d, v, i, j);
+          if (box.has(i, j)) continue;
+          const size_t k = (size_t)i + (size_t)nx * j;
+          const double a = P.a[k], b = P.b[k], c = P.c[k];
+          float sigx, sigy;
+          if (multi) {
+            sigx = (float)(sqrt(a) * T0[k]);
+            sigy = (float)(sqrt(b) * T0[k]);
+          } else {
+            sigx = (float)sqrt(a);
+            sigy = (float)sqrt(b);
+          }
+          const float coe = (float)(1.0 / (((double)sigx / dx) + ((double)sigy / dy)));
+          double px1, px2, py1, py2;
+          weno_pair(tau, k, 1, i, nx, dx, &px1, &px2);
+          weno_pair(tau, k, (size_t)nx, j, ny, dy, &py1, &py2);
+          double H;
+          if (multi) {
+            const double U = T0x[k] * tau[k] + T0[k] * (px1 + px2) / 2;
+            const double V = T0y[k] * tau[k] + T0[k] * (py1 + py2) / 2;
+            H = sqrt(a * (U * U) + b * (V * V) - 2 * c * U * V);
+          } else {
+            const double Pp = (px1 + px2) / 2, Q = (py1 + py2) / 2;
+            H = sqrt(a * (Pp * Pp) + b * (Q * Q) - 2 * c * (px1 + px2) * (py1 + py2) / 4 +
+                     2 * (a * T0x[k] - c * T0y[k]) * (px1 + px2) / 2 +
+                     2 * (b * T0y[k] - c * T0x[k]) * (py1 + py2) / 2 + a * (T0x[k] * T0x[k]) +
+                     b * (T0y[k] * T0y[k]) - 2 * c * T0x[k] * T0y[k]);
+          }
+          tau[k] = (double)coe * (P.fun[k] - H) +
+                   (double)coe * ((double)sigx * (px2 - px1) / 2 + (double)sigy * (py2 - py1) / 2) +
+                   tau[k];
+        }
+        __syncthreads();
+      }
+      // boundary extrapolation after every sweep (:502-509, :715-722)
+      const int jlo = multi ? 1 : 0, jhi = multi ? ny - 1 : ny;
+      for (int j = jlo + threadIdx.x; j < jhi; j += blockDim.x) {
+        const size_t r = (size_t)nx * j;
+        double v1 = 2 * tau[r + 1] - tau[r + 2], v2 = tau[r + 2];
+        tau[r] = v1 > v2 ? v1 : v2;
+        v1 = 2 * tau[r + nx - 2] - tau[r + nx - 3];
+        v2 = tau[r + nx - 3];
+        tau[r + nx - 1] = v1 > v2 ? v1 : v2;
+      }
+      __syncthreads();
+      const int ilo = multi ? 1 : 0, ihi = multi ? nx - 1 : nx;
+      for (int i = ilo + threadIdx.x; i < ihi; i += blockDim.x) {
+        double v1 = 2 * tau[i + (size_t)nx] - tau[i + 2 * (size_t)nx], v2 = tau[i + 2 * (size_t)nx];
+        tau[i] = v1 > v2 ? v1 : v2;
+        v1 = 2 * tau[i + (size_t)nx * (ny - 2)] - tau[i + (size_t)nx * (ny - 3)];
+        v2 = tau[i + (size_t)nx * (ny - 3)];
+        tau[i + (size_t)nx * (ny - 1)] = v1 > v2 ? v1 : v2;
+      }
+      __syncthreads();
+    }
+    double l1 = 0, lm = 0;
+    for (size_t k = threadIdx.x; k < N; k += blockDim.x) {
+      const double d = fabs(tau[k] - tau_old[k]);
+      l1 += d * dx * dy;
+      lm = fmax(lm, d);
+    }
+    block_sum_max(l1, lm, sh.red);
+    if (fabs(l1) < TOL_WENO && lm < TOL_WENO) { status = ST_OK; break; }
+  }
+  if (threadIdx.x == 0) {
+    sh.status = status;
+    sh.iters = iter > MAXITER_WENO ? MAXITER_WENO : iter;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Single-solve kernels (one block) for the drop-in symbols
+// ---------------------------------------------------------------------------
+long long single_ws_doubles(long long N) { return batch_fp64_ws_doubles(N); }
+
+__global__ void __launch_bounds__(256) k_uw_single(PeriodDev P, double x0, double y0, double* ws,
+                                                   double* T, int* si) {
+  __shared__ SolveShared sh;
+  const size_t N = (size_t)P.nx * P.ny;
+  SolveLayout L = carve(ws, N);
+  fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, L.fw, true, sh);
+  if (sh.status != ST_OK) {
+    if (threadIdx.x == 0) { si[0] = sh.status; si[1] = 0; }
+    return;
+  }
+  uw_sweeps(P, L.fw, sh, MAXITER_UW);
+  for (size_t k = threadIdx.x; k < N; k += blockDim.x) T[k] = L.fw.tau[k] * L.fw.T0[k];
+  if (threadIdx.x == 0) { si[0] = sh.status; si[1] = sh.iters; }
+}
+
+void launch_uw_single(const PeriodDev& P, double x0, double y0, double* ws, double* T,
+                      int* si, cudaStream_t st) {
+  k_uw_single<<<1, 256, 0, st>>>(P, x0, y0, ws, T, si);
+}
+
+__global__ void __launch_bounds__(256) k_weno_single(PeriodDev P, double x0, double y0, int multi,
+                                                     double* ws, double* T, int* si) {
+  __shared__ SolveShared sh;
+  const size_t N = (size_t)P.nx * P.ny;
+  SolveLayout L = carve(ws, N);
+  fwd_setup(P, x0, y0, 2.0, multi ? 1.0 : 0.0, multi ? 1.0 : 20.0, L.fw, false, sh);
+  if (sh.status != ST_OK) {
+    if (threadIdx.x == 0) { si[0] = sh.status; si[1] = 0; }
+    return;
+  }
+  weno_sweeps(P, L.fw, sh, multi);
+  for (size_t k = threadIdx.x; k < N; k += blockDim.x)
+    T[k] = multi ? L.fw.tau[k] * L.fw.T0[k] : L.fw.tau[k] + L.fw.T0[k];
+  if (threadIdx.x == 0) { si[0] = sh.status; si[1] = sh.iters; }
+}
+
+void launch_weno_single(const PeriodDev& P, double x0, double y0, int multi, double* ws,
+                        double* T, int* si, cudaStream_t st) {
+  k_weno_single<<<1, 256, 0, st>>>(P, x0, y0, multi, ws, T, si);
+}
+
+__global__ void __launch_bounds__(256) k_jse_single(PeriodDev P, const double* T,
+                                                    const double* recx, const double* recy,
+                                                    const double* sadj, int nrec, double* ws,
+                                                    double* Ta, int* si) {
+  __shared__ SolveShared sh;
+  const size_t N = (size_t)P.nx * P.ny;
+  SolveLayout L = carve(ws, N);
+  L.aw.T = T;
+  L.aw.Ta[0] = Ta;
+  for (size_t k = threadIdx.x; k < N; k += blockDim.x) L.aw.delta[0][k] = 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0) sh.flag = adj_splat(P, L.aw.delta[0], nrec, recx, recy, sadj, 0.0);
+  __syncthreads();
+  if (sh.flag != ST_OK) {
+    if (threadIdx.x == 0) { si[0] = sh.flag; si[1] = 0; }
+    return;
+  }
+  adj_setup(P, L.aw, 1);
+  int its[2] = {0, 0}, sts[2] = {ST_OK, ST_OK};
+  adj_sweeps(P, L.aw, 1, sh, its, sts);
+  if (threadIdx.x == 0) { si[0] = sts[0]; si[1] = its[0]; }
+}
+
+void launch_jse_single(const PeriodDev& P, const double* T, const double* recx,
+                       const double* recy, const double* sadj, int nrec, double* ws, double* Ta,
+                       int* si, cudaStream_t st) {
+  k_jse_single<<<1, 256, 0, st>>>(P, T, recx, recy, sadj, nrec, ws, Ta, si);
+}
+
+__global__ void k_mask_single(PeriodDev P, double* tab, double x0, double y0) {
+  apply_mask(P, tab, x0, y0);
+}
+
+void launch_mask_single(const PeriodDev& P, double* tab, double x0, double y0, cudaStream_t st) {
+  k_mask_single<<<1, 256, 0, st>>>(P, tab, x0, y0);
+}
+
+__global__ void k_interp(PeriodDev P, const double* T, int nrec, const double* recx,
+                         const double* recy, double* out, int* status) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrec) return;
+  double v = 0;
+  if (!interp2(P.xdeg, P.nx, P.ydeg, P.ny, T, recx[r], recy[r], &v)) atomicExch(status, ST_BAD_ARG);
+  out[r] = v;
+}
+
+void launch_interp(const PeriodDev& P, const double* T, int nrec, const double* recx,
+                   const double* recy, double* out, int* status, cudaStream_t st) {
+  if (nrec <= 0) return;
+  k_interp<<<(nrec + 127) / 128, 128, 0, st>>>(P, T, nrec, recx, recy, out, status);
+}
+
+}  // namespace sgb

@@ -1,0 +1,97 @@
+// kernels.cuh -- launch interface between the C ABI (capi.cu) and the device
+// code (kernels.cu, kernels_fp32.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace sgb {
+
+// Inputs of the per-period precompute.  Either (vel, m11, m12, m22) from the
+// measurement layer -- spha = m11, sphb = m22, sphc = -m12, fun = 1./vel
+// (src/measadj.f90:66-70) -- or the solver's own (spha, sphb, sphc, fun).
+struct PrepIn {
+  int nx, ny, lonlat;
+  const double* xdeg;  // caller's coordinates (nx), degrees for lon/lat
+  const double* ydeg;
+  const double* A;     // m11 or spha
+  const double* B;     // m22 or sphb
+  const double* C;     // m12 (negated) or sphc
+  const double* V;     // vel (inverted) or fun
+  int from_model;      // 1: (vel, m11, m12, m22); 0: (fun, spha, sphb, sphc)
+};
+
+// Outputs (device, N per field, nx/ny per axis) -- referenced by PeriodDev.
+struct PrepOut {
+  double *xs, *ys, *cosy, *siny, *a, *b, *c, *fun, *f2, *disx, *disy;
+};
+
+// Batched evaluation arguments (all device pointers).
+struct BatchArgs {
+  const PeriodDev* periods;
+  int nsolve;
+  const int* order;        // solve processing order (cost-descending)
+  const int* pidx;
+  const double* srcx;
+  const double* srcy;
+  const int* rec_off;
+  const int* nrec;
+  const double* recx;
+  const double* recy;
+  const double* tt;
+  const double* weight;
+  const int* path;
+  const long long* kslot;  // per solve: cell offset of its kernel contribution slot
+  int mode;                // 0 forward, 2 tomo2d, 3 tomo (density too)
+  // outputs
+  double* tekio;           // per receiver
+  double* wgt_eff;         // per receiver, weight after outlier zeroing
+  double* tt_fwd;          // per path
+  double* chi;             // per solve
+  double* kcontrib;        // adj/svel^k slots (sum of N over solves)
+  double* kcontrib_den;    // density slots (mode 3)
+  int* status;
+  int* fwd_iters;
+  int* adj_iters;
+  double* fwd_updates;     // per solve: forward cell visits (for the roofline)
+  double* adj_updates;
+  double* Tout;            // optional: per-solve travel-time field (kslot layout) or null
+  // workspace
+  double* ws;              // slots of ws_doubles each
+  long long ws_doubles;
+  int* queue;              // work counter (zeroed before launch)
+  int block;               // threads per block (for info)
+};
+
+void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st);
+void launch_batch_fp64(const BatchArgs& a, int grid, int block, cudaStream_t st);
+void launch_batch_fp32(const BatchArgs& a, int grid, int block, cudaStream_t st);
+int batch_fp64_max_blocks_per_sm(int block);
+int batch_fp32_max_blocks_per_sm(int block);
+// workspace doubles per solve slot for a grid of N cells
+long long batch_fp64_ws_doubles(long long N);
+long long batch_fp32_ws_doubles(long long N);
+
+// Ordered per-period kernel sum: out[goff_p + k] = sum over the solves of
+// period p, in work-list order, of contrib[kslot_s + k] (src/acqui.f90:314-315).
+void launch_kernel_reduce(const PeriodDev* periods_host, int nperiod, const int* plist_off,
+                          const int* plist, const long long* kslot, const double* contrib,
+                          double* out, long long ncell, const long long* goff_dev,
+                          const int* nx_dev, const int* ny_dev, cudaStream_t st);
+// chi = sum of per-solve misfits in work-list order (src/acqui.f90:135)
+void launch_chi_reduce(const double* chi_s, int nsolve, double* chi_out, cudaStream_t st);
+
+// Single-solve kernels of the drop-in symbols (one block).
+void launch_uw_single(const PeriodDev& P, double x0, double y0, double* ws, double* T,
+                      int* status_iters, cudaStream_t st);
+void launch_weno_single(const PeriodDev& P, double x0, double y0, int multiplicative, double* ws,
+                        double* T, int* status_iters, cudaStream_t st);
+void launch_jse_single(const PeriodDev& P, const double* T, const double* recx,
+                       const double* recy, const double* sadj, int nrec, double* ws, double* Ta,
+                       int* status_iters, cudaStream_t st);
+void launch_mask_single(const PeriodDev& P, double* tab, double x0, double y0, cudaStream_t st);
+void launch_interp(const PeriodDev& P, const double* T, int nrec, const double* recx,
+                   const double* recy, double* out, int* status, cudaStream_t st);
+long long single_ws_doubles(long long N);
+
+}  // namespace sgb

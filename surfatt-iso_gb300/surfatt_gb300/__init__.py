@@ -1,0 +1,382 @@
+"""Python host binding of libsurfatt_gb300.so (SurfATT travel-time + adjoint
+path on GB300).
+
+This module is a thin ctypes layer over the C ABI declared in
+``include/surfatt_gb300.h``; every computation runs in the CUDA library.
+There is no CPU fallback: if the library is missing or no GPU is present the
+calls raise.
+
+Names follow the reference:
+  * ``fsm_uw_ps_lonlat_2d`` / ``fsm_o1_jse_lonlat_2d`` / ``mask`` ... call the
+    drop-in symbols that replace the routines of src/eikon_solver_2d.f90;
+  * ``MeasAdj`` mirrors ``att_measadj`` (src/measadj.f90:25-114);
+  * ``Engine`` runs whole gradient evaluations (the per-(period, source) loop
+    of src/acqui.f90:91-161 / src/tomo2d.f90:158-201 with the kernel sums).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+from .workloads import Problem  # noqa: F401
+
+OK, SOURCE_ON_BOUNDARY, BAD_ARG, NOT_CONVERGED, OOM, CUDA_ERROR, TIMEOUT = range(7)
+STATUS_NAMES = {0: "OK", 1: "SOURCE_ON_BOUNDARY", 2: "BAD_ARG", 3: "NOT_CONVERGED", 4: "OOM",
+                5: "CUDA_ERROR", 6: "TIMEOUT"}
+PREC_FP64, PREC_FP32 = 0, 1
+MODE_FORWARD, MODE_2D, MODE_3D = 0, 2, 3
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_llp = ctypes.POINTER(ctypes.c_longlong)
+_lib = None
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTED = [
+    "fsm_uw_ps_lonlat_2d_", "fsm_uw_ps_cart_2d_", "fsm_weno3_ps_2d_", "fsm_weno3_ps_multi_2d_",
+    "fsm_o1_jse_lonlat_2d_", "fsm_o1_jse_2d_", "mask_", "surfatt_last_status",
+    "surfatt_last_iterations", "surfatt_set_exit_on_boundary", "surfatt_measadj_run_forward",
+    "surfatt_measadj_run_adjoint", "surfatt_measadj_run_adjoint_density",
+    "surfatt_engine_create", "surfatt_engine_destroy", "surfatt_engine_load",
+    "surfatt_engine_update_velocity", "surfatt_engine_run", "surfatt_engine_sync",
+    "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
+]
+
+
+class SurfattError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}")
+
+
+def build(force=False, verbose=False):
+    """Compile libsurfatt_gb300.so for sm_103a (in-tree)."""
+    return _build.build(force=force, verbose=verbose)
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def lib():
+    """Load the CUDA library (it must have been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.LIB_PATH):
+            raise RuntimeError("libsurfatt_gb300.so is not built: run surfatt_gb300.build() "
+                               "(the library is the only implementation; there is no fallback)")
+        L = ctypes.CDLL(_build.LIB_PATH)
+        L.surfatt_version.restype = ctypes.c_char_p
+        L.surfatt_engine_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                            ctypes.c_size_t]
+        for f in ("surfatt_engine_destroy",):
+            getattr(L, f).argtypes = [ctypes.c_void_p]
+            getattr(L, f).restype = None
+        L.surfatt_engine_load.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.surfatt_engine_update_velocity.argtypes = [ctypes.c_void_p, _dp]
+        L.surfatt_engine_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.surfatt_engine_sync.argtypes = [ctypes.c_void_p]
+        L.surfatt_engine_results.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.surfatt_engine_timing.argtypes = [ctypes.c_void_p, _dp, _dp, _ip]
+        L.surfatt_engine_work.argtypes = [ctypes.c_void_p, _dp, _dp]
+        dd = ctypes.c_double
+        L.surfatt_measadj_run_forward.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                                  _dp, _dp, dd, dd, ctypes.c_int, _dp, _dp, _dp,
+                                                  _dp, _dp, _dp, _dp]
+        L.surfatt_measadj_run_adjoint.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                                  _dp, dd, dd, ctypes.c_int, _dp, _dp, _dp, _dp,
+                                                  _dp, _dp, _dp]
+        L.surfatt_measadj_run_adjoint_density.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int,
+                                                          _dp, _dp, _dp, dd, dd, ctypes.c_int,
+                                                          _dp, _dp, _dp, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _f2(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def last_status():
+    return lib().surfatt_last_status()
+
+
+def last_iterations():
+    return lib().surfatt_last_iterations()
+
+
+def set_exit_on_boundary(enable: bool):
+    lib().surfatt_set_exit_on_boundary(int(bool(enable)))
+
+
+# ---------------------------------------------------------------------------
+# drop-in symbols (called exactly as gfortran would: every argument by reference)
+# ---------------------------------------------------------------------------
+def _ci(v):
+    return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def _cd(v):
+    return ctypes.byref(ctypes.c_double(float(v)))
+
+
+def _fwd_call(name, xx, yy, a, b, c, fun, x0, y0):
+    xx, yy = _c64(xx), _c64(yy)
+    nx, ny = len(xx), len(yy)
+    a, b, c, fun = (_f2(v) for v in (a, b, c, fun))
+    T = np.zeros((nx, ny), order="F")
+    u = np.zeros((nx, ny), order="F")
+    getattr(lib(), name)(_d(xx), _d(yy), _ci(nx), _ci(ny), _d(a), _d(b), _d(c), _d(T), _d(fun),
+                         _cd(x0), _cd(y0), _d(u))
+    return T, last_status(), last_iterations()
+
+
+def fsm_uw_ps_lonlat_2d(xx_deg, yy_deg, spha, sphb, sphc, fun, x0_deg, y0_deg):
+    """FSM_UW_PS_lonlat_2d on the GPU; returns (T (nx, ny), status, iterations)."""
+    return _fwd_call("fsm_uw_ps_lonlat_2d_", xx_deg, yy_deg, spha, sphb, sphc, fun, x0_deg, y0_deg)
+
+
+def fsm_uw_ps_cart_2d(xx, yy, a, b, c, fun, x0, y0):
+    return _fwd_call("fsm_uw_ps_cart_2d_", xx, yy, a, b, c, fun, x0, y0)
+
+
+def fsm_weno3_ps_2d(xx, yy, a, b, c, fun, x0, y0):
+    return _fwd_call("fsm_weno3_ps_2d_", xx, yy, a, b, c, fun, x0, y0)
+
+
+def fsm_weno3_ps_multi_2d(xx, yy, a, b, c, fun, x0, y0):
+    return _fwd_call("fsm_weno3_ps_multi_2d_", xx, yy, a, b, c, fun, x0, y0)
+
+
+def _adj_call(name, xx, yy, a, b, c, T, xrec, yrec, sadj):
+    xx, yy = _c64(xx), _c64(yy)
+    nx, ny = len(xx), len(yy)
+    a, b, c, T = (_f2(v) for v in (a, b, c, T))
+    xrec, yrec, sadj = _c64(xrec), _c64(yrec), _c64(sadj)
+    Ta = np.zeros((nx, ny), order="F")
+    getattr(lib(), name)(_d(xx), _d(yy), _ci(nx), _ci(ny), _d(a), _d(b), _d(c), _d(T), _d(Ta),
+                         _d(xrec), _d(yrec), _d(sadj), _ci(len(xrec)))
+    return Ta, last_status(), last_iterations()
+
+
+def fsm_o1_jse_lonlat_2d(xx_deg, yy_deg, spha, sphb, sphc, T, xrec_deg, yrec_deg, sadj):
+    return _adj_call("fsm_o1_jse_lonlat_2d_", xx_deg, yy_deg, spha, sphb, sphc, T, xrec_deg,
+                     yrec_deg, sadj)
+
+
+def fsm_o1_jse_2d(xx, yy, a, b, c, T, xrec, yrec, sadj):
+    return _adj_call("fsm_o1_jse_2d_", xx, yy, a, b, c, T, xrec, yrec, sadj)
+
+
+def mask(xx, yy, table, x0, y0):
+    xx, yy = _c64(xx), _c64(yy)
+    t = _f2(table).copy(order="F")
+    lib().mask_(_d(xx), _d(yy), _ci(len(xx)), _ci(len(yy)), _d(t), _cd(x0), _cd(y0))
+    st = last_status()
+    if st != OK:
+        raise SurfattError(st, "mask")
+    return t
+
+
+# ---------------------------------------------------------------------------
+# att_measadj mirror (src/measadj.f90)
+# ---------------------------------------------------------------------------
+class MeasAdj:
+    """One (period, source) measurement: get_recs / run_forward / run_adjoint /
+    run_adjoint_density / to_table, as in src/measadj.f90:25-114."""
+
+    def __init__(self, xgrids, ygrids, srcx, srcy, recx, recy, tt, weight, idx_path=None):
+        self.xgrids, self.ygrids = _c64(xgrids), _c64(ygrids)
+        self.srcx, self.srcy = float(srcx), float(srcy)
+        self.recx, self.recy, self.tt = _c64(recx), _c64(recy), _c64(tt)
+        self.weight = _c64(weight).copy()
+        self.nrec = len(self.tt)
+        self.idx_path = np.arange(self.nrec) if idx_path is None else np.asarray(idx_path)
+        self.timetable = None
+        self.tekio = None
+        self.chi = None
+
+    def run_forward(self, vel2d, m11, m22, m12):
+        nx, ny = len(self.xgrids), len(self.ygrids)
+        self.timetable = np.zeros((nx, ny), order="F")
+        self.tekio = np.zeros(self.nrec)
+        chi = ctypes.c_double(0)
+        vel2d, m11, m22, m12 = (_f2(v) for v in (vel2d, m11, m22, m12))
+        st = lib().surfatt_measadj_run_forward(
+            _d(self.xgrids), _d(self.ygrids), nx, ny, _d(vel2d), _d(m11), _d(m22), _d(m12),
+            self.srcx, self.srcy, self.nrec, _d(self.recx), _d(self.recy), _d(self.tt),
+            _d(self.weight), _d(self.timetable), _d(self.tekio), ctypes.byref(chi))
+        if st not in (OK, NOT_CONVERGED):
+            raise SurfattError(st, "run_forward")
+        self.chi = chi.value
+        return st
+
+    def run_adjoint(self, m11, m22, m12):
+        nx, ny = len(self.xgrids), len(self.ygrids)
+        adj = np.zeros((nx, ny), order="F")
+        m11, m22, m12 = (_f2(v) for v in (m11, m22, m12))
+        st = lib().surfatt_measadj_run_adjoint(
+            _d(self.xgrids), _d(self.ygrids), nx, ny, _d(m11), _d(m22), _d(m12), self.srcx,
+            self.srcy, self.nrec, _d(self.recx), _d(self.recy), _d(self.tt), _d(self.tekio),
+            _d(self.weight), _d(_f2(self.timetable)), _d(adj))
+        if st not in (OK, NOT_CONVERGED):
+            raise SurfattError(st, "run_adjoint")
+        return adj
+
+    def run_adjoint_density(self, m11, m22, m12):
+        nx, ny = len(self.xgrids), len(self.ygrids)
+        den = np.zeros((nx, ny), order="F")
+        m11, m22, m12 = (_f2(v) for v in (m11, m22, m12))
+        st = lib().surfatt_measadj_run_adjoint_density(
+            _d(self.xgrids), _d(self.ygrids), nx, ny, _d(m11), _d(m22), _d(m12), self.srcx,
+            self.srcy, self.nrec, _d(self.recx), _d(self.recy), _d(self.weight),
+            _d(_f2(self.timetable)), _d(den))
+        if st not in (OK, NOT_CONVERGED):
+            raise SurfattError(st, "run_adjoint_density")
+        return den
+
+    def to_table(self, tt_fwd):
+        tt_fwd[self.idx_path] = self.tekio
+
+
+# ---------------------------------------------------------------------------
+# batched engine
+# ---------------------------------------------------------------------------
+class _CProblem(ctypes.Structure):
+    _fields_ = [("nperiod", ctypes.c_int), ("nx", _ip), ("ny", _ip), ("xoff", _llp),
+                ("yoff", _llp), ("goff", _llp), ("xgrid", _dp), ("ygrid", _dp),
+                ("svel", _dp), ("m11", _dp), ("m12", _dp), ("m22", _dp),
+                ("nsolve", ctypes.c_int), ("pidx", _ip), ("srcx", _dp), ("srcy", _dp),
+                ("rec_off", _ip), ("nrec", _ip), ("recx", _dp), ("recy", _dp), ("tt", _dp),
+                ("weight", _dp), ("path", _ip), ("npath", ctypes.c_int)]
+
+
+class _CResult(ctypes.Structure):
+    _fields_ = [("adj_s", _dp), ("adj_density", _dp), ("chi", _dp), ("tt_fwd", _dp),
+                ("status", _ip), ("fwd_iters", _ip), ("adj_iters", _ip)]
+
+
+def pack_problem(pb, keep):
+    """ctypes view of a workloads.Problem (arrays kept alive in `keep`)."""
+
+    def P(a, kind):
+        a = np.ascontiguousarray(a, dtype={"d": np.float64, "i": np.int32, "q": np.int64}[kind])
+        keep.append(a)
+        return a.ctypes.data_as({"d": _dp, "i": _ip, "q": _llp}[kind])
+
+    return _CProblem(pb.nperiod, P(pb.nx, "i"), P(pb.ny, "i"), P(pb.xoff, "q"), P(pb.yoff, "q"),
+                     P(pb.goff, "q"), P(pb.xgrid, "d"), P(pb.ygrid, "d"), P(pb.svel, "d"),
+                     P(pb.m11, "d"), P(pb.m12, "d"), P(pb.m22, "d"), pb.nsolve, P(pb.pidx, "i"),
+                     P(pb.srcx, "d"), P(pb.srcy, "d"), P(pb.rec_off, "i"), P(pb.nrec, "i"),
+                     P(pb.recx, "d"), P(pb.recy, "d"), P(pb.tt, "d"), P(pb.weight, "d"),
+                     P(pb.path, "i"), pb.npath)
+
+
+class Engine:
+    """Batched gradient evaluations on one GPU (device-resident problem)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0):
+        self._h = ctypes.c_void_p()
+        st = lib().surfatt_engine_create(ctypes.byref(self._h), device, hbm_budget_bytes)
+        if st != OK:
+            raise SurfattError(st, "engine_create")
+        self.pb = None
+
+    def close(self):
+        if self._h:
+            lib().surfatt_engine_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, pb):
+        keep = []
+        cp = pack_problem(pb, keep)
+        st = lib().surfatt_engine_load(self._h, ctypes.byref(cp))
+        if st != OK:
+            raise SurfattError(st, "engine_load")
+        self.pb = pb
+
+    def update_velocity(self, svel):
+        svel = _c64(svel)
+        st = lib().surfatt_engine_update_velocity(self._h, _d(svel))
+        if st != OK:
+            raise SurfattError(st, "engine_update_velocity")
+
+    def run(self, mode=MODE_2D, precision=PREC_FP64):
+        st = lib().surfatt_engine_run(self._h, int(mode), int(precision))
+        if st != OK:
+            raise SurfattError(st, "engine_run")
+
+    def sync(self):
+        return lib().surfatt_engine_sync(self._h)
+
+    def results(self, adj=True, density=True, tt=True, per_solve=True):
+        pb = self.pb
+        out = {}
+        r = _CResult()
+        keep = []
+
+        def buf(name, n, dt):
+            a = np.zeros(max(n, 1), dt)
+            keep.append(a)
+            out[name] = a
+            return a.ctypes.data_as(_dp if dt == np.float64 else _ip)
+
+        chi = np.zeros(1)
+        out["chi"] = chi
+        r.chi = chi.ctypes.data_as(_dp)
+        if adj:
+            r.adj_s = buf("adj_s", pb.ncell, np.float64)
+        if density:
+            r.adj_density = buf("adj_density", pb.ncell, np.float64)
+        if tt:
+            r.tt_fwd = buf("tt_fwd", pb.npath, np.float64)
+        if per_solve:
+            r.status = buf("status", pb.nsolve, np.int32)
+            r.fwd_iters = buf("fwd_iters", pb.nsolve, np.int32)
+            r.adj_iters = buf("adj_iters", pb.nsolve, np.int32)
+        st = lib().surfatt_engine_results(self._h, ctypes.byref(r))
+        if st != OK:
+            raise SurfattError(st, "engine_results")
+        out["chi"] = float(chi[0])
+        if tt:
+            out["tt_fwd"] = out["tt_fwd"][:pb.npath]
+        return out
+
+    def timing(self):
+        t, k, n = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_int(0)
+        st = lib().surfatt_engine_timing(self._h, ctypes.byref(t), ctypes.byref(k),
+                                         ctypes.byref(n))
+        if st != OK:
+            raise SurfattError(st, "engine_timing")
+        return t.value, k.value, n.value
+
+    def work(self):
+        f, a = ctypes.c_double(0), ctypes.c_double(0)
+        st = lib().surfatt_engine_work(self._h, ctypes.byref(f), ctypes.byref(a))
+        if st != OK:
+            raise SurfattError(st, "engine_work")
+        return f.value, a.value
+
+    def evaluate(self, pb=None, mode=None, precision=PREC_FP64):
+        """load (if given) + run + results: one gradient evaluation."""
+        if pb is not None:
+            self.load(pb)
+        mode = self.pb.mode if mode is None else mode
+        self.run(mode, precision)
+        self.sync()
+        return self.results()

@@ -1,0 +1,240 @@
+"""CUDA path vs the oracle on the same seeded inputs (GPU only).
+
+Tolerances (plain FP64 path, from the parity contract): travel times and
+misfit relative error <= 1e-6, adjoint fields and kernels norm-wise relative
+error <= 1e-5.  The FP32-factored path: travel times <= 1e-5, kernels <= 1e-3.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_max, rel_pointwise
+from surfatt_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TT_TOL = 1e-6
+KER_TOL = 1e-5
+TT_TOL_F32 = 1e-5
+KER_TOL_F32 = 1e-3
+
+
+def _flat(nx, ny, vel=3.0, pert=0.06, x0=100.0, y0=22.0, d=0.05):
+    xx, yy = W.arange_grid(x0, nx, d), W.arange_grid(y0, ny, d)
+    one = np.ones((nx, ny))
+    sv = vel * W.checkerboard_2d(nx, ny, 2, 3, pert)
+    return xx, yy, one, one.copy(), np.zeros((nx, ny)), 1.0 / sv
+
+
+@pytest.mark.parametrize("nx,ny,src", [(41, 41, (101.03, 23.01)), (33, 17, (100.61, 22.37)),
+                                       (8, 8, (100.17, 22.18)), (64, 48, (101.5, 23.2))])
+def test_forward_lonlat_dropin(sg, oracle, nx, ny, src):
+    xx, yy, a, b, c, fun = _flat(nx, ny)
+    T, st, it = sg.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, *src)
+    Tr, sr, ir = oracle.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, *src)
+    assert st == sr == 0
+    assert it == ir
+    assert rel_pointwise(T, Tr) <= TT_TOL
+
+
+def test_forward_lonlat_topography_metric(sg, oracle):
+    xx, yy, topo, m11, m12, m22 = W.config5_model(n_lon=60, n_lat=50, d=0.02)
+    sv = 3.2 * W.checkerboard_2d(60, 50, 2, 2, 0.05)
+    src = (xx[25] + 0.007, yy[20] + 0.004)
+    T, st, it = sg.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12, 1.0 / sv, *src)
+    Tr, sr, ir = oracle.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12, 1.0 / sv, *src)
+    assert st == sr == 0 and it == ir
+    assert rel_pointwise(T, Tr) <= TT_TOL
+
+
+def test_forward_source_on_boundary(sg, oracle):
+    xx, yy, a, b, c, fun = _flat(20, 20)
+    sg.set_exit_on_boundary(False)
+    T, st, _ = sg.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, xx[0] + 0.01, yy[10])
+    _, sr, _ = oracle.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, xx[0] + 0.01, yy[10])
+    assert st == sr == sg.SOURCE_ON_BOUNDARY
+
+
+def test_adjoint_lonlat_dropin(sg, oracle):
+    xx, yy, a, b, c, fun = _flat(45, 39)
+    src = (101.07, 22.93)
+    Tr, _, _ = oracle.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, *src)
+    rng = np.random.default_rng(5)
+    xr = rng.uniform(xx[2], xx[-3], 12)
+    yr = rng.uniform(yy[2], yy[-3], 12)
+    sadj = rng.normal(0, 1.0, 12)
+    Ta, st, it = sg.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, Tr, xr, yr, sadj)
+    Tar, sr, ir = oracle.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, Tr, xr, yr, sadj)
+    assert st == sr == 0 and it == ir
+    assert rel_max(Ta, Tar) <= KER_TOL
+
+
+def test_adjoint_no_receivers(sg, oracle):
+    xx, yy, a, b, c, fun = _flat(20, 18)
+    Tr, _, _ = oracle.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, 100.47, 22.41)
+    e = np.zeros(0)
+    Ta, st, it = sg.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, Tr, e, e, e)
+    Tar, sr, ir = oracle.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, Tr, e, e, e)
+    assert st == sr and it == ir
+    assert np.array_equal(Ta, Tar)
+
+
+def test_mask_dropin(sg, oracle):
+    xx, yy = W.arange_grid(100, 30, 0.05), W.arange_grid(22, 25, 0.05)
+    t = np.random.default_rng(1).normal(size=(30, 25))
+    assert np.array_equal(sg.mask(xx, yy, t, 100.52, 22.61), oracle.mask(xx, yy, t, 100.52, 22.61))
+
+
+@pytest.mark.parametrize("nx,ny,src", [(40, 36, (1.03, 1.21)), (25, 31, (0.55, 0.91))])
+def test_forward_cart_dropin(sg, oracle, nx, ny, src):
+    xx, yy = np.arange(nx) * 0.05, np.arange(ny) * 0.05
+    a = np.ones((nx, ny)) * 1.1
+    b = np.ones((nx, ny)) * 0.9
+    c = np.full((nx, ny), 0.1)
+    fun = 1.0 / (3.0 * W.checkerboard_2d(nx, ny, 2, 2, 0.05))
+    T, st, it = sg.fsm_uw_ps_cart_2d(xx, yy, a, b, c, fun, *src)
+    Tr, sr, ir = oracle.fsm_uw_ps_cart_2d(xx, yy, a, b, c, fun, *src)
+    assert st == sr == 0 and it == ir
+    assert rel_pointwise(T, Tr) <= TT_TOL
+
+
+@pytest.mark.parametrize("name", ["fsm_weno3_ps_multi_2d", "fsm_weno3_ps_2d"])
+def test_weno3_dropin(sg, oracle, name):
+    nx, ny = 36, 30
+    xx, yy = np.arange(nx) * 0.1, np.arange(ny) * 0.1
+    a = np.ones((nx, ny))
+    b = np.ones((nx, ny))
+    c = np.zeros((nx, ny))
+    fun = 1.0 / (2.0 * W.checkerboard_2d(nx, ny, 1, 1, 0.05))
+    src = (1.73, 1.41)
+    T, st, it = getattr(sg, name)(xx, yy, a, b, c, fun, *src)
+    Tr, sr, ir = getattr(oracle, name)(xx, yy, a, b, c, fun, *src)
+    assert st == sr
+    assert abs(it - ir) <= 1
+    assert rel_pointwise(T, Tr) <= TT_TOL
+
+
+def test_cart_adjoint_dropin(sg, oracle):
+    nx, ny = 30, 28
+    xx, yy = np.arange(nx) * 0.05, np.arange(ny) * 0.05
+    a = np.ones((nx, ny))
+    b = np.ones((nx, ny))
+    c = np.zeros((nx, ny))
+    fun = 1.0 / (3.0 * W.checkerboard_2d(nx, ny, 2, 2, 0.05))
+    Tr, _, _ = oracle.fsm_uw_ps_cart_2d(xx, yy, a, b, c, fun, 0.71, 0.66)
+    xr, yr = np.array([0.2, 1.2, 0.33]), np.array([0.3, 1.1, 1.2])
+    s = np.array([0.5, -1.0, 2.0])
+    Ta, st, it = sg.fsm_o1_jse_2d(xx, yy, a, b, c, Tr, xr, yr, s)
+    Tar, sr, ir = oracle.fsm_o1_jse_2d(xx, yy, a, b, c, Tr, xr, yr, s)
+    assert st == sr == 0 and it == ir
+    assert rel_max(Ta, Tar) <= KER_TOL
+
+
+def test_measadj_layer(sg, oracle):
+    pb = W.flat_case(nx=40, ny=34, nsta=6, nperiod=1)
+    xx, yy = pb.grid(0)
+    v, m11, m12, m22 = (pb.field(n, 0) for n in ("svel", "m11", "m12", "m22"))
+    s, r0, nr = 2, int(pb.rec_off[2]), int(pb.nrec[2])
+    sl = slice(r0, r0 + nr)
+    ma = sg.MeasAdj(xx, yy, pb.srcx[s], pb.srcy[s], pb.recx[sl], pb.recy[sl], pb.tt[sl],
+                    pb.weight[sl])
+    ma.run_forward(v, m11, m22, m12)
+    T = np.zeros((40, 34), order="F")
+    tek = np.zeros(nr)
+    chi = np.zeros(1)
+    import ctypes
+    lib = oracle.lib()
+    it = ctypes.c_int(0)
+    D = lambda a: np.asfortranarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    args = [np.asfortranarray(x, dtype=np.float64) for x in (v, m11, m22, m12)]
+    rx, ry, tt, w = (np.ascontiguousarray(x) for x in (pb.recx[sl], pb.recy[sl], pb.tt[sl], pb.weight[sl]))
+    lib.orc_run_forward(D(xx), D(yy), 40, 34, D(args[0]), D(args[1]), D(args[2]), D(args[3]),
+                        ctypes.c_double(pb.srcx[s]), ctypes.c_double(pb.srcy[s]), nr, D(rx), D(ry),
+                        D(tt), D(w), D(T), D(tek), D(chi), ctypes.byref(it))
+    assert rel_pointwise(ma.timetable, T) <= TT_TOL
+    assert rel_pointwise(ma.tekio, tek) <= TT_TOL
+    assert abs(ma.chi - chi[0]) <= TT_TOL * abs(chi[0])
+    adj = ma.run_adjoint(m11, m22, m12)
+    den = ma.run_adjoint_density(m11, m22, m12)
+    wr = w.copy()
+    adjr = np.zeros((40, 34), order="F")
+    denr = np.zeros((40, 34), order="F")
+    lib.orc_run_adjoint(D(xx), D(yy), 40, 34, D(args[1]), D(args[2]), D(args[3]),
+                        ctypes.c_double(pb.srcx[s]), ctypes.c_double(pb.srcy[s]), nr, D(rx), D(ry),
+                        D(tt), D(tek), wr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), D(T),
+                        D(adjr), ctypes.byref(it))
+    lib.orc_run_adjoint_density(D(xx), D(yy), 40, 34, D(args[1]), D(args[2]), D(args[3]),
+                                ctypes.c_double(pb.srcx[s]), ctypes.c_double(pb.srcy[s]), nr,
+                                D(rx), D(ry), wr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                D(T), D(denr), ctypes.byref(it))
+    assert np.array_equal(ma.weight, wr)
+    assert rel_max(adj, adjr) <= KER_TOL
+    assert rel_max(den, denr) <= KER_TOL
+
+
+def _engine_vs_oracle(sg, oracle, pb, mode, prec, tt_tol, ker_tol):
+    eng = sg.Engine(0)
+    got = eng.evaluate(pb, mode=mode, precision=prec)
+    ref = oracle.gradient_eval(pb, mode=mode, nthreads=4)
+    assert np.all(got["status"] == ref["status"])
+    assert rel_pointwise(got["tt_fwd"], ref["tt_fwd"]) <= tt_tol
+    assert abs(got["chi"] - ref["chi"]) <= tt_tol * 10 * abs(ref["chi"])
+    if mode >= 2:
+        for p in range(pb.nperiod):
+            g0, n = int(pb.goff[p]), int(pb.nx[p] * pb.ny[p])
+            assert rel_max(got["adj_s"][g0:g0 + n], ref["adj_s"][g0:g0 + n]) <= ker_tol, p
+            if mode == 3:
+                assert rel_max(got["adj_density"][g0:g0 + n],
+                               ref["adj_density"][g0:g0 + n]) <= ker_tol, p
+    if prec == sg.PREC_FP64:
+        assert np.all(np.abs(got["fwd_iters"] - ref["fwd_iters"]) <= 0)
+    eng.close()
+    return got, ref
+
+
+@pytest.mark.parametrize("mode", [0, 2, 3])
+def test_engine_fp64_flat(sg, oracle, mode):
+    pb = W.flat_case(nx=50, ny=44, nsta=6, nperiod=2, mode=mode)
+    _engine_vs_oracle(sg, oracle, pb, mode, sg.PREC_FP64, TT_TOL, KER_TOL)
+
+
+def test_engine_fp64_config1(sg, oracle):
+    import os
+    from conftest import GOLDEN
+    obs = W.read_src_rec_tt(os.path.join(GOLDEN, "config1_src_rec.csv"))
+    pb = W.config1(observed_tt=obs)
+    _engine_vs_oracle(sg, oracle, pb, 2, sg.PREC_FP64, TT_TOL, KER_TOL)
+
+
+def test_engine_fp32_flat(sg, oracle):
+    pb = W.flat_case(nx=60, ny=52, nsta=7, nperiod=2, mode=3)
+    _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
+
+
+def test_engine_uneven_grids(sg, oracle):
+    pb = W.config4(nsrc=5, nperiod=3, nmax=72, nmin=40, span_deg=2.0)
+    _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
+
+
+def test_batched_equals_single_solves(sg):
+    """Every solve's result is independent of the batch it runs in."""
+    pb = W.flat_case(nx=40, ny=36, nsta=6, nperiod=2, mode=3)
+    eng = sg.Engine(0)
+    full = eng.evaluate(pb, mode=3)
+    for s in (0, 7, pb.nsolve - 1):
+        sub = pb.subset([s])
+        one = eng.evaluate(sub, mode=3)
+        r0, nr = int(pb.rec_off[s]), int(pb.nrec[s])
+        assert np.array_equal(one["tt_fwd"], full["tt_fwd"][pb.path[r0:r0 + nr]])
+    eng.close()
+
+
+def test_engine_source_on_boundary_status(sg, oracle):
+    pb = W.flat_case(nx=30, ny=30, nsta=4, nperiod=1, mode=2)
+    xx, _ = pb.grid(0)
+    pb.srcx[1] = xx[0] + 0.001
+    eng = sg.Engine(0)
+    got = eng.evaluate(pb, mode=2)
+    ref = oracle.gradient_eval(pb, mode=2)
+    assert got["status"][1] == sg.SOURCE_ON_BOUNDARY == ref["status"][1]
+    assert rel_max(got["adj_s"], ref["adj_s"]) <= KER_TOL
+    eng.close()
