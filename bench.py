@@ -1,0 +1,406 @@
+"""Benchmark of the SurfATT travel-time + adjoint path on GB300.
+
+One step = one gradient evaluation of the 3-D-iso workload (config 2/3):
+80 stations as sources x 16 periods = 1280 (source, period) solves on a
+120x120 lon/lat grid (0.05 deg), each a factored eikonal forward solve,
+receiver interpolation (79 receivers), misfit, two adjoint solves (residual
+and density sources), mask and the per-period kernel sums (/svel^3).
+
+Headline (`value`): the batched FP32-factored path (tau swept in FP32; T0,
+misfit, kernel sums and the convergence test in FP64) in solves/s with the
+problem resident in HBM, timed with CUDA events on the engine's stream.
+The plain FP64 path runs on the same workload and is reported beside it, with
+the FP32-vs-FP64 error.  `e2e` is the same metric through the C ABI with host
+buffers: upload of the whole problem from pinned memory + run + download of
+kernels, misfit and synthetic times, every step.
+
+`--impl reference` times the reference algorithm's CPU implementation (the
+C restatement in oracle/, all host threads, the reference's contiguous
+work-list split) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
+
+# Reference-formulation flops per visit (src/eikon_solver_2d.f90 as written,
+# add/sub/mul/div/sqrt = 1 flop), counted on a 32-solve stratified sample of
+# this workload by `python oracle/count_flops.py config2 32`.
+FWD_FLOPS_PER_VISIT = 351.8
+ADJ_FLOPS_PER_VISIT = 16.0
+METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config4"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def _workload(name):
+    from surfatt_gb300 import workloads as W
+    if name == "config1":
+        obs = W.read_src_rec_tt(os.path.join(ROOT, "tests", "golden", "config1_src_rec.csv"))
+        pb = W.config1(observed_tt=obs)
+        desc = "config1: 2-D, 81x81 grid, 25 stations (600 paths), 1 period"
+    elif name == "config4":
+        pb = W.config4()
+        desc = "config4: 120 sources x 25 periods = 3000 solves, grids 64^2..384^2, 3-D mode"
+    else:
+        pb = W.config2()
+        desc = ("config3 (config2 with tau swept in FP32): 3-D-iso gradient evaluation, "
+                "80 stations x 16 periods = 1280 solves, 120x120 grid at 0.05 deg, "
+                "79 receivers/solve, two adjoints/solve")
+    return pb, desc
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
+    return dist, rank, ws, local
+
+
+def _barrier(dist, local):
+    import torch
+    if dist is not None:
+        dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize(local)
+
+
+def _max_over_ranks(dist, v, local):
+    if dist is None:
+        return v
+    import torch
+    dev = f"cuda:{local}" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.cpu()[0])
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def _flush_l2(buf):
+    """Write a buffer larger than L2 (129 MB) between timed steps."""
+    import torch
+    buf.zero_()
+    torch.cuda.synchronize()
+
+
+def _time_steps(eng, pb, prec, steps, warmup, flush):
+    for _ in range(warmup):
+        eng.run(pb.mode, prec)
+        eng.sync()
+    totals, kernels, launches = [], [], 0
+    for _ in range(steps):
+        _flush_l2(flush)
+        eng.run(pb.mode, prec)
+        st = eng.sync()
+        t, k, n = eng.timing()
+        totals.append(t)
+        kernels.append(k)
+        launches += n
+        if st not in (0, 3):
+            raise RuntimeError(f"run status {st}")
+    return totals, kernels, launches
+
+
+def _errors(a, b, pb):
+    from surfatt_gb300 import workloads as W  # noqa: F401
+    out = {}
+    m = b["tt_fwd"] != 0
+    out["tt_rel_max"] = float(np.max(np.abs(a["tt_fwd"][m] - b["tt_fwd"][m]) / np.abs(b["tt_fwd"][m])))
+    out["chi_rel"] = float(abs(a["chi"] - b["chi"]) / abs(b["chi"]))
+    for key in ("adj_s", "adj_density"):
+        worst = 0.0
+        for p in range(pb.nperiod):
+            g0, n = int(pb.goff[p]), int(pb.nx[p] * pb.ny[p])
+            den = np.max(np.abs(b[key][g0:g0 + n]))
+            if den > 0:
+                worst = max(worst, float(np.max(np.abs(a[key][g0:g0 + n] - b[key][g0:g0 + n])) / den))
+        out[key + "_rel_max_per_period"] = worst
+    return out
+
+
+def _pinned_problem(pb):
+    """Copies of the problem's arrays in pinned host memory."""
+    import dataclasses
+    import torch
+
+    def pin(a):
+        a = np.ascontiguousarray(a)
+        t = torch.empty(a.shape, dtype={np.dtype(np.float64): torch.float64,
+                                        np.dtype(np.int32): torch.int32,
+                                        np.dtype(np.int64): torch.int64}[a.dtype],
+                        pin_memory=True)
+        v = t.numpy()
+        v[...] = a
+        return v, t
+
+    keep, kw = [], {}
+    for f in dataclasses.fields(pb):
+        v = getattr(pb, f.name)
+        if isinstance(v, np.ndarray):
+            arr, t = pin(v)
+            keep.append(t)
+            kw[f.name] = arr
+    return dataclasses.replace(pb, **kw), keep
+
+
+def run_ours(args):
+    import torch
+    import surfatt_gb300 as sg
+    dist, rank, world, local = _dist()
+    sg.build()
+    pb, desc = _workload(args.workload)
+    dev = local
+    torch.cuda.set_device(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    fp64_peak, fp32_peak = sg.measure_peaks(dev)
+    eng = sg.Engine(dev)
+    eng.load(pb)
+    # correctness of the headline against the plain FP64 path on this workload
+    eng.run(pb.mode, sg.PREC_FP64)
+    eng.sync()
+    r64 = eng.results()
+    fwd64, adj64 = eng.work()
+    eng.run(pb.mode, sg.PREC_FP32)
+    eng.sync()
+    r32 = eng.results()
+    fwd32, adj32 = eng.work()
+    err32 = _errors(r32, r64, pb)
+
+    # plain FP64 (reported beside the headline)
+    t64, k64, _ = _time_steps(eng, pb, sg.PREC_FP64, max(1, min(args.steps, 3)), 1, flush)
+    # headline: FP32-factored, timed region bracketed by barrier + synchronize
+    clocks = Clocks(dev)
+    _barrier(dist, dev)
+    clocks.start()
+    t0 = time.perf_counter()
+    t32, k32, launches = _time_steps(eng, pb, sg.PREC_FP32, args.steps, args.warmup, flush)
+    wall = time.perf_counter() - t0
+    _barrier(dist, dev)
+    ck = clocks.stop()
+    ms_step = statistics.mean(t32)
+    ms_step_max = _max_over_ranks(dist, ms_step, dev)
+    value = pb.nsolve * world / (ms_step_max / 1e3)
+
+    e2e = None
+    if not args.no_e2e:
+        ppb, keep = _pinned_problem(pb)
+        into = {}
+        for name, n, dt in (("adj_s", pb.ncell, np.float64), ("adj_density", pb.ncell, np.float64),
+                            ("tt_fwd", pb.npath, np.float64), ("status", pb.nsolve, np.int32),
+                            ("fwd_iters", pb.nsolve, np.int32), ("adj_iters", pb.nsolve, np.int32),
+                            ("chi", 1, np.float64)):
+            t = torch.empty(max(n, 1), dtype=torch.float64 if dt == np.float64 else torch.int32,
+                            pin_memory=True)
+            keep.append(t)
+            into[name] = t.numpy()
+        h2d = sum(getattr(ppb, f).nbytes for f in ("xgrid", "ygrid", "svel", "m11", "m12", "m22",
+                                                    "pidx", "srcx", "srcy", "rec_off", "nrec",
+                                                    "recx", "recy", "tt", "weight", "path"))
+        d2h = sum(into[k].nbytes for k in into)
+        e2e_t = []
+        for i in range(args.warmup + args.steps):
+            _flush_l2(flush)
+            _barrier(dist, dev)
+            a = time.perf_counter()
+            eng.load(ppb)
+            eng.run(pb.mode, sg.PREC_FP32)
+            eng.sync()
+            eng.results(into=into)
+            b = time.perf_counter()
+            if i >= args.warmup:
+                e2e_t.append(b - a)
+        e2e_s = _max_over_ranks(dist, statistics.mean(e2e_t), dev)
+        e2e = {"value": pb.nsolve * world / e2e_s, "unit": "solves/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned"}
+
+    # roofline of the dominant kernel (the fused batched solve kernel)
+    flops32 = fwd32 * FWD_FLOPS_PER_VISIT + adj32 * ADJ_FLOPS_PER_VISIT
+    flops64 = fwd64 * FWD_FLOPS_PER_VISIT + adj64 * ADJ_FLOPS_PER_VISIT
+    k32_ms = statistics.mean(k32)
+    k64_ms = statistics.mean(k64)
+    ach32 = flops32 / (k32_ms * 1e-3) / 1e12
+    ach64 = flops64 / (k64_ms * 1e-3) / 1e12
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(args.workload, {}).get("fp32")
+        except (OSError, ValueError):
+            traffic = None
+
+    cpu = None
+    parity = {}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        nthr = os.cpu_count() or 1
+        a = time.perf_counter()
+        ref = O.gradient_eval(pb, mode=pb.mode, nthreads=nthr)
+        b = time.perf_counter()
+        cpu = {"value": pb.nsolve / (b - a), "unit": "solves/s", "cores": nthr, "kind": "port",
+               "sample": f"the full workload ({pb.nsolve} solves), one evaluation, "
+                         f"{nthr} threads, contiguous work-list blocks",
+               "seconds": b - a}
+        parity = {"fp64_vs_oracle": _errors(r64, ref, pb), "fp32_vs_oracle": _errors(r32, ref, pb)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step_max,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 sweep / f64 T0, misfit, kernels", "data": "synthetic",
+            "config": {"workload": desc, "solves_per_step": pb.nsolve, "grid": "120x120",
+                       "periods": int(pb.nperiod), "receivers": int(len(pb.tt)),
+                       "mode": "3-D (adj and density /svel^3)", "l2": "flushed (256 MB write) between timed steps",
+                       "parallelism": f"{world} GPU(s), one engine per GPU, independent evaluations"},
+            "p50_ms": statistics.median(t32), "p99_ms": float(np.percentile(t32, 99)),
+            "cell_updates_per_s": (fwd32 + adj32) * world / (ms_step_max / 1e3),
+            "plain_fp64": {"value": pb.nsolve * world / (statistics.mean(t64) / 1e3),
+                           "unit": "solves/s", "ms_per_step": statistics.mean(t64),
+                           "solve_kernel_ms": k64_ms, "achieved_tflops": ach64,
+                           "peak_tflops_fp64": fp64_peak, "frac": ach64 / fp64_peak},
+            "speedup_fp32_vs_fp64": statistics.mean(t64) / ms_step,
+            "fp32_vs_fp64_error": err32,
+            "clocks": ck, "e2e": e2e, "gpu_launches": launches,
+            "roofline": {"bound": "fp32", "bound_note": "FP32 issue (no contraction: no tensor "
+                         "cores); algorithmic flops = reference formulation per visit",
+                         "achieved": ach32, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": ach32 / fp32_peak, "traffic": traffic,
+                         "peak_source": "surfatt_measure_peaks (FP32 FMA chains), this run",
+                         "kernel": "k_batch_fp32", "kernel_ms": k32_ms,
+                         "flops_per_launch": flops32},
+            "cpu_baseline": cpu, "parity": parity,
+            "iterations": {"fwd_mean": float(np.mean(r32["fwd_iters"])),
+                           "adj_mean": float(np.mean(r32["adj_iters"]))},
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    dist, rank, world, local = _dist()
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    pb, desc = _workload(args.workload)
+    nthr = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.gradient_eval(pb, mode=pb.mode, nthreads=nthr)
+    ts = []
+    for _ in range(args.steps):
+        a = time.perf_counter()
+        r = O.gradient_eval(pb, mode=pb.mode, nthreads=nthr)
+        ts.append(time.perf_counter() - a)
+        if r["rc"] not in (0, 3):
+            raise RuntimeError(f"oracle status {r['rc']}")
+    s = statistics.mean(ts)
+    v = pb.nsolve / s
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": desc, "solves_per_step": pb.nsolve},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": nthr, "kind": "port",
+                             "sample": f"the full workload ({pb.nsolve} solves) per step"},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
+                    "is timed through the C restatement in oracle/ on all host threads"}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

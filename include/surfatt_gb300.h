@@ -240,6 +240,11 @@ surfatt_status_t surfatt_engine_timing(surfatt_engine_t* engine, double* total_m
 surfatt_status_t surfatt_engine_work(surfatt_engine_t* engine, double* fwd_cell_updates,
                                      double* adj_cell_updates);
 
+/* FP64 and FP32 FMA issue peaks of `device` in TFLOP/s (an FMA = 2 flops),
+ * measured with independent FMA chains (about 0.1 s).  No counterpart in the
+ * reference: these are the denominators of the sweep kernels' roofline. */
+surfatt_status_t surfatt_measure_peaks(int device, double* fp64_tflops, double* fp32_tflops);
+
 /* Library version string. */
 const char* surfatt_version(void);
 

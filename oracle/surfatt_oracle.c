@@ -40,6 +40,17 @@
 
 #define IDX(ix, iy, nx) ((size_t)(ix) + (size_t)(nx) * (size_t)(iy))
 
+/* Operation counting build (-DORC_COUNT_FLOPS): tallies, per forward visit,
+ * the two-sided cases evaluated, those with Delta >= 0 and the one-sided
+ * cases, and the adjoint visits, to derive the reference formulation's
+ * floating-point operation count per visit. */
+#ifdef ORC_COUNT_FLOPS
+static long long cnt_visit, cnt_two, cnt_delta, cnt_one, cnt_adj;
+#define COUNT(c) (c)++
+#else
+#define COUNT(c) ((void)0)
+#endif
+
 static const double PI_S = (double)3.14159265358979323846f; /* :785, :1297 */
 static const double R_EARTH = 6371.0;                        /* :777, :1296 */
 static const double TOL_UW = (double)1e-4f;                  /* :775 */
@@ -95,6 +106,7 @@ static int uw_sweeps(int nx, int ny, double dx, double dy, const double* a, cons
         for (int iy = y1; iy != y2; iy += ydir) {
           size_t k = IDX(ix, iy, nx);
           if (!ischange[k]) continue;
+          COUNT(cnt_visit);
           double ak = a[k], bk = b[k], ck = c[k], fk = fun[k], t0 = T0[k];
           double t = tau[k];
           /* two-sided cases (:911-994) */
@@ -122,11 +134,13 @@ static int uw_sweeps(int nx, int ny, double dx, double dy, const double* a, cons
                 py = (T0y[k] - t0 / dy); qy = t0 / dy * tau[k + nx];
                 break;
             }
+            COUNT(cnt_two);
             double eqn_a = ak * (px * px) + bk * (py * py) - 2 * ck * px * py;
             double eqn_b = 2 * ak * px * qx + 2 * bk * py * qy - 2 * ck * (px * qy + py * qx);
             double eqn_c = ak * (qx * qx) + bk * (qy * qy) - 2 * ck * qx * qy - fk * fk;
             double Delta = eqn_b * eqn_b - 4 * eqn_a * eqn_c;
             if (Delta >= 0) {
+              COUNT(cnt_delta);
               for (int isol = 1; isol <= 2; ++isol) {
                 double tmp = (isol == 1) ? (-eqn_b + sqrt(Delta)) / (2 * eqn_a)
                                          : (-eqn_b - sqrt(Delta)) / (2 * eqn_a);
@@ -169,6 +183,7 @@ static int uw_sweeps(int nx, int ny, double dx, double dy, const double* a, cons
                 nb = k + nx; p = (T0y[k] - t0 / dy); q = t0 / dy * tau[nb]; dis = disy;
                 break;
             }
+            COUNT(cnt_one);
             double tnb = tau[nb];
             double tmp = (dis - q) / p;
             if (tmp * t0 >= tnb * T0[nb] && tmp > tnb * 0.5 && tmp < t) t = tmp;
@@ -515,6 +530,7 @@ static int jse_core(const double* xx, const double* yy, int nx, int ny, const do
         for (int ix = xf; ix != xl + xs; ix += xs) {
           for (int iy = yf; iy != yl + ys; iy += ys) {
             size_t k = IDX(ix, iy, nx);
+            COUNT(cnt_adj);
             double d = (a2p[k] - a1m[k]) / dx + (b2p[k] - b1m[k]) / dy;
             if (fabs(d) < EPS14) {
               Ta[k] = 0;
@@ -878,3 +894,10 @@ int orc_gradient_eval(const orc_problem* pb, int mode, int nthreads, double* adj
   return orc_gradient_eval_range(pb, mode, nthreads, 0, pb->nsolve, adj_s, adj_density, chi,
                                  tt_fwd, status, fwd_iters, adj_iters);
 }
+
+#ifdef ORC_COUNT_FLOPS
+void orc_flop_counts(long long* out5) {
+  out5[0] = cnt_visit; out5[1] = cnt_two; out5[2] = cnt_delta; out5[3] = cnt_one; out5[4] = cnt_adj;
+  cnt_visit = cnt_two = cnt_delta = cnt_one = cnt_adj = 0;
+}
+#endif

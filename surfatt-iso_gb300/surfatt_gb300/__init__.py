@@ -41,6 +41,7 @@ EXPORTED = [
     "surfatt_engine_create", "surfatt_engine_destroy", "surfatt_engine_load",
     "surfatt_engine_update_velocity", "surfatt_engine_run", "surfatt_engine_sync",
     "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
+    "surfatt_measure_peaks",
 ]
 
 
@@ -104,6 +105,15 @@ def _c64(a):
 
 def _f2(a):
     return np.asfortranarray(a, dtype=np.float64)
+
+
+def measure_peaks(device=0):
+    """(fp64_tflops, fp32_tflops) FMA issue peaks measured on `device`."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    st = lib().surfatt_measure_peaks(int(device), ctypes.byref(a), ctypes.byref(b))
+    if st != OK:
+        raise SurfattError(st, "measure_peaks")
+    return a.value, b.value
 
 
 def last_status():
@@ -324,19 +334,25 @@ class Engine:
     def sync(self):
         return lib().surfatt_engine_sync(self._h)
 
-    def results(self, adj=True, density=True, tt=True, per_solve=True):
+    def results(self, adj=True, density=True, tt=True, per_solve=True, into=None):
+        """Copy the last run's results to host arrays (new arrays, or the
+        preallocated ones of `into`, e.g. pinned buffers)."""
         pb = self.pb
         out = {}
         r = _CResult()
         keep = []
 
         def buf(name, n, dt):
-            a = np.zeros(max(n, 1), dt)
+            if into is not None and name in into:
+                a = into[name]
+                assert a.dtype == dt and a.flags.c_contiguous and a.size >= max(n, 1)
+            else:
+                a = np.zeros(max(n, 1), dt)
             keep.append(a)
             out[name] = a
             return a.ctypes.data_as(_dp if dt == np.float64 else _ip)
 
-        chi = np.zeros(1)
+        chi = into["chi"] if into is not None and "chi" in into else np.zeros(1)
         out["chi"] = chi
         r.chi = chi.ctypes.data_as(_dp)
         if adj:
