@@ -245,6 +245,26 @@ surfatt_status_t surfatt_engine_work(surfatt_engine_t* engine, double* fwd_cell_
  * reference: these are the denominators of the sweep kernels' roofline. */
 surfatt_status_t surfatt_measure_peaks(int device, double* fp64_tflops, double* fp32_tflops);
 
+/* FSM_UW_PS_lonlat_2d on device arrays without allocating any memory.
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory when they call the solver (a host framework whose memory
+ * pool owns the HBM, or a loop that cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  All arrays are device pointers
+ * with the drop-in's layout; T (nx, ny) receives the travel times and
+ * status_iters[0..1] (device ints) the status and sweep iterations.  The
+ * solve is enqueued on `stream` (a cudaStream_t, NULL = default stream) and
+ * the call returns without waiting.  Scratch is a fixed array inside the
+ * library (about 4.8 MB per GPU, held until the process exits): grids above
+ * 16384 cells or 2048 nodes per axis are rejected with SURFATT_BAD_ARG.  The
+ * first call on a device looks up the scratch address and should come
+ * before any stream capture.  Calls share the scratch: calls that overlap on
+ * the GPU race and must be ordered (one stream, or events). */
+surfatt_status_t surfatt_uw_lonlat_solve_noalloc(const double* xx_deg, const double* yy_deg,
+                                                 int nx, int ny, const double* spha,
+                                                 const double* sphb, const double* sphc,
+                                                 const double* fun, double x0_deg, double y0_deg,
+                                                 double* T, int* status_iters, void* stream);
+
 /* Library version string. */
 const char* surfatt_version(void);
 

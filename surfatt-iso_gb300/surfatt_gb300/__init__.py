@@ -41,7 +41,7 @@ EXPORTED = [
     "surfatt_engine_create", "surfatt_engine_destroy", "surfatt_engine_load",
     "surfatt_engine_update_velocity", "surfatt_engine_run", "surfatt_engine_sync",
     "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
-    "surfatt_measure_peaks",
+    "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
 ]
 
 
@@ -114,6 +114,21 @@ def measure_peaks(device=0):
     if st != OK:
         raise SurfattError(st, "measure_peaks")
     return a.value, b.value
+
+
+def uw_lonlat_solve_noalloc(xx_deg, yy_deg, nx, ny, spha, sphb, sphc, fun, x0_deg, y0_deg, T,
+                            status_iters, stream=0):
+    """surfatt_uw_lonlat_solve_noalloc on device pointers (integers), e.g.
+    torch tensors' data_ptr(); enqueued on `stream`, returns the launch status.
+    For callers that must not allocate device memory at call time; the
+    library's fixed scratch limits grids to 16384 cells."""
+    L = lib()
+    f = L.surfatt_uw_lonlat_solve_noalloc
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                  ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    return f(xx_deg, yy_deg, int(nx), int(ny), spha, sphb, sphc, fun, float(x0_deg),
+             float(y0_deg), T, status_iters, stream)
 
 
 def last_status():
