@@ -46,7 +46,8 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config4"])
+    ap.add_argument("--workload", default="config2",
+                    choices=["config1", "config2", "config2s", "config4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -58,6 +59,10 @@ def _workload(name):
         obs = W.read_src_rec_tt(os.path.join(ROOT, "tests", "golden", "config1_src_rec.csv"))
         pb = W.config1(observed_tt=obs)
         desc = "config1: 2-D, 81x81 grid, 25 stations (600 paths), 1 period"
+    elif name == "config2s":
+        pb = W.config2(nsta=20)
+        desc = ("config2s: config 2 with 20 stations (16 periods, 380 solves, 120x120), "
+                "a bounded case for profiler captures")
     elif name == "config4":
         pb = W.config4()
         desc = "config4: 120 sources x 25 periods = 3000 solves, grids 64^2..384^2, 3-D mode"
@@ -238,10 +243,12 @@ def run_ours(args):
     eng.sync()
     r64 = eng.results()
     fwd64, adj64 = eng.work()
+    launch64 = eng.launch_config()
     eng.run(pb.mode, sg.PREC_FP32)
     eng.sync()
     r32 = eng.results()
     fwd32, adj32 = eng.work()
+    launch32 = eng.launch_config()
     err32 = _errors(r32, r64, pb)
 
     # plain FP64 (reported beside the headline)
@@ -350,6 +357,7 @@ def run_ours(args):
                          "kernel": "k_batch_fp32", "kernel_ms": k32_ms,
                          "flops_per_launch": flops32},
             "cpu_baseline": cpu, "parity": parity,
+            "launch": {"fp32": launch32, "fp64": launch64},
             "iterations": {"fwd_mean": float(np.mean(r32["fwd_iters"])),
                            "adj_mean": float(np.mean(r32["adj_iters"]))},
             "wall_s_timed_region": wall,

@@ -235,6 +235,11 @@ surfatt_status_t surfatt_engine_results(surfatt_engine_t* engine, surfatt_result
 surfatt_status_t surfatt_engine_timing(surfatt_engine_t* engine, double* total_ms,
                                        double* solve_kernel_ms, int* launches);
 
+/* Launch configuration of the last run's solve kernel: blocks, threads per
+ * block, resident blocks per SM, dynamic shared memory per block. */
+surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* engine, int* grid, int* block,
+                                              int* blocks_per_sm, size_t* smem_bytes);
+
 /* Total sweep cell visits of the last run (forward, adjoint), for the
  * algorithmic roofline. */
 surfatt_status_t surfatt_engine_work(surfatt_engine_t* engine, double* fwd_cell_updates,

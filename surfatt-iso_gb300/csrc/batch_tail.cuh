@@ -8,11 +8,11 @@
 
 namespace sgb {
 
-// Steps after the forward sweeps that do not depend on the sweep precision:
-// T -> receivers -> misfit -> adjoint -> mask -> kernel slot.
-__device__ inline void solve_tail(const BatchArgs& A, const PeriodDev& P, int s,
-                                  const double* T, const AdjWs& aw, SolveShared& sh,
-                                  int fwd_status, int fwd_iters) {
+// Receiver times (interp2 on the caller's degree grid), misfit and outlier
+// weights of solve s (src/measadj.f90:71-72, 82-84).  Leaves the block
+// synchronised; a receiver outside the grid sets sh.flag.
+__device__ inline void tail_receivers(const BatchArgs& A, const PeriodDev& P, int s,
+                                      const double* T, SolveShared& sh) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
   const int r0 = A.rec_off[s], nr = A.nrec[s];
@@ -43,6 +43,17 @@ __device__ inline void solve_tail(const BatchArgs& A, const PeriodDev& P, int s,
   if (A.Tout)
     for (size_t k = threadIdx.x; k < N; k += blockDim.x) A.Tout[A.kslot[s] + k] = T[k];
   __syncthreads();
+}
+
+// Steps of the plain FP64 solve after its forward sweeps:
+// T -> receivers -> misfit -> adjoint(s) -> mask -> kernel slot.
+__device__ inline void solve_tail(const BatchArgs& A, const PeriodDev& P, int s,
+                                  const double* T, const AdjWs& aw, SolveShared& sh,
+                                  int fwd_status, int fwd_iters) {
+  const int nx = P.nx, ny = P.ny;
+  const size_t N = (size_t)nx * ny;
+  const int r0 = A.rec_off[s], nr = A.nrec[s];
+  tail_receivers(A, P, s, T, sh);
   int st = fwd_status;
   if (sh.flag != ST_OK && st == ST_OK) st = sh.flag;
   int aiters = 0;

@@ -13,6 +13,7 @@
 
 #include "../../include/surfatt_gb300.h"
 #include "kernels.cuh"
+#include "launch.cuh"
 
 using namespace sgb;
 
@@ -89,7 +90,8 @@ struct PeriodBufs {
   PrepOut out() {
     return PrepOut{xs.as<double>(), ys.as<double>(), cosy.as<double>(), siny.as<double>(),
                    a.as<double>(), b.as<double>(), c.as<double>(), fun.as<double>(),
-                   f2.as<double>(), disx.as<double>(), disy.as<double>()};
+                   f2.as<double>(), disx.as<double>(), disy.as<double>(), nullptr, nullptr,
+                   nullptr, nullptr};
   }
   PeriodDev dev(int nx, int ny, int lonlat, double dx, double dy, const double* svel) {
     PeriodDev P;
@@ -113,6 +115,10 @@ struct PeriodBufs {
     P.disy = disy.as<double>();
     P.svel = svel;
     P.goff = 0;
+    P.f32 = nullptr;
+    P.isv = nullptr;
+    P.p4a = nullptr;
+    P.p4b = nullptr;
     return P;
   }
 };
@@ -467,14 +473,15 @@ struct surfatt_engine {
   std::vector<long long> kslot;
   // device buffers
   DBuf d_periods, d_xdeg, d_ydeg, d_xs, d_ys, d_cosy, d_siny, d_A, d_B, d_C, d_V, d_a, d_b, d_c,
-      d_fun, d_f2, d_disx, d_disy, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
+      d_fun, d_f2, d_disx, d_disy, d_f32, d_isv, d_p4a, d_p4b, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
       d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
   DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
       d_fupd, d_aupd, d_ws, d_queue;
-  int grid = 0, block = 128;
+  int grid = 0, block = 128, per_sm = 0, last_block = 0;
+  size_t last_smem = 0;
   std::vector<DBuf*> all() {
     return {&d_periods, &d_xdeg, &d_ydeg, &d_xs, &d_ys, &d_cosy, &d_siny, &d_A, &d_B, &d_C,
-            &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_pidx, &d_srcx, &d_srcy,
+            &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_f32, &d_isv, &d_p4a, &d_p4b, &d_pidx, &d_srcx, &d_srcy,
             &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
             &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
             &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
@@ -509,7 +516,9 @@ int run_prep_all(surfatt_engine* e) {
                 e->d_cosy.as<double>() + e->yoff[p], e->d_siny.as<double>() + e->yoff[p],
                 e->d_a.as<double>() + g, e->d_b.as<double>() + g, e->d_c.as<double>() + g,
                 e->d_fun.as<double>() + g, e->d_f2.as<double>() + g,
-                e->d_disx.as<double>() + g, e->d_disy.as<double>() + g};
+                e->d_disx.as<double>() + g, e->d_disy.as<double>() + g,
+                e->d_f32.as<float>() + 6 * g, e->d_isv.as<double>() + 2 * g,
+                e->d_p4a.as<float4>() + g, e->d_p4b.as<float4>() + g};
     launch_prep(in, out, e->st);
   }
   CK(cudaGetLastError());
@@ -622,6 +631,8 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
        up(e, e->d_V, pb->svel, NC);
   for (DBuf* b : {&e->d_a, &e->d_b, &e->d_c, &e->d_fun, &e->d_f2, &e->d_disx, &e->d_disy})
     r |= up(e, *b, (double*)nullptr, NC);
+  r |= up(e, e->d_f32, (float*)nullptr, 6 * NC) | up(e, e->d_isv, (double*)nullptr, 2 * NC);
+  r |= up(e, e->d_p4a, (float4*)nullptr, NC) | up(e, e->d_p4b, (float4*)nullptr, NC);
   r |= up(e, e->d_pidx, pb->pidx, ns) | up(e, e->d_srcx, pb->srcx, ns) |
        up(e, e->d_srcy, pb->srcy, ns) | up(e, e->d_rec_off, pb->rec_off, ns) |
        up(e, e->d_nrec, pb->nrec, ns);
@@ -671,6 +682,10 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
     P.disy = e->d_disy.as<double>() + g;
     P.svel = e->d_V.as<double>() + g;
     P.goff = g;
+    P.f32 = e->d_f32.as<float>() + 6 * g;
+    P.isv = e->d_isv.as<double>() + 2 * g;
+    P.p4a = e->d_p4a.as<float4>() + g;
+    P.p4b = e->d_p4b.as<float4>() + g;
   }
   r = up(e, e->d_periods, e->periods.data(), np);
   if (r) return (surfatt_status_t)r;
@@ -695,20 +710,20 @@ surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
     return SURFATT_BAD_ARG;
   if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
   CK(cudaSetDevice(e->device));
-  cudaDeviceProp prop;
-  CK(cudaGetDeviceProperties(&prop, e->device));
-  const int block = e->block;
-  int per_sm = prec == SURFATT_PREC_FP64 ? batch_fp64_max_blocks_per_sm(block)
-                                         : batch_fp32_max_blocks_per_sm(block);
-  if (per_sm < 1) per_sm = 1;
-  int grid = prop.multiProcessorCount * per_sm;
-  if (grid > e->nsolve) grid = std::max(1, e->nsolve);
-  const long long wsd = prec == SURFATT_PREC_FP64 ? batch_fp64_ws_doubles(e->max_cells)
-                                                 : batch_fp32_ws_doubles(e->max_cells);
-  int r = eng_ensure(e, e->d_ws, (size_t)grid * wsd * sizeof(double));
+  EvalShape sh;
+  sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
+  LaunchPlan plan;
+  int r = plan_evaluation(sh, prec == SURFATT_PREC_FP64 ? 0 : 1, e->device, 0, &plan);
   if (r) return (surfatt_status_t)r;
-  e->grid = grid;
-  BatchArgs A;
+  r = eng_ensure(e, e->d_ws,
+                 (size_t)plan.grid * plan.slots_per_block * plan.ws_doubles * sizeof(double));
+  if (r) return (surfatt_status_t)r;
+  e->grid = plan.grid;
+  e->per_sm = plan.per_sm;
+  e->last_block = plan.block;
+  e->last_smem = plan.smem;
+  EvalDev dev;
+  BatchArgs& A = dev.args;
   A.periods = e->d_periods.as<PeriodDev>();
   A.nsolve = e->nsolve;
   A.order = e->d_order.as<int>();
@@ -723,7 +738,6 @@ surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
   A.weight = e->d_weight.as<double>();
   A.path = e->d_path.as<int>();
   A.kslot = e->d_kslot.as<long long>();
-  A.mode = mode;
   A.tekio = e->d_tekio.as<double>();
   A.wgt_eff = e->d_wgt.as<double>();
   A.tt_fwd = e->d_ttfwd.as<double>();
@@ -736,41 +750,21 @@ surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
   A.fwd_updates = e->d_fupd.as<double>();
   A.adj_updates = e->d_aupd.as<double>();
   A.Tout = nullptr;
-  A.ws = e->d_ws.as<double>();
-  A.ws_doubles = wsd;
-  A.queue = e->d_queue.as<int>();
-  A.block = block;
-  e->launches = 0;
+  dev.plist_off = e->d_plist_off.as<int>();
+  dev.plist = e->d_plist.as<int>();
+  dev.goff = e->d_goff.as<long long>();
+  dev.nx = e->d_nx.as<int>();
+  dev.ny = e->d_ny.as<int>();
+  dev.chi_total = e->d_chi.as<double>();
+  dev.adj_s = e->d_adj.as<double>();
+  dev.adj_density = e->d_adjd.as<double>();
   CK(cudaEventRecord(e->ev0, e->st));
-  CK(cudaMemsetAsync(e->d_queue.p, 0, sizeof(int), e->st));
-  CK(cudaMemsetAsync(e->d_ttfwd.p, 0, std::max(1, e->npath) * sizeof(double), e->st));
-  CK(cudaMemsetAsync(e->d_aupd.p, 0, std::max(1, e->nsolve) * sizeof(double), e->st));
-  CK(cudaEventRecord(e->evk0, e->st));
-  if (e->nsolve > 0) {
-    if (prec == SURFATT_PREC_FP64) launch_batch_fp64(A, grid, block, e->st);
-    else launch_batch_fp32(A, grid, block, e->st);
-    e->launches++;
-  }
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(e->evk1, e->st));
-  if (mode >= 2) {
-    launch_kernel_reduce(nullptr, e->nperiod, e->d_plist_off.as<int>(), e->d_plist.as<int>(),
-                         e->d_kslot.as<long long>(), e->d_kc.as<double>(), e->d_adj.as<double>(),
-                         e->ncell, e->d_goff.as<long long>(), e->d_nx.as<int>(),
-                         e->d_ny.as<int>(), e->st);
-    e->launches++;
-    if (mode == 3) {
-      launch_kernel_reduce(nullptr, e->nperiod, e->d_plist_off.as<int>(), e->d_plist.as<int>(),
-                           e->d_kslot.as<long long>(), e->d_kcd.as<double>(),
-                           e->d_adjd.as<double>(), e->ncell, e->d_goff.as<long long>(),
-                           e->d_nx.as<int>(), e->d_ny.as<int>(), e->st);
-      e->launches++;
-    }
-  }
-  launch_chi_reduce(e->d_chis.as<double>(), e->nsolve, e->d_chi.as<double>(), e->st);
-  e->launches++;
-  CK(cudaGetLastError());
+  const int n = enqueue_evaluation(sh, dev, plan, mode, prec == SURFATT_PREC_FP64 ? 0 : 1,
+                                   e->d_ws.as<double>(), e->d_queue.as<int>(), e->st, e->evk0,
+                                   e->evk1);
+  if (n < 0) return (surfatt_status_t)(-n);
   CK(cudaEventRecord(e->ev1, e->st));
+  e->launches = n;
   e->ran = true;
   e->last_mode = mode;
   return SURFATT_OK;
@@ -829,6 +823,16 @@ surfatt_status_t surfatt_engine_timing(surfatt_engine_t* e, double* total_ms,
   if (total_ms) *total_ms = a;
   if (solve_kernel_ms) *solve_kernel_ms = b;
   if (launches) *launches = e->launches;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* e, int* grid, int* block,
+                                              int* blocks_per_sm, size_t* smem_bytes) {
+  if (!e || !e->ran) return SURFATT_BAD_ARG;
+  if (grid) *grid = e->grid;
+  if (block) *block = e->last_block;
+  if (blocks_per_sm) *blocks_per_sm = e->per_sm;
+  if (smem_bytes) *smem_bytes = e->last_smem;
   return SURFATT_OK;
 }
 

@@ -53,6 +53,14 @@ struct PeriodDev {
   const double* disy;                  // sqrt(fun**2*(a/(a*b-c**2)))  (:1055)
   const double* svel;                  // phase velocity (kernel division)
   long long goff;                      // cell offset of the period in packed arrays
+  // FP32 copies for the FP32-factored sweeps (null when not prepared):
+  // f32 + m*N, m = 0..5: a, b, c, fun**2, disx, disy
+  const float* f32;
+  // 1/svel**2 and 1/svel**3 (isv, isv + N) for the FP32 path's kernel slots
+  const double* isv;
+  // per-cell FP32 records: {a, b, c, fun**2} and {disx, disy, 1/svel**2, 1/svel**3}
+  const float4* p4a;
+  const float4* p4b;
 };
 
 // Source/receiver cell and REAL(4) bilinear weights:

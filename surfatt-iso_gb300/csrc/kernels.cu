@@ -54,6 +54,29 @@ __global__ void k_prep(PrepIn in, PrepOut out) {
     out.f2[k] = f * f;
     out.disx[k] = sqrt(f * f * (b / (a * b - c * c)));
     out.disy[k] = sqrt(f * f * (a / (a * b - c * c)));
+    if (out.f32) {
+      out.f32[k] = (float)a;
+      out.f32[N + k] = (float)b;
+      out.f32[2 * N + k] = (float)c;
+      out.f32[3 * N + k] = (float)(f * f);
+      out.f32[4 * N + k] = (float)out.disx[k];
+      out.f32[5 * N + k] = (float)out.disy[k];
+    }
+    if (out.isv && in.from_model) {
+      const double v = in.V[k];
+      out.isv[k] = 1.0 / (v * v);
+      out.isv[N + k] = 1.0 / (v * v * v);
+    }
+    if (out.p4a) out.p4a[k] = make_float4((float)a, (float)b, (float)c, (float)(f * f));
+    if (out.p4b) {
+      float i2 = 0.f, i3 = 0.f;
+      if (in.from_model) {
+        const double v = in.V[k];
+        i2 = (float)(1.0 / (v * v));
+        i3 = (float)(1.0 / (v * v * v));
+      }
+      out.p4b[k] = make_float4((float)out.disx[k], (float)out.disy[k], i2, i3);
+    }
   }
 }
 
@@ -176,6 +199,30 @@ void launch_kernel_reduce(const PeriodDev* /*periods_host*/, int nperiod, const 
   dim3 grid(64, nperiod);
   k_kernel_reduce<<<grid, 256, 0, st>>>(nperiod, plist_off, plist, kslot, contrib, out,
                                         goff_dev, nx_dev, ny_dev);
+}
+
+__global__ void k_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plist,
+                                    const long long* kslot, const float* contrib, double* out,
+                                    const long long* goff, const int* nxs, const int* nys) {
+  const int p = blockIdx.y;
+  if (p >= nperiod) return;
+  const long long N = (long long)nxs[p] * nys[p];
+  const int s0 = plist_off[p], s1 = plist_off[p + 1];
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < N;
+       k += (long long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int q = s0; q < s1; ++q) acc = acc + (double)contrib[kslot[plist[q]] + k];
+    out[goff[p] + k] = acc;
+  }
+}
+
+void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plist,
+                              const long long* kslot, const float* contrib, double* out,
+                              const long long* goff_dev, const int* nx_dev, const int* ny_dev,
+                              cudaStream_t st) {
+  dim3 grid(64, nperiod);
+  k_kernel_reduce_f32<<<grid, 256, 0, st>>>(nperiod, plist_off, plist, kslot, contrib, out,
+                                            goff_dev, nx_dev, ny_dev);
 }
 
 __global__ void k_chi_reduce(const double* chi_s, int n, double* out) {

@@ -24,6 +24,10 @@ struct PrepIn {
 // Outputs (device, N per field, nx/ny per axis) -- referenced by PeriodDev.
 struct PrepOut {
   double *xs, *ys, *cosy, *siny, *a, *b, *c, *fun, *f2, *disx, *disy;
+  float* f32;   // optional (6N): FP32 a, b, c, fun**2, disx, disy
+  double* isv;  // optional (2N): 1/svel**2, 1/svel**3 (model inputs only)
+  float4* p4a;  // optional (N): {a, b, c, fun**2}
+  float4* p4b;  // optional (N): {disx, disy, 1/svel**2, 1/svel**3}
 };
 
 // Batched evaluation arguments (all device pointers).
@@ -61,13 +65,21 @@ struct BatchArgs {
   long long ws_doubles;
   int* queue;              // work counter (zeroed before launch)
   int block;               // threads per block (for info)
+  int max_nx;              // largest nx over periods (shared-memory column arrays)
+  int smem_tau;            // FP32 kernel: 1 = tau / Ta in shared memory
+  size_t smem_bytes;       // FP32 kernel: dynamic shared memory per block
 };
 
 void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st);
 void launch_batch_fp64(const BatchArgs& a, int grid, int block, cudaStream_t st);
 void launch_batch_fp32(const BatchArgs& a, int grid, int block, cudaStream_t st);
 int batch_fp64_max_blocks_per_sm(int block);
-int batch_fp32_max_blocks_per_sm(int block);
+int batch_fp32_max_blocks_per_sm(int block, size_t smem_bytes, int smem_tau);
+// Dynamic shared memory of the FP32 kernel: the column cos/sin arrays, plus
+// tau when every grid (pitched: pitch*ny cells) fits; *tau_resident says which.
+size_t batch_fp32_smem_bytes(long long max_pitched_cells, int max_nx, int* tau_resident);
+int batch_fp32_pitch(int nx);
+constexpr int kFp32MaxThreads = 512;
 // workspace doubles per solve slot for a grid of N cells
 long long batch_fp64_ws_doubles(long long N);
 long long batch_fp32_ws_doubles(long long N);
@@ -78,6 +90,16 @@ void launch_kernel_reduce(const PeriodDev* periods_host, int nperiod, const int*
                           const int* plist, const long long* kslot, const double* contrib,
                           double* out, long long ncell, const long long* goff_dev,
                           const int* nx_dev, const int* ny_dev, cudaStream_t st);
+// Same with FP32 per-solve slots, summed in FP64.
+void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plist,
+                              const long long* kslot, const float* contrib, double* out,
+                              const long long* goff_dev, const int* nx_dev, const int* ny_dev,
+                              cudaStream_t st);
+// Warp-per-solve FP32 kernel (grids of at most 32*bands rows).
+void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st);
+int batch_fp32w_max_blocks_per_sm(int bands);
+long long batch_fp32w_ws_doubles(long long N);
+int fp32w_bands(int max_ny);
 // chi = sum of per-solve misfits in work-list order (src/acqui.f90:135)
 void launch_chi_reduce(const double* chi_s, int nsolve, double* chi_out, cudaStream_t st);
 

@@ -1,0 +1,778 @@
+// kernels_fp32w.cu -- FP32-factored batched solve, one warp per (period,
+// source) solve, for grids of at most 128 rows.
+//
+// Wavefront without block barriers.  In each of the four sweeps, lane l owns
+// the logical rows v = l + 32*m (m < MB) and at step t visits the cell
+// u = t - v of each of its rows.  Of the four stencil neighbours of (u, v),
+// the two already updated in this sweep come from registers: (u-1, v) is the
+// lane's own previous result, (u, v-1) the previous result of the lane below
+// (one __shfl_up; lane 0 takes lane 31's value of the band below).  The two
+// not yet updated, (u+1, v) and (u, v+1), are read from global memory a step
+// ahead (they are rewritten only after that read), together with the cell's
+// operands.  Visiting u = t - v for every row reproduces the reference's
+// in-place Gauss-Seidel order exactly (a cell's up-/left-stream neighbours
+// are final, its down-/right-stream ones are old), with one __syncwarp() per
+// step instead of a block barrier and no shared memory, so a GPU holds one
+// resident solve per warp (register-bound) rather than per block.
+//
+// Precision (the FP32-factored form): tau and the adjoint fields are FP32;
+// the sweep update is the tau = tau_X + delta form of the block kernel.  T0
+// and its gradient come from the haversine form of the reference's
+// great-circle distance (well conditioned at small distances) in FP32, and
+// in FP64 with the reference's own formula within two cells of the source.
+// Misfit, receiver times, the convergence decisions (FP64 reduction of the
+// lanes' partial sums) and the per-period kernel sums are FP64.
+#include "kernels.cuh"
+#include "solver_fp64.cuh"
+
+namespace sgb {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Workspace per warp slot: S (float4: T0, T0x, T0y, -), W (float4 adjoint
+// weights), tau, old, 1/d, two scaled adjoint sources.
+long long batch_fp32w_ws_doubles(long long N) {
+  const long long floats = 8 * N + 5 * N + 2 * 4096;
+  long long d = (floats + 1) / 2 + 64;
+  return (d + 31) / 32 * 32;  // keep every slot 256-byte aligned
+}
+
+struct WSlot {
+  float4* S;
+  float4* W;
+  float* tau;
+  float* old;
+  float* id;
+  float* src[2];
+  float* col;  // per column sin and cos of half the longitude offset (2 * nx)
+};
+
+__device__ inline WSlot wcarve(double* base, size_t N) {
+  WSlot V;
+  V.S = reinterpret_cast<float4*>(base);
+  V.W = V.S + N;
+  V.tau = reinterpret_cast<float*>(V.W + N);
+  V.old = V.tau + N;
+  V.id = V.old + N;
+  V.src[0] = V.id + N;
+  V.src[1] = V.src[0] + N;
+  V.col = V.src[1] + N;
+  return V;
+}
+
+struct WSolve {
+  int status;
+  double fun0;
+  Box box;   // frozen source box
+  Box mbox;  // mask box (|x-x0| < 1.5 dx, |y-y0| < 1.5 dy)
+  int si, sj;  // source cell
+};
+
+__device__ __forceinline__ double shfl_d(double v, int src) {
+  return __shfl_sync(FULL, v, src);
+}
+
+// ---------------------------------------------------------------------------
+// setup
+// ---------------------------------------------------------------------------
+__device__ inline WSolve w_locate(const PeriodDev& P, double x0, double y0, double xd0,
+                                  double yd0, int lane) {
+  WSolve w;
+  const int nx = P.nx, ny = P.ny;
+  if (lane == 0) {
+    w.status = ST_OK;
+    w.fun0 = 0;
+    float r1 = 0.f, r2 = 0.f;
+    const int i0 = locate_cell(P.xs, nx - 1, P.dx, x0, &r1);
+    const int j0 = locate_cell(P.ys, ny - 1, P.dy, y0, &r2);
+    if (i0 < 0 || j0 < 0) {
+      w.status = ST_BAD_ARG;
+      w.si = w.sj = 0;
+    } else {
+      float w00 = (1 - r1) * (1 - r2), w01 = (1 - r1) * r2, w10 = r1 * (1 - r2), w11 = r1 * r2;
+      const size_t k00 = i0 + (size_t)nx * j0;
+      w.fun0 = (double)w00 * P.fun[k00] + (double)w01 * P.fun[k00 + nx] +
+               (double)w10 * P.fun[k00 + 1] + (double)w11 * P.fun[k00 + nx + 1];
+      w.si = i0;
+      w.sj = j0;
+    }
+    int a0 = nx, a1 = -1, b0 = ny, b1 = -1, c0 = nx, c1 = -1, e0 = ny, e1 = -1;
+    const double ddx = P.xdeg[1] - P.xdeg[0], ddy = P.ydeg[1] - P.ydeg[0];
+    for (int i = 0; i < nx; ++i) {
+      if (fabs((P.xs[i] - x0) / P.dx) <= 1.0) { a0 = min(a0, i); a1 = max(a1, i); }
+      if (fabs(P.xdeg[i] - xd0) < 1.5 * ddx) { c0 = min(c0, i); c1 = max(c1, i); }
+    }
+    for (int j = 0; j < ny; ++j) {
+      if (fabs((P.ys[j] - y0) / P.dy) <= 1.0) { b0 = min(b0, j); b1 = max(b1, j); }
+      if (fabs(P.ydeg[j] - yd0) < 1.5 * ddy) { e0 = min(e0, j); e1 = max(e1, j); }
+    }
+    w.box = Box{a0, a1, b0, b1};
+    w.mbox = Box{c0, c1, e0, e1};
+    if (w.status == ST_OK && a0 <= a1 && b0 <= b1 &&
+        (a0 == 0 || a1 == nx - 1 || b0 == 0 || b1 == ny - 1))
+      w.status = ST_SOURCE_ON_BOUNDARY;
+  }
+  w.status = __shfl_sync(FULL, w.status, 0);
+  w.fun0 = shfl_d(w.fun0, 0);
+  w.si = __shfl_sync(FULL, w.si, 0);
+  w.sj = __shfl_sync(FULL, w.sj, 0);
+  w.box.i0 = __shfl_sync(FULL, w.box.i0, 0);
+  w.box.i1 = __shfl_sync(FULL, w.box.i1, 0);
+  w.box.j0 = __shfl_sync(FULL, w.box.j0, 0);
+  w.box.j1 = __shfl_sync(FULL, w.box.j1, 0);
+  w.mbox.i0 = __shfl_sync(FULL, w.mbox.i0, 0);
+  w.mbox.i1 = __shfl_sync(FULL, w.mbox.i1, 0);
+  w.mbox.j0 = __shfl_sync(FULL, w.mbox.j0, 0);
+  w.mbox.j1 = __shfl_sync(FULL, w.mbox.j1, 0);
+  return w;
+}
+
+// T0, T0x, T0y of every cell into S; tau initialised (1 in the frozen box).
+// d = 2 asin(sqrt(h)), h = sin^2(dy/2) + cos y cos y0 sin^2(dx/2), is the
+// reference's acos(sin y sin y0 + cos y cos y0 cos dx) without its
+// cancellation; sin d = 2 sqrt(h (1-h)).
+__device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSolve& w,
+                            const WSlot& V, int lane) {
+  const int nx = P.nx, ny = P.ny;
+  const double rf = R_EARTH * w.fun0;
+  const float rff = (float)rf;
+  const float cy0 = (float)cos(y0);
+  const double cy0d = cos(y0), sy0d = sin(y0);
+  for (int i = lane; i < nx; i += 32) {
+    const float hx = (float)((P.xs[i] - x0) * 0.5);
+    V.col[i] = sinf(hx);
+    V.col[nx + i] = cosf(hx);
+  }
+  __syncwarp();
+  for (int j = 0; j < ny; ++j) {
+    const float hy = (float)((P.ys[j] - y0) * 0.5);
+    const float shy = sinf(hy), chy = cosf(hy);
+    const float cy = (float)P.cosy[j], sy = (float)P.siny[j];
+    for (int i = lane; i < nx; i += 32) {
+      const size_t k = i + (size_t)nx * j;
+      const float shx = V.col[i], chx = V.col[nx + i];
+      float t0, gx, gy;
+      if (abs(i - w.si) <= 2 && abs(j - w.sj) <= 2) {
+        // near the source: the reference's FP64 expressions (:847-856)
+        const double cyy = P.cosy[j], syy = P.siny[j];
+        const double cdx = cos(P.xs[i] - x0), sdx = sin(P.xs[i] - x0);
+        const double tmp = syy * sy0d + cyy * cy0d * cdx;
+        double cl = tmp < 1.0 ? tmp : 1.0;
+        cl = cl > -1.0 ? cl : -1.0;
+        const double td = acos(cl) * R_EARTH * w.fun0;
+        double tx = 0, ty = 0;
+        if (td != 0) {
+          const double rs = 1.0 / sqrt(1 - tmp * tmp);
+          tx = -(rs * cyy * cy0d * (-1.0) * sdx * R_EARTH * w.fun0);
+          ty = -(rs * (cyy * sy0d - syy * cy0d * cdx) * R_EARTH * w.fun0);
+        }
+        t0 = (float)td;
+        gx = (float)tx;
+        gy = (float)ty;
+      } else {
+        const float h = shy * shy + cy * cy0 * (shx * shx);
+        const float sh = sqrtf(h);
+        const float d = 2.f * asinf(fminf(sh, 1.f));
+        const float sind = 2.f * sh * sqrtf(fmaxf(1.f - h, 0.f));
+        t0 = rff * d;
+        if (sind > 0.f) {
+          const float inv = rff / sind;
+          gx = inv * cy * cy0 * (2.f * shx * chx);
+          // -(cos y sin y0 - sin y cos y0 cos dx) = -(sin(y0-y) + 2 sin y cos y0 sin^2(dx/2))
+          gy = -inv * (-2.f * shy * chy + 2.f * sy * cy0 * (shx * shx));
+        } else {
+          gx = 0.f;
+          gy = 0.f;
+        }
+      }
+      V.S[k] = make_float4(t0, gx, gy, 0.f);
+      V.tau[k] = w.box.has(i, j) ? 1.0f : 10.0f;
+    }
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// forward sweep visit (tau = tau_X + delta form, FP32x2 pairs)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 wbc(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 wadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 wmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 wfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 wneg(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ float w_pick(float r, float chx, float chy, float sx, float sy, bool ok) {
+  const bool cx = sx > 0.f ? chx >= 0.f : chx <= 0.f;
+  const bool cy = sy > 0.f ? chy >= 0.f : chy <= 0.f;
+  return (ok && cx && cy) ? r : __int_as_float(0x7f800000);
+}
+
+__device__ __forceinline__ float w_two_sided(float2 px, float2 tX, float2 U0, float py, float tY,
+                                             float sY, float gy, float cy, float a, float b,
+                                             float c, float f2, bool okx, bool oky) {
+  const float2 A = wfma(px, wfma(wbc(a), px, wbc(-2.f * c * py)), wbc(b * py * py));
+  const float2 bx = wfma(wbc(a), px, wbc(-c * py));
+  const float2 by = wfma(wbc(-c), px, wbc(b * py));
+  const float2 V0 = wfma(wbc(gy), tX, wmul(wbc(-sY * cy), wadd(tX, wbc(-tY))));
+  const float2 CU = wfma(wbc(a), U0, wmul(wbc(-c), V0));
+  const float2 CV = wfma(wbc(b), V0, wmul(wbc(-c), U0));
+  const float2 C = wfma(U0, CU, wfma(V0, CV, wbc(-f2)));
+  const float2 H = wfma(bx, U0, wmul(by, V0));
+  const float2 D = wfma(H, H, wmul(wneg(A), C));
+  const bool vx = okx && D.x >= 0.f, vy = oky && D.y >= 0.f;
+  const float2 sq = make_float2(sqrtf(fmaxf(D.x, 0.f)), sqrtf(fmaxf(D.y, 0.f)));
+  const float2 ia = make_float2(__frcp_rn(A.x), __frcp_rn(A.y));
+  const float2 d1 = wmul(wadd(sq, wneg(H)), ia);
+  const float2 d2 = wmul(wadd(wneg(sq), wneg(H)), ia);
+  const float2 x1 = wfma(bx, d1, CU), y1 = wfma(by, d1, CV);
+  const float2 x2 = wfma(bx, d2, CU), y2 = wfma(by, d2, CV);
+  const float2 r1 = wadd(tX, d1), r2 = wadd(tX, d2);
+  const float sy = -sY;
+  float m = w_pick(r1.x, x1.x, y1.x, 1.f, sy, vx);
+  m = fminf(m, w_pick(r2.x, x2.x, y2.x, 1.f, sy, vx));
+  m = fminf(m, w_pick(r1.y, x1.y, y1.y, -1.f, sy, vy));
+  m = fminf(m, w_pick(r2.y, x2.y, y2.y, -1.f, sy, vy));
+  return m;
+}
+
+__device__ __forceinline__ float w_one_sided(float2 p, float2 tnb, float2 t0nb, float g,
+                                             float dis, float t0, bool okx, bool oky) {
+  const float2 ip = make_float2(__frcp_rn(p.x), __frcp_rn(p.y));
+  const float2 gt = wmul(wbc(g), tnb);
+  const float2 r1 = wfma(wadd(wbc(dis), wneg(gt)), ip, tnb);
+  const float2 r2 = wfma(wadd(wbc(-dis), wneg(gt)), ip, tnb);
+  const float2 lim = wmul(tnb, t0nb), half = wmul(tnb, wbc(0.5f));
+  const float2 s1 = wmul(r1, wbc(t0)), s2 = wmul(r2, wbc(t0));
+  const float inf = __int_as_float(0x7f800000);
+  float m = (okx && s1.x >= lim.x && r1.x > half.x) ? r1.x : inf;
+  m = fminf(m, (okx && s2.x >= lim.x && r2.x > half.x) ? r2.x : inf);
+  m = fminf(m, (oky && s1.y >= lim.y && r1.y > half.y) ? r1.y : inf);
+  m = fminf(m, (oky && s2.y >= lim.y && r2.y > half.y) ? r2.y : inf);
+  return m;
+}
+
+// Operands of one forward visit, loaded a step ahead.  The downstream
+// neighbours are not loaded here: the logical east cell (u+1, v) is this
+// band's next cell and the logical north cell (u, v+1) is the next cell of
+// the lane above, so their old tau and T0 come from `nxt` (own register or
+// __shfl_down); the south T0 comes from the lane below (__shfl_up).
+struct WFwd {
+  bool on, frz;
+  float own, old;  // old tau of the cell; tau at the start of the iteration
+  float t0, gx, gy;
+  float4 pa;       // a, b, c, fun^2
+  float dsx, dsy;
+};
+
+__device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, int xdir, int ydir,
+                                        const PeriodDev& P, const WSlot& V, const Box& box,
+                                        bool last) {
+  const int u = t - v;
+  o.on = v < ny && u >= 0 && u < nx;
+  if (!o.on) {
+    o.own = 0.f;
+    o.t0 = 0.f;
+    return;
+  }
+  const int i = xdir > 0 ? u : nx - 1 - u;
+  const int j = ydir > 0 ? v : ny - 1 - v;
+  const int k = i + nx * j;
+  o.frz = box.has(i, j);
+  o.own = V.tau[k];
+  const float4 sv = V.S[k];
+  o.t0 = sv.x;
+  o.gx = sv.y;
+  o.gy = sv.z;
+  o.pa = P.p4a[k];
+  const float4 pb = P.p4b[k];
+  o.dsx = pb.x;
+  o.dsy = pb.y;
+  if (last) o.old = V.old[k];
+}
+
+// Visit with logical neighbours mapped to the physical W/E/S/N of the
+// reference's update.  west/south: new values; east/north: old values.
+__device__ __forceinline__ float wf_visit(const WFwd& o, float west, float east, float south,
+                                          float north, float t0w, float t0e, float t0s, float t0n,
+                                          bool hasw, bool hass, bool hase, bool hasn, int xdir,
+                                          int ydir, float idx, float idy) {
+  const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
+  const float ts = ydir > 0 ? south : north, tn = ydir > 0 ? north : south;
+  const bool hw = xdir > 0 ? hasw : hase, he = xdir > 0 ? hase : hasw;
+  const bool hs = ydir > 0 ? hass : hasn, hn = ydir > 0 ? hasn : hass;
+  const float t0wp = xdir > 0 ? t0w : t0e, t0ep = xdir > 0 ? t0e : t0w;
+  const float t0sp = ydir > 0 ? t0s : t0n, t0np = ydir > 0 ? t0n : t0s;
+  const float t0 = o.t0, gx = o.gx, gy = o.gy;
+  const float a = o.pa.x, b = o.pa.y, c = o.pa.z, f2 = o.pa.w;
+  const float cx = t0 * idx, cy = t0 * idy;
+  const float2 px = make_float2(gx + cx, gx - cx);
+  const float2 tX = make_float2(tw, te);
+  const float2 U0 = wmul(wbc(gx), tX);
+  float m = w_two_sided(px, tX, U0, gy + cy, ts, -1.f, gy, cy, a, b, c, f2, hw && hs, he && hs);
+  m = fminf(m, w_two_sided(px, tX, U0, gy - cy, tn, 1.f, gy, cy, a, b, c, f2, hw && hn, he && hn));
+  m = fminf(m, w_one_sided(px, tX, make_float2(t0wp, t0ep), gx, o.dsx, t0, hw, he));
+  m = fminf(m, w_one_sided(make_float2(gy + cy, gy - cy), make_float2(ts, tn),
+                           make_float2(t0sp, t0np), gy, o.dsy, t0, hs, hn));
+  return fminf(o.own, m);
+}
+
+// Value of row v-1 held by the lane below (lane 31 of the band below for lane 0).
+template <int MB>
+__device__ __forceinline__ void w_from_below(const float (&x)[MB], float (&out)[MB], int lane) {
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    const float up = __shfl_up_sync(FULL, x[m], 1);
+    const float wr = __shfl_sync(FULL, x[m > 0 ? m - 1 : 0], 31);
+    out[m] = lane > 0 ? up : wr;
+  }
+}
+
+// Value of row v+1 held by the lane above (lane 0 of the band above for lane 31).
+template <int MB>
+__device__ __forceinline__ void w_from_above(const float (&x)[MB], float (&out)[MB], int lane) {
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    const float dn = __shfl_down_sync(FULL, x[m], 1);
+    const float wr = __shfl_sync(FULL, x[m + 1 < MB ? m + 1 : m], 0);
+    out[m] = lane < 31 ? dn : wr;
+  }
+}
+
+template <int MB>
+__device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w, int lane,
+                                    int* status_out, int* iters_out) {
+  const int nx = P.nx, ny = P.ny;
+  const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
+  const int nsteps = nx + ny - 1;
+  int iter, status = ST_NOT_CONVERGED;
+  for (iter = 1; iter <= MAXITER_UW; ++iter) {
+    float l1 = 0.f, lmax = 0.f;
+    for (int s = 0; s < 4; ++s) {
+      int xdir, ydir;
+      sweep_dirs(s, xdir, ydir);
+      const bool last = s == 3;
+      float res[MB], t0prev[MB];
+      WFwd cur[MB];
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        res[m] = 0.f;
+        t0prev[m] = 0.f;
+        wf_load(cur[m], 0, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+      }
+      for (int t = 0; t < nsteps; ++t) {
+        WFwd nxt[MB];
+#pragma unroll
+        for (int m = 0; m < MB; ++m)
+          wf_load(nxt[m], t + 1, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+        float south[MB], t0s[MB], north[MB], t0n[MB], nown[MB], nt0[MB];
+#pragma unroll
+        for (int m = 0; m < MB; ++m) {
+          nown[m] = nxt[m].own;
+          nt0[m] = nxt[m].t0;
+        }
+        w_from_below<MB>(res, south, lane);
+        w_from_below<MB>(t0prev, t0s, lane);
+        w_from_above<MB>(nown, north, lane);
+        w_from_above<MB>(nt0, t0n, lane);
+#pragma unroll
+        for (int m = 0; m < MB; ++m) {
+          if (cur[m].on) {
+            const int v = lane + 32 * m, u = t - v;
+            const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? v : ny - 1 - v);
+            float nv;
+            if (cur[m].frz) {
+              nv = cur[m].own;
+            } else {
+              nv = wf_visit(cur[m], res[m], nown[m], south[m], north[m], t0prev[m], nt0[m],
+                            t0s[m], t0n[m], u > 0, v > 0, u < nx - 1, v < ny - 1, xdir, ydir,
+                            idx, idy);
+            }
+            V.tau[k] = nv;
+            if (s == 0) V.old[k] = cur[m].own;
+            if (last && !cur[m].frz) {
+              const float dd = fabsf(nv - cur[m].old) * cur[m].t0;
+              l1 += dd;
+              lmax = fmaxf(lmax, dd);
+            }
+            res[m] = nv;
+            t0prev[m] = cur[m].t0;
+          }
+          cur[m] = nxt[m];
+        }
+        __syncwarp();
+      }
+    }
+    // FP64 decision over the lanes' partial sums (:1091-1115)
+    double sl1 = (double)l1, smax = (double)lmax;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sl1 += __shfl_xor_sync(FULL, sl1, o);
+      smax = fmax(smax, __shfl_xor_sync(FULL, smax, o));
+    }
+    sl1 = sl1 / (double)nx / (double)ny;
+    if (fabs(sl1) < TOL_UW && smax < TOL_UW) {
+      status = ST_OK;
+      break;
+    }
+  }
+  *status_out = status;
+  *iters_out = iter > MAXITER_UW ? MAXITER_UW : iter;
+}
+
+// ---------------------------------------------------------------------------
+// adjoint
+// ---------------------------------------------------------------------------
+// Weights of Ta = src + ww*Ta_W + we*Ta_E + ws*Ta_S + wn*Ta_N (face fluxes of
+// :1348-1370 with T = tau*T0 in FP32) and 1/d per interior cell.
+__device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, int lane) {
+  const int nx = P.nx, ny = P.ny;
+  const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
+  const float* T0 = reinterpret_cast<const float*>(V.S);
+  const float4* PA = P.p4a;
+  auto T = [&](size_t k) { return V.tau[k] * T0[4 * k]; };
+  for (int j = 0; j < ny; ++j) {
+    for (int i = lane; i < nx; i += 32) {
+      const size_t k = i + (size_t)nx * j;
+      if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1) {
+        V.W[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        V.id[k] = 0.f;
+        continue;
+      }
+      const size_t w = k - 1, e = k + 1, s = k - nx, n = k + nx;
+      const float4 pk = PA[k], pw = PA[w], pe = PA[e], ps = PA[s], pn = PA[n];
+      const float Tk = T(k), Tw = T(w), Te = T(e), Ts = T(s), Tn = T(n);
+      const float Twn = T(w + nx), Tws = T(w - nx), Ten = T(e + nx), Tes = T(e - nx);
+      const float Tse = T(s + 1), Tsw = T(s - 1), Tne = T(n + 1), Tnw = T(n - 1);
+      const float a1 = -((Tk - Tw) * idx * (pk.x + pw.x) * 0.5f) +
+                       (Tn - Ts + Twn - Tws) * (0.25f * idy) * (pk.z + pw.z) * 0.5f;
+      const float a2 = -((Te - Tk) * idx * (pe.x + pk.x) * 0.5f) +
+                       (Ten - Tes + Tn - Ts) * (0.25f * idy) * (pe.z + pk.z) * 0.5f;
+      const float b1 = -((Tk - Ts) * idy * (pk.y + ps.y) * 0.5f) +
+                       (Te - Tw + Tse - Tsw) * (0.25f * idx) * (pk.z + ps.z) * 0.5f;
+      const float b2 = -((Tn - Tk) * idy * (pn.y + pk.y) * 0.5f) +
+                       (Tne - Tnw + Te - Tw) * (0.25f * idx) * (pn.z + pk.z) * 0.5f;
+      const float a1m = fminf(a1, 0.f), a1p = fmaxf(a1, 0.f);
+      const float a2m = fminf(a2, 0.f), a2p = fmaxf(a2, 0.f);
+      const float b1m = fminf(b1, 0.f), b1p = fmaxf(b1, 0.f);
+      const float b2m = fminf(b2, 0.f), b2p = fmaxf(b2, 0.f);
+      const float d = (a2p - a1m) * idx + (b2p - b1m) * idy;
+      float id = 0.f;
+      float4 W = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!(fabsf(d) < (float)EPS14)) {
+        id = __frcp_rn(d);
+        W = make_float4(a1p * idx * id, -(a2m * idx) * id, b1p * idy * id, -(b2m * idy) * id);
+      }
+      V.W[k] = W;
+      V.id[k] = id;
+    }
+  }
+  __syncwarp();
+}
+
+struct WAdj {
+  bool on;
+  float own, old, src;
+  float4 w;  // ww, we, ws, wn
+};
+
+__device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, int nx, int xdir,
+                                        int ydir, const WSlot& V, const float* src, bool last) {
+  const int u = t - v;
+  o.on = v < nv && u >= 0 && u < nu;
+  if (!o.on) {
+    o.own = 0.f;
+    return;
+  }
+  const int i = xdir > 0 ? 1 + u : nu - u;  // interior [1, nx-2]
+  const int j = ydir > 0 ? 1 + v : nv - v;
+  const int k = i + nx * j;
+  o.own = V.tau[k];
+  o.w = V.W[k];
+  o.src = src[k];
+  if (last) o.old = V.old[k];
+}
+
+// Sweeps one adjoint field (held in V.tau) to convergence: the reference's
+// absolute rule (:1429) or no change beyond the FP32 resolution of the field.
+// Neighbours outside the interior are the boundary's zeros.
+template <int MB>
+__device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src, int lane,
+                                    int* status_out, int* iters_out) {
+  const int nx = P.nx, ny = P.ny;
+  const int nu = nx - 2, nv = ny - 2;
+  const int nsteps = nu + nv - 1;
+  for (int j = 0; j < ny; ++j)
+    for (int i = lane; i < nx; i += 32) {
+      const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
+      V.tau[i + (size_t)nx * j] = in ? 100.f : 0.f;
+    }
+  __syncwarp();
+  int iter, status = ST_NOT_CONVERGED;
+  for (iter = 1; iter <= MAXITER_JSE; ++iter) {
+    float l1 = 0.f, lmax = 0.f, vmax = 0.f;
+    for (int s = 0; s < 4; ++s) {
+      int xdir, ydir;
+      sweep_dirs(s, xdir, ydir);
+      const bool last = s == 3;
+      float res[MB];
+      WAdj cur[MB];
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        res[m] = 0.f;
+        wa_load(cur[m], 0, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+      }
+      for (int t = 0; t < nsteps; ++t) {
+        WAdj nxt[MB];
+#pragma unroll
+        for (int m = 0; m < MB; ++m)
+          wa_load(nxt[m], t + 1, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+        float south[MB], north[MB], nown[MB];
+#pragma unroll
+        for (int m = 0; m < MB; ++m) nown[m] = nxt[m].own;
+        w_from_below<MB>(res, south, lane);
+        w_from_above<MB>(nown, north, lane);
+#pragma unroll
+        for (int m = 0; m < MB; ++m) {
+          if (cur[m].on) {
+            const int v = lane + 32 * m, u = t - v;
+            const int k = (xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 1 + v : nv - v);
+            const float west = u > 0 ? res[m] : 0.f;
+            const float east = u < nu - 1 ? nown[m] : 0.f;
+            const float sth = v > 0 ? south[m] : 0.f;
+            const float nth = v < nv - 1 ? north[m] : 0.f;
+            const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
+            const float ts = ydir > 0 ? sth : nth, tn = ydir > 0 ? nth : sth;
+            const float4 W = cur[m].w;
+            const float val = cur[m].src + W.x * tw + W.y * te + W.z * ts + W.w * tn;
+            V.tau[k] = val;
+            if (s == 0) V.old[k] = cur[m].own;
+            if (last) {
+              const float dd = fabsf(val - cur[m].old);
+              l1 += dd;
+              lmax = fmaxf(lmax, dd);
+              vmax = fmaxf(vmax, fabsf(val));
+            }
+            res[m] = val;
+          }
+          cur[m] = nxt[m];
+        }
+        __syncwarp();
+      }
+    }
+    double sl1 = (double)l1, smax = (double)lmax, svmax = (double)vmax;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sl1 += __shfl_xor_sync(FULL, sl1, o);
+      smax = fmax(smax, __shfl_xor_sync(FULL, smax, o));
+      svmax = fmax(svmax, __shfl_xor_sync(FULL, svmax, o));
+    }
+    sl1 = sl1 / (double)(nx * ny);
+    if ((fabs(sl1) < TOL_JSE && smax < TOL_JSE) || smax <= svmax * 0x1p-21) {
+      status = ST_OK;
+      break;
+    }
+  }
+  *status_out = status;
+  *iters_out = iter > MAXITER_JSE ? MAXITER_JSE : iter;
+}
+
+// T = tau*T0 at a node (FP64 product of the FP32 factors)
+__device__ __forceinline__ double w_T(const WSlot& V, size_t k) {
+  return (double)V.tau[k] * (double)reinterpret_cast<const float*>(V.S)[4 * k];
+}
+
+// interp2_0_dp on the caller's increasing degree grid (src/shared/utils.f90:917-942)
+__device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, double yq,
+                                double* out) {
+  const int nx = P.nx, ny = P.ny;
+  int lo = -1, hi = nx;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xq >= P.xdeg[mid]) lo = mid; else hi = mid;
+  }
+  if (lo < 0 || lo >= nx - 1) return false;
+  int ylo = -1, yhi = ny;
+  while (yhi - ylo > 1) {
+    const int mid = (ylo + yhi) >> 1;
+    if (yq >= P.ydeg[mid]) ylo = mid; else yhi = mid;
+  }
+  if (ylo < 0 || ylo >= ny - 1) return false;
+  const double* x = P.xdeg;
+  const double* y = P.ydeg;
+  const int x1 = lo, x2 = lo + 1, y1 = ylo, y2 = ylo + 1;
+  const double vn = fabs((x[x2] - x[x1]) * (y[y2] - y[y1]));
+  const double n1 = fabs((x[x2] - xq) * (y[y2] - yq));
+  const double n2 = fabs((x[x1] - xq) * (y[y2] - yq));
+  const double n3 = fabs((x[x2] - xq) * (y[y1] - yq));
+  const double n4 = fabs((x[x1] - xq) * (y[y1] - yq));
+  double r = 0;
+  r = r + w_T(V, x1 + (size_t)nx * y1) * (n1 / vn);
+  r = r + w_T(V, x2 + (size_t)nx * y1) * (n2 / vn);
+  r = r + w_T(V, x1 + (size_t)nx * y2) * (n3 / vn);
+  r = r + w_T(V, x2 + (size_t)nx * y2) * (n4 / vn);
+  *out = r;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// the kernel
+// ---------------------------------------------------------------------------
+template <int MB>
+__global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  double* base = A.ws + gw * A.ws_doubles;
+  float* kf = reinterpret_cast<float*>(A.kcontrib);
+  float* kdf = reinterpret_cast<float*>(A.kcontrib_den);
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(A.queue, 1);
+    q = __shfl_sync(FULL, q, 0);
+    if (q >= A.nsolve) break;
+    const int s = A.order[q];
+    const PeriodDev P = A.periods[A.pidx[s]];
+    const int nx = P.nx, ny = P.ny;
+    const size_t N = (size_t)nx * ny;
+    const int r0 = A.rec_off[s], nr = A.nrec[s];
+    const WSlot V = wcarve(base, N);
+    const double xd0 = A.srcx[s], yd0 = A.srcy[s];
+    const double x0 = xd0 / 180.0 * PI_S, y0 = yd0 / 180.0 * PI_S;
+    const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
+    if (w.status != ST_OK) {
+      for (int r = lane; r < nr; r += 32) {
+        A.tekio[r0 + r] = 0.0;
+        A.wgt_eff[r0 + r] = 0.0;
+        A.tt_fwd[A.path[r0 + r]] = 0.0;
+      }
+      if (A.mode >= 2)
+        for (size_t k = lane; k < N; k += 32) {
+          kf[A.kslot[s] + k] = 0.f;
+          if (A.mode == 3) kdf[A.kslot[s] + k] = 0.f;
+        }
+      if (lane == 0) {
+        A.chi[s] = 0.0;
+        A.status[s] = w.status;
+        A.fwd_iters[s] = 0;
+        A.adj_iters[s] = 0;
+        if (A.fwd_updates) A.fwd_updates[s] = 0;
+      }
+      __syncwarp();
+      continue;
+    }
+    w_t0(P, x0, y0, w, V, lane);
+    int fst = ST_OK, fit = 0;
+    w_fwd_sweeps<MB>(P, V, w, lane, &fst, &fit);
+    if (A.fwd_updates && lane == 0) {
+      const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
+      A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
+    }
+    // receiver times, misfit, outlier weights (src/measadj.f90:71-72, 82-84)
+    int bad = 0;
+    for (int r = lane; r < nr; r += 32) {
+      double v = 0.0;
+      if (!w_interp(P, V, A.recx[r0 + r], A.recy[r0 + r], &v)) bad = 1;
+      A.tekio[r0 + r] = v;
+      A.tt_fwd[A.path[r0 + r]] = v;
+    }
+    bad = __any_sync(FULL, bad);
+    __syncwarp();
+    if (lane == 0) {
+      double ssum = 0;
+      for (int r = 0; r < nr; ++r) {
+        const double d = A.tekio[r0 + r] - A.tt[r0 + r];
+        ssum = ssum + A.weight[r0 + r] * (d * d);
+      }
+      A.chi[s] = 0.5 * ssum;
+      for (int r = 0; r < nr; ++r) {
+        double wt = A.weight[r0 + r];
+        if (fabs(A.tekio[r0 + r] - A.tt[r0 + r]) / A.tt[r0 + r] > 0.5) wt = 0.;
+        A.wgt_eff[r0 + r] = wt;
+      }
+    }
+    __syncwarp();
+    int st = fst;
+    if (bad && st == ST_OK) st = ST_BAD_ARG;
+    int aiters = 0;
+    if (A.mode >= 2) {
+      const int nf = A.mode == 3 ? 2 : 1;
+      w_adj_setup(P, V, lane);
+      for (int f = 0; f < nf; ++f)
+        for (size_t k = lane; k < N; k += 32) V.src[f][k] = 0.f;
+      __syncwarp();
+      if (lane == 0) {
+        // adjoint sources weight*(tekio-tt) (src/measadj.f90:88) and -weight
+        // (:102), bilinear splat over the cell area (:1328-1336), scaled by 1/d
+        for (int f = 0; f < nf && st != ST_BAD_ARG; ++f)
+          for (int r = 0; r < nr; ++r) {
+            const double wt = A.wgt_eff[r0 + r];
+            const double sv = f == 0 ? wt * (A.tekio[r0 + r] - A.tt[r0 + r]) : -1.0 * wt;
+            const double xr = A.recx[r0 + r] / 180.0 * PI_S, yr = A.recy[r0 + r] / 180.0 * PI_S;
+            float r1 = 0.f, r2 = 0.f;
+            const int i0 = locate_cell(P.xs, nx, P.dx, xr, &r1);
+            const int j0 = locate_cell(P.ys, ny, P.dy, yr, &r2);
+            if (i0 < 0 || j0 < 0) { st = ST_BAD_ARG; break; }
+            const double den = P.dx * R_EARTH * cos(yr) * P.dy * R_EARTH;
+            const size_t k = i0 + (size_t)nx * j0;
+            float* sf = V.src[f];
+            sf[k] += (float)(sv * (double)(1 - r1) * (double)(1 - r2) / den) * V.id[k];
+            if (j0 + 1 < ny) sf[k + nx] += (float)(sv * (double)(1 - r1) * (double)r2 / den) * V.id[k + nx];
+            if (i0 + 1 < nx) sf[k + 1] += (float)(sv * (double)r1 * (double)(1 - r2) / den) * V.id[k + 1];
+            if (i0 + 1 < nx && j0 + 1 < ny)
+              sf[k + nx + 1] += (float)(sv * (double)r1 * (double)r2 / den) * V.id[k + nx + 1];
+          }
+      }
+      st = __shfl_sync(FULL, st, 0);
+      __syncwarp();
+      int its[2] = {0, 0};
+      for (int f = 0; f < nf; ++f) {
+        int ast = ST_OK;
+        w_adj_sweeps<MB>(P, V, V.src[f], lane, &ast, &its[f]);
+        if (ast != ST_OK && st == ST_OK) st = ast;
+        // mask (:1449-1467) and the slot adj/svel**k (:314-315), FP32 here,
+        // summed per period in FP64
+        float* out = (f == 0 ? kf : kdf) + A.kslot[s];
+        for (int j = 0; j < ny; ++j)
+          for (int i = lane; i < nx; i += 32) {
+            const size_t k = i + (size_t)nx * j;
+            const float4 pb = P.p4b[k];
+            const float isv = A.mode == 3 ? pb.w : pb.z;
+            out[k] = w.mbox.has(i, j) ? 0.f : V.tau[k] * isv;
+          }
+        __syncwarp();
+      }
+      aiters = its[0] > its[1] ? its[0] : its[1];
+      if (A.adj_updates && lane == 0)
+        A.adj_updates[s] = (double)(its[0] + its[1]) * 4.0 * (nx - 2) * (ny - 2);
+    }
+    if (lane == 0) {
+      A.status[s] = st;
+      A.fwd_iters[s] = fit;
+      A.adj_iters[s] = aiters;
+    }
+    __syncwarp();
+  }
+}
+
+int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
+
+void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st) {
+  switch (bands) {
+    case 1: k_batch_fp32w<1><<<grid, 128, 0, st>>>(a); break;
+    case 2: k_batch_fp32w<2><<<grid, 128, 0, st>>>(a); break;
+    case 3: k_batch_fp32w<3><<<grid, 128, 0, st>>>(a); break;
+    default: k_batch_fp32w<4><<<grid, 128, 0, st>>>(a); break;
+  }
+}
+
+int batch_fp32w_max_blocks_per_sm(int bands) {
+  int n = 0;
+  switch (bands) {
+    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<1>, 128, 0); break;
+    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<2>, 128, 0); break;
+    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<3>, 128, 0); break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<4>, 128, 0); break;
+  }
+  return n;
+}
+
+}  // namespace sgb

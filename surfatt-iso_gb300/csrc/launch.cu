@@ -1,0 +1,113 @@
+// launch.cu -- launch configuration and kernel sequence of one gradient
+// evaluation (shared by the engine and the serving loop).
+#include <algorithm>
+
+#include "launch.cuh"
+
+namespace sgb {
+
+void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goffs, int np, int ns,
+                           int npth) {
+  nperiod = np;
+  nsolve = ns;
+  npath = npth;
+  ncell = max_cells = max_pitched = 0;
+  max_nx = max_ny = max_diag = 0;
+  for (int p = 0; p < np; ++p) {
+    const long long N = (long long)nxs[p] * nys[p];
+    ncell = std::max(ncell, goffs[p] + N);
+    max_cells = std::max(max_cells, N);
+    max_nx = std::max(max_nx, nxs[p]);
+    max_ny = std::max(max_ny, nys[p]);
+    max_diag = std::max(max_diag, std::min(nxs[p], nys[p]));
+    max_pitched = std::max(max_pitched, (long long)batch_fp32_pitch(nxs[p]) * nys[p]);
+  }
+}
+
+int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan) {
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return ST_CUDA_ERROR;
+  LaunchPlan p;
+  if (prec == 0) {
+    p.kind = KK_FP64;
+    p.block = 128;
+    p.per_sm = batch_fp64_max_blocks_per_sm(p.block);
+    p.ws_doubles = batch_fp64_ws_doubles(sh.max_cells);
+  } else if (sh.max_ny <= 128 && sh.max_nx <= 4096) {
+    // one warp per solve, lanes own the rows
+    p.kind = KK_FP32_WARP;
+    p.block = 128;
+    p.slots_per_block = 4;
+    p.bands = fp32w_bands(sh.max_ny);
+    p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands);
+    p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
+  } else {
+    // one block per solve, one thread per cell of the longest anti-diagonal
+    if (sh.max_diag > kFp32MaxThreads) return ST_BAD_ARG;
+    p.kind = KK_FP32_BLOCK;
+    p.block = std::max(32, (sh.max_diag + 31) / 32 * 32);
+    p.smem = batch_fp32_smem_bytes(sh.max_pitched, sh.max_nx, &p.smem_tau);
+    p.per_sm = batch_fp32_max_blocks_per_sm(p.block, p.smem, p.smem_tau);
+    p.ws_doubles = batch_fp32_ws_doubles(sh.max_cells);
+  }
+  if (p.per_sm < 1) p.per_sm = 1;
+  p.grid = nsm * p.per_sm;
+  if (max_grid > 0) p.grid = std::min(p.grid, max_grid);
+  const int need = (std::max(1, sh.nsolve) + p.slots_per_block - 1) / p.slots_per_block;
+  p.grid = std::max(1, std::min(p.grid, need));
+  *plan = p;
+  return ST_OK;
+}
+
+int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan& plan, int mode,
+                       int prec, double* ws, int* queue, cudaStream_t st, cudaEvent_t ev_k0,
+                       cudaEvent_t ev_k1) {
+  BatchArgs A = dev.args;
+  A.mode = mode;
+  A.ws = ws;
+  A.ws_doubles = plan.ws_doubles;
+  A.queue = queue;
+  A.block = plan.block;
+  A.max_nx = sh.max_nx;
+  A.smem_tau = plan.smem_tau;
+  A.smem_bytes = plan.smem;
+  int launches = 0;
+  if (cudaMemsetAsync(queue, 0, sizeof(int), st) != cudaSuccess) return -ST_CUDA_ERROR;
+  if (sh.npath > 0 &&
+      cudaMemsetAsync(A.tt_fwd, 0, (size_t)sh.npath * sizeof(double), st) != cudaSuccess)
+    return -ST_CUDA_ERROR;
+  if (A.adj_updates && sh.nsolve > 0 &&
+      cudaMemsetAsync(A.adj_updates, 0, (size_t)sh.nsolve * sizeof(double), st) != cudaSuccess)
+    return -ST_CUDA_ERROR;
+  if (ev_k0) cudaEventRecord(ev_k0, st);
+  (void)prec;
+  if (sh.nsolve > 0) {
+    if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
+    else if (plan.kind == KK_FP32_BLOCK) launch_batch_fp32(A, plan.grid, plan.block, st);
+    else launch_batch_fp32w(A, plan.grid, plan.bands, st);
+    ++launches;
+  }
+  if (ev_k1) cudaEventRecord(ev_k1, st);
+  if (mode >= 2) {
+    const int nf = mode == 3 ? 2 : 1;
+    for (int f = 0; f < nf; ++f) {
+      double* kc = f == 0 ? A.kcontrib : A.kcontrib_den;
+      double* out = f == 0 ? dev.adj_s : dev.adj_density;
+      if (plan.kind == KK_FP32_WARP)
+        launch_kernel_reduce_f32(sh.nperiod, dev.plist_off, dev.plist, A.kslot,
+                                 reinterpret_cast<const float*>(kc), out, dev.goff, dev.nx,
+                                 dev.ny, st);
+      else
+        launch_kernel_reduce(nullptr, sh.nperiod, dev.plist_off, dev.plist, A.kslot, kc, out,
+                             sh.ncell, dev.goff, dev.nx, dev.ny, st);
+      ++launches;
+    }
+  }
+  launch_chi_reduce(A.chi, sh.nsolve, dev.chi_total, st);
+  ++launches;
+  if (cudaGetLastError() != cudaSuccess) return -ST_CUDA_ERROR;
+  return launches;
+}
+
+}  // namespace sgb

@@ -1,0 +1,62 @@
+// launch.cuh -- one gradient evaluation on device-resident buffers: launch
+// configuration (block size, shared memory, resident blocks) and the kernel
+// sequence (batched solve kernel, ordered per-period kernel sums, misfit
+// sum).  Used by the engine and by the serving loop.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace sgb {
+
+// Host-side shape of an evaluation (what the launch configuration needs).
+struct EvalShape {
+  int nperiod = 0, nsolve = 0, npath = 0;
+  long long ncell = 0, max_cells = 0, max_pitched = 0;
+  int max_nx = 0, max_ny = 0, max_diag = 0;
+  void from_grids(const int* nx, const int* ny, const long long* goff, int np, int ns, int npth);
+};
+
+// Device pointers of an evaluation (inputs, outputs, per-period reduction
+// lists).  `args` is the solve kernel's argument block without workspace.
+struct EvalDev {
+  BatchArgs args;
+  const int* plist_off;   // per-period solve lists (work-list order)
+  const int* plist;
+  const long long* goff;
+  const int* nx;
+  const int* ny;
+  double* chi_total;      // 1 double
+  double* adj_s;          // ncell
+  double* adj_density;    // ncell
+};
+
+// Solve kernels: plain FP64 (one block per solve), FP32 one block per solve
+// (any grid), FP32 one warp per solve (grids of at most 128 rows).
+enum KernelKind { KK_FP64 = 0, KK_FP32_BLOCK = 1, KK_FP32_WARP = 2 };
+
+struct LaunchPlan {
+  int kind = KK_FP64;
+  int grid = 0, block = 0, per_sm = 0, smem_tau = 0, bands = 0;
+  int slots_per_block = 1;   // solves resident per block (warps for KK_FP32_WARP)
+  size_t smem = 0;
+  long long ws_doubles = 0;  // per resident solve
+};
+
+// Launch configuration for `prec` (0 FP64, 1 FP32) on `device`; grid capped
+// at `max_grid` (0 = resident capacity of the device).  Returns ST_BAD_ARG
+// when a grid's diagonal exceeds the FP32 kernel's block limit.
+int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan);
+
+// Enqueue the evaluation on `st`: queue reset, tt_fwd reset, solve kernel,
+// per-period reductions (modes 2, 3) and the misfit sum.  `ws` must hold
+// plan.grid * plan.ws_doubles doubles; `queue` one int.  Records
+// ev_k0/ev_k1 around the solve kernel when given.  Returns the number of
+// kernel launches, or a negative status.
+int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan& plan, int mode,
+                       int prec, double* ws, int* queue, cudaStream_t st, cudaEvent_t ev_k0,
+                       cudaEvent_t ev_k1);
+
+}  // namespace sgb

@@ -108,6 +108,10 @@ __global__ void __launch_bounds__(256) k_uw_noalloc(const double* xdeg, const do
   P.disy = disy;
   P.svel = nullptr;
   P.goff = 0;
+  P.f32 = nullptr;
+  P.isv = nullptr;
+  P.p4a = nullptr;
+  P.p4b = nullptr;
   fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, W, true, sh);
   if (sh.status != ST_OK) {
     if (threadIdx.x == 0) { si[0] = sh.status; si[1] = 0; }

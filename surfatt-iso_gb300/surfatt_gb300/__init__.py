@@ -41,6 +41,7 @@ EXPORTED = [
     "surfatt_engine_create", "surfatt_engine_destroy", "surfatt_engine_load",
     "surfatt_engine_update_velocity", "surfatt_engine_run", "surfatt_engine_sync",
     "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
+    "surfatt_engine_launch_config",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
 ]
 
@@ -395,6 +396,18 @@ class Engine:
         if st != OK:
             raise SurfattError(st, "engine_timing")
         return t.value, k.value, n.value
+
+    def launch_config(self):
+        g, b, n = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        sm = ctypes.c_size_t(0)
+        L = lib()
+        L.surfatt_engine_launch_config.argtypes = [ctypes.c_void_p, _ip, _ip, _ip,
+                                                   ctypes.POINTER(ctypes.c_size_t)]
+        st = L.surfatt_engine_launch_config(self._h, ctypes.byref(g), ctypes.byref(b),
+                                            ctypes.byref(n), ctypes.byref(sm))
+        if st != OK:
+            raise SurfattError(st, "engine_launch_config")
+        return dict(grid=g.value, block=b.value, blocks_per_sm=n.value, smem_bytes=sm.value)
 
     def work(self):
         f, a = ctypes.c_double(0), ctypes.c_double(0)

@@ -210,6 +210,23 @@ def test_engine_fp32_flat(sg, oracle):
     _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
 
 
+def test_engine_fp32_four_bands(sg, oracle):
+    """FP32 warp-per-solve kernel with four 32-row bands per lane (ny = 120)."""
+    pb = W.flat_case(nx=130, ny=120, nsta=5, nperiod=2, mode=3)
+    _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
+
+
+def test_engine_fp32_mode2_odd_grid(sg, oracle):
+    pb = W.flat_case(nx=71, ny=45, nsta=6, nperiod=1, mode=2)
+    _engine_vs_oracle(sg, oracle, pb, 2, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
+
+
+def test_engine_fp32_block_kernel_tall_grids(sg, oracle):
+    """Grids taller than 128 rows use the one-block-per-solve FP32 kernel."""
+    pb = W.config4(nsrc=4, nperiod=3, nmax=168, nmin=48, span_deg=2.0)
+    _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
+
+
 def test_engine_uneven_grids(sg, oracle):
     pb = W.config4(nsrc=5, nperiod=3, nmax=72, nmin=40, span_deg=2.0)
     _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
