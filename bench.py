@@ -244,11 +244,12 @@ def run_ours(args):
     r64 = eng.results()
     fwd64, adj64 = eng.work()
     launch64 = eng.launch_config()
+    tuned = eng.autotune(pb.mode, sg.PREC_FP32)
     eng.run(pb.mode, sg.PREC_FP32)
     eng.sync()
     r32 = eng.results()
     fwd32, adj32 = eng.work()
-    launch32 = eng.launch_config()
+    launch32 = dict(eng.launch_config(), **eng.kernel_variant())
     err32 = _errors(r32, r64, pb)
 
     # plain FP64 (reported beside the headline)
@@ -357,7 +358,7 @@ def run_ours(args):
                          "kernel": "k_batch_fp32", "kernel_ms": k32_ms,
                          "flops_per_launch": flops32},
             "cpu_baseline": cpu, "parity": parity,
-            "launch": {"fp32": launch32, "fp64": launch64},
+            "launch": {"fp32": launch32, "fp64": launch64, "autotune": tuned},
             "iterations": {"fwd_mean": float(np.mean(r32["fwd_iters"])),
                            "adj_mean": float(np.mean(r32["adj_iters"]))},
             "wall_s_timed_region": wall,

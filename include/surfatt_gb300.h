@@ -240,6 +240,19 @@ surfatt_status_t surfatt_engine_timing(surfatt_engine_t* engine, double* total_m
 surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* engine, int* grid, int* block,
                                               int* blocks_per_sm, size_t* smem_bytes);
 
+/* Time every solve-kernel variant that applies to the loaded problem (plain
+ * FP64: one; FP32: one warp per solve with or without operand prefetch, one
+ * block per solve) with one warm-up and one timed evaluation each, and use
+ * the fastest for later runs of this precision until the next load.  Returns
+ * the chosen variant (0 FP64, 1 FP32 block, 2 FP32 warp), its prefetch flag
+ * and its solve-kernel time. */
+surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* engine, surfatt_mode_t mode,
+                                         surfatt_precision_t precision, int* kind, int* prefetch,
+                                         double* best_ms);
+/* Variant and prefetch flag used by the last run. */
+surfatt_status_t surfatt_engine_kernel_variant(surfatt_engine_t* engine, int* kind,
+                                               int* prefetch);
+
 /* Total sweep cell visits of the last run (forward, adjoint), for the
  * algorithmic roofline. */
 surfatt_status_t surfatt_engine_work(surfatt_engine_t* engine, double* fwd_cell_updates,
@@ -269,6 +282,50 @@ surfatt_status_t surfatt_uw_lonlat_solve_noalloc(const double* xx_deg, const dou
                                                  const double* sphb, const double* sphc,
                                                  const double* fun, double x0_deg, double y0_deg,
                                                  double* T, int* status_iters, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * 4. Serving loop (no counterpart in the reference, whose drivers call the
+ *    path synchronously): requests -- gradient evaluations, line-search
+ *    trial models, forward-only runs -- admitted by an HBM budget and run
+ *    concurrently, with models and station tables resident on the device.
+ * ------------------------------------------------------------------------- */
+typedef struct surfatt_server surfatt_server_t;
+
+typedef struct {
+  long long submitted, completed, failed, solves;
+  double p50_ms, p99_ms, mean_ms; /* submit -> result ready, per request */
+  double span_s;                  /* first submit -> last completion */
+  double solves_per_s;            /* solves completed / span */
+  size_t hbm_budget_bytes, hbm_peak_bytes;
+  int inflight_peak;
+} surfatt_server_stats_t;
+
+/* A server on `device` owning one device allocation of hbm_budget_bytes
+ * (every model, work list and in-flight request lives in it) and running at
+ * most max_inflight requests at a time. */
+surfatt_status_t surfatt_server_create(surfatt_server_t** server, int device,
+                                       size_t hbm_budget_bytes, int max_inflight);
+/* Waits for running requests, drops queued ones, frees everything. */
+void surfatt_server_destroy(surfatt_server_t* server);
+/* Make the periods of `pb` (grids, metric m11/m12/m22, velocity) resident. */
+surfatt_status_t surfatt_server_add_model(surfatt_server_t* server, const surfatt_problem_t* pb,
+                                          int* model_id);
+/* Make the work list of `pb` (solves, receivers, observed times, weights,
+ * path indices) resident, for the periods of model `model_id`. */
+surfatt_status_t surfatt_server_add_worklist(surfatt_server_t* server, int model_id,
+                                             const surfatt_problem_t* pb, int* worklist_id);
+/* Queue an evaluation of a work list; `svel` (may be NULL: the model's
+ * velocity) is a velocity model laid out like pb->svel, copied at submit. */
+surfatt_status_t surfatt_server_submit(surfatt_server_t* server, int worklist_id,
+                                       const double* svel, surfatt_mode_t mode,
+                                       surfatt_precision_t precision, long long* ticket);
+/* Wait (timeout_s <= 0: no limit) for a request, copy its results into
+ * `out` (host buffers; NULL members are skipped) and release it. */
+surfatt_status_t surfatt_server_wait(surfatt_server_t* server, long long ticket,
+                                     double timeout_s, surfatt_result_t* out,
+                                     double* latency_ms);
+surfatt_status_t surfatt_server_stats(surfatt_server_t* server, surfatt_server_stats_t* stats);
+surfatt_status_t surfatt_server_reset_stats(surfatt_server_t* server);
 
 /* Library version string. */
 const char* surfatt_version(void);

@@ -477,8 +477,9 @@ struct surfatt_engine {
       d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
   DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
       d_fupd, d_aupd, d_ws, d_queue;
-  int grid = 0, block = 128, per_sm = 0, last_block = 0;
+  int grid = 0, block = 128, per_sm = 0, last_block = 0, last_kind = 0, last_pf = 0;
   size_t last_smem = 0;
+  int tuned_kind[2] = {-1, -1}, tuned_pf[2] = {-1, -1};  // per precision, -1: automatic
   std::vector<DBuf*> all() {
     return {&d_periods, &d_xdeg, &d_ydeg, &d_xs, &d_ys, &d_cosy, &d_siny, &d_A, &d_B, &d_C,
             &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_f32, &d_isv, &d_p4a, &d_p4b, &d_pidx, &d_srcx, &d_srcy,
@@ -569,6 +570,8 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   CK(cudaSetDevice(e->device));
   e->loaded = false;
   e->ran = false;
+  e->tuned_kind[0] = e->tuned_kind[1] = -1;
+  e->tuned_pf[0] = e->tuned_pf[1] = -1;
   const int np = pb->nperiod, ns = pb->nsolve;
   e->nperiod = np;
   e->nsolve = ns;
@@ -703,17 +706,15 @@ surfatt_status_t surfatt_engine_update_velocity(surfatt_engine_t* e, const doubl
   return (surfatt_status_t)run_prep_all(e);
 }
 
-surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
-                                    surfatt_precision_t prec) {
-  if (!e || !e->loaded) return SURFATT_BAD_ARG;
-  if (mode != SURFATT_MODE_FORWARD && mode != SURFATT_MODE_2D && mode != SURFATT_MODE_3D)
-    return SURFATT_BAD_ARG;
-  if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
+}  // extern "C"
+
+namespace {
+int engine_enqueue(surfatt_engine* e, int mode, int prec, int force_kind, int force_pf) {
   CK(cudaSetDevice(e->device));
   EvalShape sh;
   sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
   LaunchPlan plan;
-  int r = plan_evaluation(sh, prec == SURFATT_PREC_FP64 ? 0 : 1, e->device, 0, &plan);
+  int r = plan_evaluation(sh, prec, e->device, 0, &plan, force_kind, force_pf);
   if (r) return (surfatt_status_t)r;
   r = eng_ensure(e, e->d_ws,
                  (size_t)plan.grid * plan.slots_per_block * plan.ws_doubles * sizeof(double));
@@ -722,6 +723,8 @@ surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
   e->per_sm = plan.per_sm;
   e->last_block = plan.block;
   e->last_smem = plan.smem;
+  e->last_kind = plan.kind;
+  e->last_pf = plan.pf;
   EvalDev dev;
   BatchArgs& A = dev.args;
   A.periods = e->d_periods.as<PeriodDev>();
@@ -759,14 +762,58 @@ surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
   dev.adj_s = e->d_adj.as<double>();
   dev.adj_density = e->d_adjd.as<double>();
   CK(cudaEventRecord(e->ev0, e->st));
-  const int n = enqueue_evaluation(sh, dev, plan, mode, prec == SURFATT_PREC_FP64 ? 0 : 1,
-                                   e->d_ws.as<double>(), e->d_queue.as<int>(), e->st, e->evk0,
-                                   e->evk1);
-  if (n < 0) return (surfatt_status_t)(-n);
+  const int n = enqueue_evaluation(sh, dev, plan, mode, prec, e->d_ws.as<double>(),
+                                   e->d_queue.as<int>(), e->st, e->evk0, e->evk1);
+  if (n < 0) return -n;
   CK(cudaEventRecord(e->ev1, e->st));
   e->launches = n;
   e->ran = true;
   e->last_mode = mode;
+  return SURFATT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
+                                    surfatt_precision_t prec) {
+  if (!e || !e->loaded) return SURFATT_BAD_ARG;
+  if (mode != SURFATT_MODE_FORWARD && mode != SURFATT_MODE_2D && mode != SURFATT_MODE_3D)
+    return SURFATT_BAD_ARG;
+  if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
+  const int p = prec == SURFATT_PREC_FP64 ? 0 : 1;
+  return (surfatt_status_t)engine_enqueue(e, mode, p, e->tuned_kind[p], e->tuned_pf[p]);
+}
+
+surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* e, surfatt_mode_t mode,
+                                         surfatt_precision_t prec, int* kind, int* pf,
+                                         double* best_ms) {
+  if (!e || !e->loaded) return SURFATT_BAD_ARG;
+  if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
+  const int p = prec == SURFATT_PREC_FP64 ? 0 : 1;
+  EvalShape sh;
+  sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
+  double best = 1e300;
+  int bk = -1, bp = -1;
+  for (const auto& c : plan_candidates(sh, p)) {
+    float ms = 0.f;
+    int r = engine_enqueue(e, mode, p, c.first, c.second);  // warm-up / first touch
+    if (r) return (surfatt_status_t)r;
+    r = engine_enqueue(e, mode, p, c.first, c.second);
+    if (r) return (surfatt_status_t)r;
+    CK(cudaEventSynchronize(e->ev1));
+    CK(cudaEventElapsedTime(&ms, e->evk0, e->evk1));
+    if (ms < best) {
+      best = ms;
+      bk = c.first;
+      bp = c.second;
+    }
+  }
+  e->tuned_kind[p] = bk;
+  e->tuned_pf[p] = bp;
+  if (kind) *kind = bk;
+  if (pf) *pf = bp;
+  if (best_ms) *best_ms = best;
   return SURFATT_OK;
 }
 
@@ -833,6 +880,13 @@ surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* e, int* grid, in
   if (block) *block = e->last_block;
   if (blocks_per_sm) *blocks_per_sm = e->per_sm;
   if (smem_bytes) *smem_bytes = e->last_smem;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_kernel_variant(surfatt_engine_t* e, int* kind, int* pf) {
+  if (!e || !e->ran) return SURFATT_BAD_ARG;
+  if (kind) *kind = e->last_kind;
+  if (pf) *pf = e->last_pf;
   return SURFATT_OK;
 }
 

@@ -76,6 +76,14 @@ __host__ __device__ inline int locate_cell(const double* xx, int limit, double d
   return i;
 }
 
+// Approximate reciprocal and square root of the FP32 sweeps (hardware MUFU,
+// about 2 ulp, no special-case branches): the update adds their products to
+// tau_X as a small increment, so this error stays far below FP32 resolution
+// of tau.  sqrt of a non-positive argument returns 0 (its root is rejected by
+// the caller's D >= 0 test).
+__device__ __forceinline__ float frcp_fast(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ float fsqrt_fast(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+
 // Block-wide reductions (blockDim.x a multiple of 32, <= 1024).
 __device__ inline double warp_sum(double v) {
 #pragma unroll

@@ -20,16 +20,18 @@ __global__ void k_prep(PrepIn in, PrepOut out) {
   const size_t N = (size_t)nx * ny;
   const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t nthr = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = tid; i < (size_t)nx; i += nthr)
-    out.xs[i] = in.lonlat ? in.xdeg[i] / 180.0 * PI_S : in.xdeg[i];
-  for (size_t j = tid; j < (size_t)ny; j += nthr) {
-    const double y = in.lonlat ? in.ydeg[j] / 180.0 * PI_S : in.ydeg[j];
-    out.ys[j] = y;
-    if (in.lonlat) {
-      out.cosy[j] = cos(y);
-      out.siny[j] = sin(y);
+  if (out.xs)  // axis outputs are optional (already prepared for this grid)
+    for (size_t i = tid; i < (size_t)nx; i += nthr)
+      out.xs[i] = in.lonlat ? in.xdeg[i] / 180.0 * PI_S : in.xdeg[i];
+  if (out.ys)
+    for (size_t j = tid; j < (size_t)ny; j += nthr) {
+      const double y = in.lonlat ? in.ydeg[j] / 180.0 * PI_S : in.ydeg[j];
+      out.ys[j] = y;
+      if (in.lonlat) {
+        out.cosy[j] = cos(y);
+        out.siny[j] = sin(y);
+      }
     }
-  }
   for (size_t k = tid; k < N; k += nthr) {
     const int j = (int)(k / nx);
     double A = in.A[k], B = in.B[k], C = in.C[k], f;

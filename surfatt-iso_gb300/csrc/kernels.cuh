@@ -96,8 +96,8 @@ void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plis
                               const long long* goff_dev, const int* nx_dev, const int* ny_dev,
                               cudaStream_t st);
 // Warp-per-solve FP32 kernel (grids of at most 32*bands rows).
-void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st);
-int batch_fp32w_max_blocks_per_sm(int bands);
+void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int pf, cudaStream_t st);
+int batch_fp32w_max_blocks_per_sm(int bands, int pf);
 long long batch_fp32w_ws_doubles(long long N);
 int fp32w_bands(int max_ny);
 // chi = sum of per-solve misfits in work-list order (src/acqui.f90:135)

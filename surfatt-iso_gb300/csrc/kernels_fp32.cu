@@ -229,8 +229,8 @@ __device__ __forceinline__ float two_sided_pair(float2 px, float2 tX, float2 U0,
   const float2 H = fma2(bx, U0, mul2(by, V0));
   const float2 D = fma2(H, H, mul2(neg2(A), C));
   const bool vx = okx && D.x >= 0.f, vy = oky && D.y >= 0.f;
-  const float2 sq = make_float2(sqrtf(fmaxf(D.x, 0.f)), sqrtf(fmaxf(D.y, 0.f)));
-  const float2 ia = make_float2(__frcp_rn(A.x), __frcp_rn(A.y));
+  const float2 sq = make_float2(fsqrt_fast(D.x), fsqrt_fast(D.y));
+  const float2 ia = make_float2(frcp_fast(A.x), frcp_fast(A.y));
   const float2 d1 = mul2(add2(sq, neg2(H)), ia);
   const float2 d2 = mul2(add2(neg2(sq), neg2(H)), ia);
   const float2 x1 = fma2(bx, d1, CU), y1 = fma2(by, d1, CV);
@@ -248,7 +248,7 @@ __device__ __forceinline__ float two_sided_pair(float2 px, float2 tX, float2 U0,
 // when tau*T0 >= tnb*T0nb and tau > tnb/2 (:1017-1028).
 __device__ __forceinline__ float one_sided_pair(float2 p, float2 tnb, float2 t0nb, float g,
                                                 float dis, float t0, bool okx, bool oky) {
-  const float2 ip = make_float2(__frcp_rn(p.x), __frcp_rn(p.y));
+  const float2 ip = make_float2(frcp_fast(p.x), frcp_fast(p.y));
   const float2 gt = mul2(bc2(g), tnb);
   const float2 r1 = fma2(add2(bc2(dis), neg2(gt)), ip, tnb);
   const float2 r2 = fma2(add2(bc2(-dis), neg2(gt)), ip, tnb);

@@ -220,8 +220,8 @@ __device__ __forceinline__ float w_two_sided(float2 px, float2 tX, float2 U0, fl
   const float2 H = wfma(bx, U0, wmul(by, V0));
   const float2 D = wfma(H, H, wmul(wneg(A), C));
   const bool vx = okx && D.x >= 0.f, vy = oky && D.y >= 0.f;
-  const float2 sq = make_float2(sqrtf(fmaxf(D.x, 0.f)), sqrtf(fmaxf(D.y, 0.f)));
-  const float2 ia = make_float2(__frcp_rn(A.x), __frcp_rn(A.y));
+  const float2 sq = make_float2(fsqrt_fast(D.x), fsqrt_fast(D.y));
+  const float2 ia = make_float2(frcp_fast(A.x), frcp_fast(A.y));
   const float2 d1 = wmul(wadd(sq, wneg(H)), ia);
   const float2 d2 = wmul(wadd(wneg(sq), wneg(H)), ia);
   const float2 x1 = wfma(bx, d1, CU), y1 = wfma(by, d1, CV);
@@ -237,7 +237,7 @@ __device__ __forceinline__ float w_two_sided(float2 px, float2 tX, float2 U0, fl
 
 __device__ __forceinline__ float w_one_sided(float2 p, float2 tnb, float2 t0nb, float g,
                                              float dis, float t0, bool okx, bool oky) {
-  const float2 ip = make_float2(__frcp_rn(p.x), __frcp_rn(p.y));
+  const float2 ip = make_float2(frcp_fast(p.x), frcp_fast(p.y));
   const float2 gt = wmul(wbc(g), tnb);
   const float2 r1 = wfma(wadd(wbc(dis), wneg(gt)), ip, tnb);
   const float2 r2 = wfma(wadd(wbc(-dis), wneg(gt)), ip, tnb);
@@ -264,6 +264,20 @@ struct WFwd {
   float dsx, dsy;
 };
 
+// The cell's constants (T0 gradient, metric, slowness, one-sided terms).
+__device__ __forceinline__ void wf_load_heavy(WFwd& o, int k, const PeriodDev& P, const WSlot& V) {
+  const float4 sv = V.S[k];
+  o.gx = sv.y;
+  o.gy = sv.z;
+  o.pa = P.p4a[k];
+  const float4 pb = P.p4b[k];
+  o.dsx = pb.x;
+  o.dsy = pb.y;
+}
+
+// HEAVY: also load the constants now (a step ahead of their use) rather
+// than at the visit.
+template <bool HEAVY>
 __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, int xdir, int ydir,
                                         const PeriodDev& P, const WSlot& V, const Box& box,
                                         bool last) {
@@ -279,14 +293,8 @@ __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, i
   const int k = i + nx * j;
   o.frz = box.has(i, j);
   o.own = V.tau[k];
-  const float4 sv = V.S[k];
-  o.t0 = sv.x;
-  o.gx = sv.y;
-  o.gy = sv.z;
-  o.pa = P.p4a[k];
-  const float4 pb = P.p4b[k];
-  o.dsx = pb.x;
-  o.dsy = pb.y;
+  o.t0 = reinterpret_cast<const float*>(V.S)[4 * k];
+  if (HEAVY) wf_load_heavy(o, k, P, V);
   if (last) o.old = V.old[k];
 }
 
@@ -338,7 +346,11 @@ __device__ __forceinline__ void w_from_above(const float (&x)[MB], float (&out)[
   }
 }
 
-template <int MB>
+// PF = 1: every operand of the next step is loaded a step ahead; PF = 0:
+// only the values exchanged between lanes are, the cell's constants are
+// loaded at the visit (they stream along the lane's row and hit in L1),
+// which frees registers for more resident warps.
+template <int MB, int PF>
 __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w, int lane,
                                     int* status_out, int* iters_out) {
   const int nx = P.nx, ny = P.ny;
@@ -357,13 +369,13 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
         t0prev[m] = 0.f;
-        wf_load(cur[m], 0, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+        wf_load<PF == 1>(cur[m], 0, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
       }
       for (int t = 0; t < nsteps; ++t) {
         WFwd nxt[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m)
-          wf_load(nxt[m], t + 1, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+          wf_load<PF == 1>(nxt[m], t + 1, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
         float south[MB], t0s[MB], north[MB], t0n[MB], nown[MB], nt0[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m) {
@@ -383,6 +395,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
             if (cur[m].frz) {
               nv = cur[m].own;
             } else {
+              if (PF == 0) wf_load_heavy(cur[m], k, P, V);
               nv = wf_visit(cur[m], res[m], nown[m], south[m], north[m], t0prev[m], nt0[m],
                             t0s[m], t0n[m], u > 0, v > 0, u < nx - 1, v < ny - 1, xdir, ydir,
                             idx, idy);
@@ -617,7 +630,7 @@ __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, d
 // ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
-template <int MB>
+template <int MB, int PF>
 __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
   const int lane = threadIdx.x & 31;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -661,7 +674,7 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
     }
     w_t0(P, x0, y0, w, V, lane);
     int fst = ST_OK, fit = 0;
-    w_fwd_sweeps<MB>(P, V, w, lane, &fst, &fit);
+    w_fwd_sweeps<MB, PF>(P, V, w, lane, &fst, &fit);
     if (A.fwd_updates && lane == 0) {
       const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
       A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
@@ -755,24 +768,51 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
 
 int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 
-void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st) {
-  switch (bands) {
-    case 1: k_batch_fp32w<1><<<grid, 128, 0, st>>>(a); break;
-    case 2: k_batch_fp32w<2><<<grid, 128, 0, st>>>(a); break;
-    case 3: k_batch_fp32w<3><<<grid, 128, 0, st>>>(a); break;
-    default: k_batch_fp32w<4><<<grid, 128, 0, st>>>(a); break;
+template <int MB, int PF>
+static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
+  k_batch_fp32w<MB, PF><<<grid, 128, 0, st>>>(a);
+}
+
+template <int MB, int PF>
+static int occupancy_w() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF>, 128, 0);
+  return n;
+}
+
+void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int pf, cudaStream_t st) {
+  if (pf) {
+    switch (bands) {
+      case 1: launch_w<1, 1>(a, grid, st); break;
+      case 2: launch_w<2, 1>(a, grid, st); break;
+      case 3: launch_w<3, 1>(a, grid, st); break;
+      default: launch_w<4, 1>(a, grid, st); break;
+    }
+  } else {
+    switch (bands) {
+      case 1: launch_w<1, 0>(a, grid, st); break;
+      case 2: launch_w<2, 0>(a, grid, st); break;
+      case 3: launch_w<3, 0>(a, grid, st); break;
+      default: launch_w<4, 0>(a, grid, st); break;
+    }
   }
 }
 
-int batch_fp32w_max_blocks_per_sm(int bands) {
-  int n = 0;
-  switch (bands) {
-    case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<1>, 128, 0); break;
-    case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<2>, 128, 0); break;
-    case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<3>, 128, 0); break;
-    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<4>, 128, 0); break;
+int batch_fp32w_max_blocks_per_sm(int bands, int pf) {
+  if (pf) {
+    switch (bands) {
+      case 1: return occupancy_w<1, 1>();
+      case 2: return occupancy_w<2, 1>();
+      case 3: return occupancy_w<3, 1>();
+      default: return occupancy_w<4, 1>();
+    }
   }
-  return n;
+  switch (bands) {
+    case 1: return occupancy_w<1, 0>();
+    case 2: return occupancy_w<2, 0>();
+    case 3: return occupancy_w<3, 0>();
+    default: return occupancy_w<4, 0>();
+  }
 }
 
 }  // namespace sgb

@@ -24,7 +24,22 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
   }
 }
 
-int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan) {
+std::vector<std::pair<int, int>> plan_candidates(const EvalShape& sh, int prec) {
+  std::vector<std::pair<int, int>> c;
+  if (prec == 0) {
+    c.push_back({KK_FP64, 0});
+    return c;
+  }
+  if (sh.max_ny <= 128 && sh.max_nx <= 4096) {
+    c.push_back({KK_FP32_WARP, 1});
+    c.push_back({KK_FP32_WARP, 0});
+  }
+  if (sh.max_diag <= kFp32MaxThreads) c.push_back({KK_FP32_BLOCK, 0});
+  return c;
+}
+
+int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan,
+                    int force_kind, int force_pf) {
   int nsm = 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
     return ST_CUDA_ERROR;
@@ -34,13 +49,14 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.block = 128;
     p.per_sm = batch_fp64_max_blocks_per_sm(p.block);
     p.ws_doubles = batch_fp64_ws_doubles(sh.max_cells);
-  } else if (sh.max_ny <= 128 && sh.max_nx <= 4096) {
+  } else if (force_kind != KK_FP32_BLOCK && sh.max_ny <= 128 && sh.max_nx <= 4096) {
     // one warp per solve, lanes own the rows
     p.kind = KK_FP32_WARP;
     p.block = 128;
     p.slots_per_block = 4;
     p.bands = fp32w_bands(sh.max_ny);
-    p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands);
+    p.pf = force_pf >= 0 ? force_pf : 1;
+    p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
     p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
   } else {
     // one block per solve, one thread per cell of the longest anti-diagonal
@@ -85,7 +101,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   if (sh.nsolve > 0) {
     if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_BLOCK) launch_batch_fp32(A, plan.grid, plan.block, st);
-    else launch_batch_fp32w(A, plan.grid, plan.bands, st);
+    else launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
     ++launches;
   }
   if (ev_k1) cudaEventRecord(ev_k1, st);

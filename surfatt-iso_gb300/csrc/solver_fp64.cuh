@@ -19,7 +19,9 @@
 
 namespace sgb {
 
-// Per-cell constants of the plain forward sweep (index * N + cell).
+// Per-cell constants of the plain forward sweep, one contiguous record of
+// KC_COUNT doubles per cell (K[cell * KC_COUNT + index]): a visit reads one
+// record instead of one word from each of 26 arrays.
 enum FwdConst {
   KC_CX = 0,     // T0/dx
   KC_CY,         // T0/dy
@@ -43,7 +45,7 @@ struct FwdWs {
   double* tau;
   double* tau_old;
   double* T0;
-  double* K;  // KC_COUNT * N
+  double* K;  // N records of KC_COUNT (hoisted path) or T0x, T0y arrays (WENO3)
 };
 
 // Frozen source box (:859-872): |(xx(i)-x0)/dx| <= R and |(yy(j)-y0)/dy| <= R.
@@ -157,27 +159,27 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
     const double a = P.a[k], b = P.b[k], c = P.c[k];
     const double cx = t0 / dx, cy = t0 / dy;
     const double pxm = t0x + cx, pxp = t0x - cx, pym = t0y + cy, pyp = t0y - cy;
-    double* K = W.K;
-    K[KC_CX * N + k] = cx;
-    K[KC_CY * N + k] = cy;
-    K[KC_PXM * N + k] = pxm;
-    K[KC_PXP * N + k] = pxp;
-    K[KC_PYM * N + k] = pym;
-    K[KC_PYP * N + k] = pyp;
+    double* K = W.K + k * (size_t)KC_COUNT;
+    K[KC_CX] = cx;
+    K[KC_CY] = cy;
+    K[KC_PXM] = pxm;
+    K[KC_PXP] = pxp;
+    K[KC_PYM] = pym;
+    K[KC_PYP] = pyp;
 #pragma unroll
     for (int cs = 0; cs < 4; ++cs) {
       const double px = cs < 2 ? pxm : pxp;
       const double py = (cs == 0 || cs == 2) ? pym : pyp;
       const double ea = a * (px * px) + b * (py * py) - 2 * c * px * py;
-      K[(KC_EA + cs) * N + k] = ea;
-      K[(KC_IEA + cs) * N + k] = 1.0 / ea;
-      K[(KC_BX + cs) * N + k] = a * px - c * py;
-      K[(KC_BY + cs) * N + k] = b * py - c * px;
+      K[KC_EA + cs] = ea;
+      K[KC_IEA + cs] = 1.0 / ea;
+      K[KC_BX + cs] = a * px - c * py;
+      K[KC_BY + cs] = b * py - c * px;
     }
-    K[KC_IPXM * N + k] = 1.0 / pxm;
-    K[KC_IPXP * N + k] = 1.0 / pxp;
-    K[KC_IPYM * N + k] = 1.0 / pym;
-    K[KC_IPYP * N + k] = 1.0 / pyp;
+    K[KC_IPXM] = 1.0 / pxm;
+    K[KC_IPXP] = 1.0 / pxp;
+    K[KC_IPYM] = 1.0 / pym;
+    K[KC_IPYP] = 1.0 / pyp;
   }
   __syncthreads();
 }
@@ -185,14 +187,15 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
 // One visit of cell k by the plain first-order upwind update (:904-1079):
 // returns min(tau, every causal two-sided root, every admissible one-sided
 // root).
-__device__ __forceinline__ double uw_update(const double* __restrict__ K, size_t N, size_t k,
+__device__ __forceinline__ double uw_update(const double* __restrict__ Kall, size_t N, size_t k,
                                             int i, int j, int nx, int ny,
                                             const double* __restrict__ tau,
                                             const double* __restrict__ T0, double a, double b,
                                             double c, double f2, double disx, double disy,
                                             double t) {
   const bool hw = i > 0, he = i < nx - 1, hs = j > 0, hn = j < ny - 1;
-  const double cx = K[KC_CX * N + k], cy = K[KC_CY * N + k];
+  const double* __restrict__ K = Kall + k * (size_t)KC_COUNT;
+  const double cx = K[KC_CX], cy = K[KC_CY];
   const double tw = hw ? tau[k - 1] : 0.0, te = he ? tau[k + 1] : 0.0;
   const double ts = hs ? tau[k - nx] : 0.0, tn = hn ? tau[k + nx] : 0.0;
   const double qw = -(cx * tw), qe = cx * te, qs = -(cy * ts), qn = cy * tn;
@@ -202,15 +205,15 @@ __device__ __forceinline__ double uw_update(const double* __restrict__ K, size_t
     if (!ok) continue;
     const double qx = cs < 2 ? qw : qe;
     const double qy = (cs == 0 || cs == 2) ? qs : qn;
-    const double ea = K[(KC_EA + cs) * N + k];
-    const double bx = K[(KC_BX + cs) * N + k], by = K[(KC_BY + cs) * N + k];
+    const double ea = K[KC_EA + cs];
+    const double bx = K[KC_BX + cs], by = K[KC_BY + cs];
     const double Cx = a * qx - c * qy;
     const double Cy = b * qy - c * qx;
     const double ec = qx * Cx + qy * Cy - f2;
     const double hb = bx * qx + by * qy;
     const double del = hb * hb - ea * ec;
     if (del >= 0) {
-      const double iea = K[(KC_IEA + cs) * N + k];
+      const double iea = K[KC_IEA + cs];
       const double s = sqrt(del);
       const double r1 = (-hb + s) * iea, r2 = (-hb - s) * iea;
       const double x1 = bx * r1 + Cx, y1 = by * r1 + Cy;
@@ -232,7 +235,7 @@ __device__ __forceinline__ double uw_update(const double* __restrict__ K, size_t
     const double tnb = cs == 0 ? tw : cs == 1 ? te : cs == 2 ? ts : tn;
     const size_t nb = cs == 0 ? k - 1 : cs == 1 ? k + 1 : cs == 2 ? k - nx : k + nx;
     const double dis = cs < 2 ? disx : disy;
-    const double ip = K[(KC_IPXM + cs) * N + k];
+    const double ip = K[KC_IPXM + cs];
     const double lim = tnb * T0[nb], half = tnb * 0.5;
     const double r1 = (dis - q) * ip, r2 = (-dis - q) * ip;
     if (r1 * t0 >= lim && r1 > half && r1 < t) t = r1;
@@ -349,11 +352,12 @@ __device__ inline void adj_setup(const PeriodDev& P, const AdjWs& W, int nfield)
       ws = b1p / dy * id;
       wn = -(b2m / dy) * id;
     }
-    W.K[KA_WW * N + k] = ww;
-    W.K[KA_WE * N + k] = we;
-    W.K[KA_WS * N + k] = ws;
-    W.K[KA_WN * N + k] = wn;
-    W.K[KA_ID * N + k] = id;
+    double* Kr = W.K + k * (size_t)KA_COUNT;  // one record per cell
+    Kr[KA_WW] = ww;
+    Kr[KA_WE] = we;
+    Kr[KA_WS] = ws;
+    Kr[KA_WN] = wn;
+    Kr[KA_ID] = id;
     for (int f = 0; f < nfield; ++f) W.Ta[f][k] = 100;
   }
   __syncthreads();
@@ -381,9 +385,10 @@ __device__ inline void adj_sweeps(const PeriodDev& P, const AdjWs& W, int nfield
           int i, j;
           g.cell(d, v, i, j);
           const size_t k = (size_t)i + (size_t)nx * j;
-          const double ww = K[KA_WW * N + k], we = K[KA_WE * N + k];
-          const double ws = K[KA_WS * N + k], wn = K[KA_WN * N + k];
-          const double id = K[KA_ID * N + k];
+          const double* Kr = K + k * (size_t)KA_COUNT;
+          const double ww = Kr[KA_WW], we = Kr[KA_WE];
+          const double ws = Kr[KA_WS], wn = Kr[KA_WN];
+          const double id = Kr[KA_ID];
 #pragma unroll
           for (int f = 0; f < 2; ++f) {
             if (!active[f]) continue;

@@ -41,8 +41,11 @@ EXPORTED = [
     "surfatt_engine_create", "surfatt_engine_destroy", "surfatt_engine_load",
     "surfatt_engine_update_velocity", "surfatt_engine_run", "surfatt_engine_sync",
     "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
-    "surfatt_engine_launch_config",
+    "surfatt_engine_launch_config", "surfatt_engine_autotune", "surfatt_engine_kernel_variant",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
+    "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
+    "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
+    "surfatt_server_stats", "surfatt_server_reset_stats",
 ]
 
 
@@ -409,6 +412,27 @@ class Engine:
             raise SurfattError(st, "engine_launch_config")
         return dict(grid=g.value, block=b.value, blocks_per_sm=n.value, smem_bytes=sm.value)
 
+    def autotune(self, mode=MODE_2D, precision=PREC_FP32):
+        """Time the applicable kernel variants and keep the fastest."""
+        L = lib()
+        L.surfatt_engine_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip,
+                                              _ip, _dp]
+        k, p, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        st = L.surfatt_engine_autotune(self._h, int(mode), int(precision), ctypes.byref(k),
+                                       ctypes.byref(p), ctypes.byref(ms))
+        if st != OK:
+            raise SurfattError(st, "engine_autotune")
+        return dict(kind=k.value, prefetch=p.value, kernel_ms=ms.value)
+
+    def kernel_variant(self):
+        L = lib()
+        L.surfatt_engine_kernel_variant.argtypes = [ctypes.c_void_p, _ip, _ip]
+        k, p = ctypes.c_int(0), ctypes.c_int(0)
+        st = L.surfatt_engine_kernel_variant(self._h, ctypes.byref(k), ctypes.byref(p))
+        if st != OK:
+            raise SurfattError(st, "engine_kernel_variant")
+        return dict(kind=k.value, prefetch=p.value)
+
     def work(self):
         f, a = ctypes.c_double(0), ctypes.c_double(0)
         st = lib().surfatt_engine_work(self._h, ctypes.byref(f), ctypes.byref(a))
@@ -424,3 +448,112 @@ class Engine:
         self.run(mode, precision)
         self.sync()
         return self.results()
+
+
+# ---------------------------------------------------------------------------
+# serving loop
+# ---------------------------------------------------------------------------
+class _CServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("failed", ctypes.c_longlong), ("solves", ctypes.c_longlong),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("span_s", ctypes.c_double),
+                ("solves_per_s", ctypes.c_double), ("hbm_budget_bytes", ctypes.c_size_t),
+                ("hbm_peak_bytes", ctypes.c_size_t), ("inflight_peak", ctypes.c_int)]
+
+
+class Server:
+    """Request loop on one GPU: resident models and work lists, requests
+    admitted by an HBM budget and run concurrently (continuous batching)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=8 << 30, max_inflight=4):
+        L = lib()
+        L.surfatt_server_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                            ctypes.c_size_t, ctypes.c_int]
+        L.surfatt_server_destroy.argtypes = [ctypes.c_void_p]
+        L.surfatt_server_destroy.restype = None
+        L.surfatt_server_add_model.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _ip]
+        L.surfatt_server_add_worklist.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                  _ip]
+        L.surfatt_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, ctypes.c_int,
+                                            ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+        L.surfatt_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double,
+                                          ctypes.c_void_p, _dp]
+        L.surfatt_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.surfatt_server_reset_stats.argtypes = [ctypes.c_void_p]
+        self._h = ctypes.c_void_p()
+        st = L.surfatt_server_create(ctypes.byref(self._h), device, int(hbm_budget_bytes),
+                                     int(max_inflight))
+        if st != OK:
+            raise SurfattError(st, "server_create")
+        self._shape = {}
+
+    def close(self):
+        if self._h:
+            lib().surfatt_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_model(self, pb):
+        keep = []
+        cp = pack_problem(pb, keep)
+        mid = ctypes.c_int(0)
+        st = lib().surfatt_server_add_model(self._h, ctypes.byref(cp), ctypes.byref(mid))
+        if st != OK:
+            raise SurfattError(st, "server_add_model")
+        return mid.value
+
+    def add_worklist(self, model_id, pb):
+        keep = []
+        cp = pack_problem(pb, keep)
+        wid = ctypes.c_int(0)
+        st = lib().surfatt_server_add_worklist(self._h, int(model_id), ctypes.byref(cp),
+                                               ctypes.byref(wid))
+        if st != OK:
+            raise SurfattError(st, "server_add_worklist")
+        self._shape[wid.value] = (pb.ncell, pb.npath, pb.nsolve)
+        return wid.value
+
+    def submit(self, worklist_id, svel=None, mode=MODE_2D, precision=PREC_FP64):
+        t = ctypes.c_longlong(0)
+        v = None if svel is None else np.ascontiguousarray(svel, dtype=np.float64)
+        st = lib().surfatt_server_submit(self._h, int(worklist_id),
+                                         None if v is None else _d(v), int(mode), int(precision),
+                                         ctypes.byref(t))
+        if st != OK:
+            raise SurfattError(st, "server_submit")
+        return (t.value, worklist_id)
+
+    def wait(self, ticket, timeout_s=0.0):
+        """Returns (status, result dict, latency_ms)."""
+        tk, wid = ticket
+        ncell, npath, nsolve = self._shape[wid]
+        out = dict(adj_s=np.zeros(max(ncell, 1)), adj_density=np.zeros(max(ncell, 1)),
+                   tt_fwd=np.zeros(max(npath, 1)), chi=np.zeros(1),
+                   status=np.zeros(max(nsolve, 1), np.int32),
+                   fwd_iters=np.zeros(max(nsolve, 1), np.int32),
+                   adj_iters=np.zeros(max(nsolve, 1), np.int32))
+        r = _CResult(_d(out["adj_s"]), _d(out["adj_density"]), _d(out["chi"]),
+                     _d(out["tt_fwd"]), out["status"].ctypes.data_as(_ip),
+                     out["fwd_iters"].ctypes.data_as(_ip), out["adj_iters"].ctypes.data_as(_ip))
+        lat = ctypes.c_double(0)
+        st = lib().surfatt_server_wait(self._h, tk, float(timeout_s), ctypes.byref(r),
+                                       ctypes.byref(lat))
+        out["chi"] = float(out["chi"][0])
+        out["tt_fwd"] = out["tt_fwd"][:npath]
+        return st, out, lat.value
+
+    def stats(self):
+        s = _CServerStats()
+        st = lib().surfatt_server_stats(self._h, ctypes.byref(s))
+        if st != OK:
+            raise SurfattError(st, "server_stats")
+        return {f: getattr(s, f) for f, _ in _CServerStats._fields_}
+
+    def reset_stats(self):
+        lib().surfatt_server_reset_stats(self._h)
