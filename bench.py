@@ -37,6 +37,7 @@ sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
 # this workload by `python oracle/count_flops.py config2 32`.
 FWD_FLOPS_PER_VISIT = 351.8
 ADJ_FLOPS_PER_VISIT = 16.0
+KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w"}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
 
 
@@ -47,7 +48,11 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=["config1", "config2", "config2s", "config4"])
+                    choices=["config1", "config2", "config2s", "config4", "serving"])
+    ap.add_argument("--requests", type=int, default=40,
+                    help="serving: requests in the Poisson stream")
+    ap.add_argument("--load", type=float, default=0.7,
+                    help="serving: offered load as a fraction of the closed-loop capacity")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -355,7 +360,8 @@ def run_ours(args):
                          "achieved": ach32, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": ach32 / fp32_peak, "traffic": traffic,
                          "peak_source": "surfatt_measure_peaks (FP32 FMA chains), this run",
-                         "kernel": "k_batch_fp32", "kernel_ms": k32_ms,
+                         "kernel": KERNEL_NAMES.get(launch32.get("kind"), "k_batch_fp32"),
+                         "kernel_ms": k32_ms,
                          "flops_per_launch": flops32},
             "cpu_baseline": cpu, "parity": parity,
             "launch": {"fp32": launch32, "fp64": launch64, "autotune": tuned},
@@ -407,9 +413,71 @@ def run_reference(args):
         dist.destroy_process_group()
 
 
+def run_serving(args):
+    """Serving workload (curved surface, seed 4): a closed-loop pass (every
+    request queued at once) measures the server's capacity; the Poisson
+    stream then offers `--load` of that capacity and its p50/p99 request
+    latency and solves/s are reported.  Each rank serves its own stream."""
+    import torch
+    import surfatt_gb300 as sg
+    from surfatt_gb300 import serving as S
+    dist, rank, world, local = _dist()
+    sg.build()
+    torch.cuda.set_device(local)
+    cat = S.Catalog()
+    reqs = S.make_requests(cat, args.requests, seed=4)
+    srv = sg.Server(local, hbm_budget_bytes=16 << 30, max_inflight=8)
+    mids = {n: srv.add_model(cat.models[n]) for n in cat.models}
+    # warm-up: the first requests of the stream, run once and discarded
+    warm = S.run_poisson(srv, reqs[:max(3, args.warmup)], 1e6, sg.PREC_FP32, model_ids=mids)
+    closed = S.run_poisson(srv, reqs, 1e6, sg.PREC_FP32, model_ids=mids)
+    cap_rate = len(reqs) / closed["wall_s"]
+    rate = args.load * cap_rate
+    clocks = Clocks(local)
+    _barrier(dist, local)
+    clocks.start()
+    res = S.run_poisson(srv, reqs, rate, sg.PREC_FP32, seed=5, model_ids=mids)
+    _barrier(dist, local)
+    ck = clocks.stop()
+    st = srv.stats()
+    lat = np.asarray(res["latency_ms"])
+    bad = [s for s in res["status"] + closed["status"] + warm["status"] if s not in (0, 3)]
+    wall = _max_over_ranks(dist, res["wall_s"], local)
+    kinds = {k: sum(1 for r in reqs if r["kind"] == k) for k in ("gradient", "linesearch",
+                                                                   "checkerboard")}
+    if rank == 0:
+        line = {
+            "metric": "serving solves/s (Poisson request stream, FP32-factored)",
+            "value": res["solves"] * world / wall, "unit": "solves/s", "n_gpus": world,
+            "steps": len(reqs), "warmup": len(warm["status"]), "ms_per_step": float(np.mean(lat)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 sweep / f64 T0, misfit, kernels", "data": "synthetic",
+            "config": {"workload": "serving on a curved surface (seed 4): Gaussian island 4 km "
+                                   "+ 200 m roughness, surface-metric eikonal, grids 64^2..512^2, "
+                                   "15 periods, 140 stations; requests of 10-120 sources x 1-15 "
+                                   "periods (gradient / line-search trial / checkerboard forward)",
+                       "requests": len(reqs), "request_kinds": kinds,
+                       "solves": res["solves"], "offered_rate_per_s": rate,
+                       "closed_loop_rate_per_s": cap_rate, "load": args.load,
+                       "hbm_budget_bytes": st["hbm_budget_bytes"], "max_inflight": 8},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "closed_loop": {"solves_per_s": closed["solves"] / closed["wall_s"],
+                            "p50_ms": float(np.percentile(closed["latency_ms"], 50)),
+                            "p99_ms": float(np.percentile(closed["latency_ms"], 99))},
+            "server_stats": st, "failed_requests": len(bad), "clocks": ck,
+        }
+        print(json.dumps(line))
+    srv.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 if __name__ == "__main__":
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "serving":
+        run_serving(a)
     else:
         run_ours(a)

@@ -241,17 +241,38 @@ surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* engine, int* gri
                                               int* blocks_per_sm, size_t* smem_bytes);
 
 /* Time every solve-kernel variant that applies to the loaded problem (plain
- * FP64: one; FP32: one warp per solve with or without operand prefetch, one
- * block per solve) with one warm-up and one timed evaluation each, and use
- * the fastest for later runs of this precision until the next load.  Returns
- * the chosen variant (0 FP64, 1 FP32 block, 2 FP32 warp), its prefetch flag
+ * FP64: one; FP32: the warp-per-solve kernel's variants -- 0 / 3: cell
+ * constants loaded at the visit, 12 / 8 resident warps per SM; 1 / 2: every
+ * operand loaded a step ahead, 8 / 12 resident warps per SM -- and the
+ * block-per-solve kernel) with one warm-up and one timed evaluation each,
+ * and use the fastest for later runs of this precision until the next load.
+ * Returns the chosen kernel (0 FP64, 1 FP32 block, 2 FP32 warp), its variant
  * and its solve-kernel time. */
 surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* engine, surfatt_mode_t mode,
-                                         surfatt_precision_t precision, int* kind, int* prefetch,
+                                         surfatt_precision_t precision, int* kind, int* variant,
                                          double* best_ms);
-/* Variant and prefetch flag used by the last run. */
-surfatt_status_t surfatt_engine_kernel_variant(surfatt_engine_t* engine, int* kind,
-                                               int* prefetch);
+/* Choose the solve kernel of later runs at `precision` by hand (as
+ * surfatt_engine_autotune would): kind (0 FP64, 1 FP32 block, 2 FP32 warp)
+ * and warp-kernel variant (0..3); -1 leaves a field automatic.  A kernel that
+ * does not apply to the loaded grids makes the next run return
+ * SURFATT_BAD_ARG. */
+surfatt_status_t surfatt_engine_set_kernel(surfatt_engine_t* engine, surfatt_precision_t precision,
+                                          int kind, int variant);
+/* Per-phase SM cycle counters of the FP32 warp kernel (default: off).  When
+ * on, every run sums clock64() intervals per solve phase over all solves:
+ * [0] source cell + T0, [1] forward sweeps, [2] receiver times + misfit,
+ * [3] adjoint coefficients + sources, [4] adjoint sweeps, [5] mask + kernel
+ * slot; surfatt_engine_phase_cycles copies the six sums of the last run. */
+surfatt_status_t surfatt_engine_set_profile(surfatt_engine_t* engine, int enable);
+surfatt_status_t surfatt_engine_phase_cycles(surfatt_engine_t* engine, double* cycles);
+/* Kernel and variant used by the last run. */
+surfatt_status_t surfatt_engine_kernel_variant(surfatt_engine_t* engine, int* kind, int* variant);
+
+/* Capture each (mode, precision) evaluation -- resets, solve kernel, kernel
+ * sums, misfit sum -- into a CUDA graph on its first run and replay it with
+ * one graph launch afterwards (default: on).  A load, or a buffer that had to
+ * grow, makes the next run capture again; a velocity update does not. */
+surfatt_status_t surfatt_engine_set_graphs(surfatt_engine_t* engine, int enable);
 
 /* Total sweep cell visits of the last run (forward, adjoint), for the
  * algorithmic roofline. */

@@ -476,17 +476,36 @@ struct surfatt_engine {
       d_fun, d_f2, d_disx, d_disy, d_f32, d_isv, d_p4a, d_p4b, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
       d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
   DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
-      d_fupd, d_aupd, d_ws, d_queue;
+      d_fupd, d_aupd, d_ws, d_queue, d_phase;
   int grid = 0, block = 128, per_sm = 0, last_block = 0, last_kind = 0, last_pf = 0;
   size_t last_smem = 0;
-  int tuned_kind[2] = {-1, -1}, tuned_pf[2] = {-1, -1};  // per precision, -1: automatic
+  KernelChoice tuned[2];  // per precision; -1 fields: automatic
+  // Captured evaluations: one executable graph per (mode, precision), valid
+  // while the buffers and the problem shape it was captured on are unchanged
+  // (`gen` moves on every load and every reallocation).
+  struct Captured {
+    cudaGraphExec_t exec = nullptr;
+    long long gen = -1;
+    int kind = -1, pf = -1, grid = 0, launches = 0;
+  };
+  Captured graphs[4][2];
+  long long gen = 0;
+  bool use_graphs = true;
+  bool profile = false;  // per-phase cycle counters of the FP32 warp kernel
+  void drop_graphs() {
+    for (auto& m : graphs)
+      for (auto& g : m) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = Captured();
+      }
+  }
   std::vector<DBuf*> all() {
     return {&d_periods, &d_xdeg, &d_ydeg, &d_xs, &d_ys, &d_cosy, &d_siny, &d_A, &d_B, &d_C,
             &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_f32, &d_isv, &d_p4a, &d_p4b, &d_pidx, &d_srcx, &d_srcy,
             &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
             &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
             &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
-            &d_aupd, &d_ws, &d_queue};
+            &d_aupd, &d_ws, &d_queue, &d_phase};
   }
 };
 
@@ -496,6 +515,7 @@ int eng_ensure(surfatt_engine* e, DBuf& b, size_t bytes) {
   b.counter = &e->allocated;
   if (bytes <= b.cap) return SURFATT_OK;
   if (e->budget && e->allocated - b.cap + bytes > e->budget) return SURFATT_OOM;
+  ++e->gen;  // a captured evaluation may hold the old pointer
   return b.ensure(bytes);
 }
 
@@ -556,6 +576,7 @@ void surfatt_engine_destroy(surfatt_engine_t* e) {
   if (!e) return;
   cudaSetDevice(e->device);
   cudaStreamSynchronize(e->st);
+  e->drop_graphs();
   for (DBuf* b : e->all()) b->release();
   cudaEventDestroy(e->ev0);
   cudaEventDestroy(e->ev1);
@@ -570,8 +591,8 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   CK(cudaSetDevice(e->device));
   e->loaded = false;
   e->ran = false;
-  e->tuned_kind[0] = e->tuned_kind[1] = -1;
-  e->tuned_pf[0] = e->tuned_pf[1] = -1;
+  ++e->gen;
+  e->tuned[0] = e->tuned[1] = KernelChoice();
   const int np = pb->nperiod, ns = pb->nsolve;
   e->nperiod = np;
   e->nsolve = ns;
@@ -709,12 +730,16 @@ surfatt_status_t surfatt_engine_update_velocity(surfatt_engine_t* e, const doubl
 }  // extern "C"
 
 namespace {
-int engine_enqueue(surfatt_engine* e, int mode, int prec, int force_kind, int force_pf) {
+// Enqueue one evaluation.  With `graph`, the evaluation (resets, solve
+// kernel, kernel sums, misfit sum) is captured once into an executable graph
+// per (mode, precision) and replayed by one cudaGraphLaunch afterwards.
+int engine_enqueue(surfatt_engine* e, int mode, int prec, const KernelChoice& force,
+                   bool graph = false) {
   CK(cudaSetDevice(e->device));
   EvalShape sh;
   sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
   LaunchPlan plan;
-  int r = plan_evaluation(sh, prec, e->device, 0, &plan, force_kind, force_pf);
+  int r = plan_evaluation(sh, prec, e->device, 0, &plan, force);
   if (r) return (surfatt_status_t)r;
   r = eng_ensure(e, e->d_ws,
                  (size_t)plan.grid * plan.slots_per_block * plan.ws_doubles * sizeof(double));
@@ -753,6 +778,11 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, int force_kind, int fo
   A.fwd_updates = e->d_fupd.as<double>();
   A.adj_updates = e->d_aupd.as<double>();
   A.Tout = nullptr;
+  if (e->profile) {
+    r = eng_ensure(e, e->d_phase, PH_COUNT * sizeof(unsigned long long));
+    if (r) return r;
+    A.phase_cycles = e->d_phase.as<unsigned long long>();
+  }
   dev.plist_off = e->d_plist_off.as<int>();
   dev.plist = e->d_plist.as<int>();
   dev.goff = e->d_goff.as<long long>();
@@ -761,12 +791,47 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, int force_kind, int fo
   dev.chi_total = e->d_chi.as<double>();
   dev.adj_s = e->d_adj.as<double>();
   dev.adj_density = e->d_adjd.as<double>();
-  CK(cudaEventRecord(e->ev0, e->st));
-  const int n = enqueue_evaluation(sh, dev, plan, mode, prec, e->d_ws.as<double>(),
-                                   e->d_queue.as<int>(), e->st, e->evk0, e->evk1);
-  if (n < 0) return -n;
-  CK(cudaEventRecord(e->ev1, e->st));
-  e->launches = n;
+  if (graph) {
+    auto& g = e->graphs[mode][prec];
+    if (!g.exec || g.gen != e->gen || g.kind != plan.kind || g.pf != plan.pf ||
+        g.grid != plan.grid) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = surfatt_engine::Captured();
+      cudaGraph_t gr = nullptr;
+      CK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeRelaxed));
+      const int n = enqueue_evaluation(sh, dev, plan, mode, prec, e->d_ws.as<double>(),
+                                       e->d_queue.as<int>(), e->st, e->evk0, e->evk1);
+      const cudaError_t ce = cudaStreamEndCapture(e->st, &gr);
+      if (n < 0 || ce != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        cudaGetLastError();
+        return n < 0 ? -n : SURFATT_CUDA_ERROR;
+      }
+      const cudaError_t ci = cudaGraphInstantiate(&g.exec, gr, 0);
+      cudaGraphDestroy(gr);
+      if (ci != cudaSuccess) {
+        g.exec = nullptr;
+        cudaGetLastError();
+        return SURFATT_CUDA_ERROR;
+      }
+      g.gen = e->gen;
+      g.kind = plan.kind;
+      g.pf = plan.pf;
+      g.grid = plan.grid;
+      g.launches = n;
+    }
+    CK(cudaEventRecord(e->ev0, e->st));
+    CK(cudaGraphLaunch(g.exec, e->st));
+    CK(cudaEventRecord(e->ev1, e->st));
+    e->launches = g.launches;
+  } else {
+    CK(cudaEventRecord(e->ev0, e->st));
+    const int n = enqueue_evaluation(sh, dev, plan, mode, prec, e->d_ws.as<double>(),
+                                     e->d_queue.as<int>(), e->st, e->evk0, e->evk1);
+    if (n < 0) return -n;
+    CK(cudaEventRecord(e->ev1, e->st));
+    e->launches = n;
+  }
   e->ran = true;
   e->last_mode = mode;
   return SURFATT_OK;
@@ -782,11 +847,51 @@ surfatt_status_t surfatt_engine_run(surfatt_engine_t* e, surfatt_mode_t mode,
     return SURFATT_BAD_ARG;
   if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
   const int p = prec == SURFATT_PREC_FP64 ? 0 : 1;
-  return (surfatt_status_t)engine_enqueue(e, mode, p, e->tuned_kind[p], e->tuned_pf[p]);
+  return (surfatt_status_t)engine_enqueue(e, mode, p, e->tuned[p],
+                                          e->use_graphs);
+}
+
+surfatt_status_t surfatt_engine_set_kernel(surfatt_engine_t* e, surfatt_precision_t prec,
+                                          int kind, int variant) {
+  if (!e) return SURFATT_BAD_ARG;
+  if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
+  const int p = prec == SURFATT_PREC_FP64 ? 0 : 1;
+  if (p == 0 && kind != -1 && kind != KK_FP64) return SURFATT_BAD_ARG;
+  if (p == 1 && kind != -1 && kind != KK_FP32_BLOCK && kind != KK_FP32_WARP)
+    return SURFATT_BAD_ARG;
+  if (variant < -1 || variant >= fp32w_variant_count()) return SURFATT_BAD_ARG;
+  e->tuned[p] = KernelChoice{kind, variant};
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_set_profile(surfatt_engine_t* e, int enable) {
+  if (!e) return SURFATT_BAD_ARG;
+  e->profile = enable != 0;
+  ++e->gen;  // the kernel arguments change
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_phase_cycles(surfatt_engine_t* e, double* cycles) {
+  if (!e || !e->ran || !cycles || !e->profile || !e->d_phase.p) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->st));
+  unsigned long long c[PH_COUNT];
+  CK(cudaMemcpy(c, e->d_phase.p, sizeof(c), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < PH_COUNT; ++i) cycles[i] = (double)c[i];
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_set_graphs(surfatt_engine_t* e, int enable) {
+  if (!e) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->st));
+  e->use_graphs = enable != 0;
+  if (!e->use_graphs) e->drop_graphs();
+  return SURFATT_OK;
 }
 
 surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* e, surfatt_mode_t mode,
-                                         surfatt_precision_t prec, int* kind, int* pf,
+                                         surfatt_precision_t prec, int* kind, int* variant,
                                          double* best_ms) {
   if (!e || !e->loaded) return SURFATT_BAD_ARG;
   if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
@@ -794,25 +899,29 @@ surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* e, surfatt_mode_t mod
   EvalShape sh;
   sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
   double best = 1e300;
-  int bk = -1, bp = -1;
-  for (const auto& c : plan_candidates(sh, p)) {
+  KernelChoice bc;
+  // one warm-up and one timed evaluation of a candidate
+  auto time_one = [&](const KernelChoice& c) -> int {
     float ms = 0.f;
-    int r = engine_enqueue(e, mode, p, c.first, c.second);  // warm-up / first touch
-    if (r) return (surfatt_status_t)r;
-    r = engine_enqueue(e, mode, p, c.first, c.second);
-    if (r) return (surfatt_status_t)r;
+    int r = engine_enqueue(e, mode, p, c);
+    if (r) return r;
+    r = engine_enqueue(e, mode, p, c);
+    if (r) return r;
     CK(cudaEventSynchronize(e->ev1));
     CK(cudaEventElapsedTime(&ms, e->evk0, e->evk1));
     if (ms < best) {
       best = ms;
-      bk = c.first;
-      bp = c.second;
+      bc = c;
     }
+    return SURFATT_OK;
+  };
+  for (const auto& c : plan_candidates(sh, p)) {
+    const int r = time_one(c);
+    if (r) return (surfatt_status_t)r;
   }
-  e->tuned_kind[p] = bk;
-  e->tuned_pf[p] = bp;
-  if (kind) *kind = bk;
-  if (pf) *pf = bp;
+  e->tuned[p] = bc;
+  if (kind) *kind = bc.kind;
+  if (variant) *variant = bc.variant;
   if (best_ms) *best_ms = best;
   return SURFATT_OK;
 }

@@ -68,6 +68,18 @@ struct BatchArgs {
   int max_nx;              // largest nx over periods (shared-memory column arrays)
   int smem_tau;            // FP32 kernel: 1 = tau / Ta in shared memory
   size_t smem_bytes;       // FP32 kernel: dynamic shared memory per block
+  unsigned long long* phase_cycles = nullptr;  // optional: SM cycles per solve phase, summed
+};
+
+// Solve phases timed when BatchArgs::phase_cycles is set (FP32 warp kernel).
+enum SolvePhase {
+  PH_SETUP = 0,     // source cell, frozen box, T0 field
+  PH_FWD = 1,       // forward sweeps
+  PH_RECV = 2,      // receiver times, misfit, outlier weights
+  PH_ADJ_SETUP = 3, // adjoint coefficients and sources
+  PH_ADJ = 4,       // adjoint sweeps
+  PH_SLOT = 5,      // mask and kernel slot
+  PH_COUNT = 6
 };
 
 void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st);
@@ -95,9 +107,11 @@ void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plis
                               const long long* kslot, const float* contrib, double* out,
                               const long long* goff_dev, const int* nx_dev, const int* ny_dev,
                               cudaStream_t st);
-// Warp-per-solve FP32 kernel (grids of at most 32*bands rows).
-void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int pf, cudaStream_t st);
-int batch_fp32w_max_blocks_per_sm(int bands, int pf);
+// Warp-per-solve FP32 kernel (grids of at most 32*bands rows), one warp per
+// block; `variant` < fp32w_variant_count() selects prefetch and register cap.
+void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st);
+int batch_fp32w_max_blocks_per_sm(int bands, int variant);
+int fp32w_variant_count();
 long long batch_fp32w_ws_doubles(long long N);
 int fp32w_bands(int max_ny);
 // chi = sum of per-solve misfits in work-list order (src/acqui.f90:135)

@@ -72,6 +72,7 @@ __device__ __forceinline__ double shfl_d(double v, int src) {
   return __shfl_sync(FULL, v, src);
 }
 
+
 // ---------------------------------------------------------------------------
 // setup
 // ---------------------------------------------------------------------------
@@ -630,10 +631,13 @@ __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, d
 // ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
-template <int MB, int PF>
-__global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
+// One warp per block; MINW resident warps per SM is the launch bound.  The
+// register file is split between the SM's four schedulers, so 8 warps (two
+// per scheduler) allow 255 registers a thread and 12 warps (three) 168.
+template <int MB, int PF, int MINW>
+__global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
   const int lane = threadIdx.x & 31;
-  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long gw = blockIdx.x;
   double* base = A.ws + gw * A.ws_doubles;
   float* kf = reinterpret_cast<float*>(A.kcontrib);
   float* kdf = reinterpret_cast<float*>(A.kcontrib_den);
@@ -650,6 +654,16 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
     const WSlot V = wcarve(base, N);
     const double xd0 = A.srcx[s], yd0 = A.srcy[s];
     const double x0 = xd0 / 180.0 * PI_S, y0 = yd0 / 180.0 * PI_S;
+    unsigned long long* const pc = A.phase_cycles;
+    long long c0 = pc ? clock64() : 0;
+    // adds the cycles since the previous mark to phase `ph` (lane 0, when on)
+    auto mark = [&](int ph) {
+      if (pc) {
+        const long long c1 = clock64();
+        if (lane == 0) atomicAdd(pc + ph, (unsigned long long)(c1 - c0));
+        c0 = c1;
+      }
+    };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
     if (w.status != ST_OK) {
       for (int r = lane; r < nr; r += 32) {
@@ -673,8 +687,10 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
       continue;
     }
     w_t0(P, x0, y0, w, V, lane);
+    mark(PH_SETUP);
     int fst = ST_OK, fit = 0;
     w_fwd_sweeps<MB, PF>(P, V, w, lane, &fst, &fit);
+    mark(PH_FWD);
     if (A.fwd_updates && lane == 0) {
       const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
       A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
@@ -703,6 +719,7 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
       }
     }
     __syncwarp();
+    mark(PH_RECV);
     int st = fst;
     if (bad && st == ST_OK) st = ST_BAD_ARG;
     int aiters = 0;
@@ -736,10 +753,12 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
       }
       st = __shfl_sync(FULL, st, 0);
       __syncwarp();
+      mark(PH_ADJ_SETUP);
       int its[2] = {0, 0};
       for (int f = 0; f < nf; ++f) {
         int ast = ST_OK;
         w_adj_sweeps<MB>(P, V, V.src[f], lane, &ast, &its[f]);
+        mark(PH_ADJ);
         if (ast != ST_OK && st == ST_OK) st = ast;
         // mask (:1449-1467) and the slot adj/svel**k (:314-315), FP32 here,
         // summed per period in FP64
@@ -752,6 +771,7 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
             out[k] = w.mbox.has(i, j) ? 0.f : V.tau[k] * isv;
           }
         __syncwarp();
+        mark(PH_SLOT);
       }
       aiters = its[0] > its[1] ? its[0] : its[1];
       if (A.adj_updates && lane == 0)
@@ -768,50 +788,61 @@ __global__ void __launch_bounds__(128) k_batch_fp32w(BatchArgs A) {
 
 int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 
-template <int MB, int PF>
+// Variants of the warp kernel: operand prefetch and resident warps per SM.
+//   0: constants loaded at the visit, 12 warps per SM (168 registers)
+//   1: every operand loaded a step ahead, 8 warps per SM (255 registers)
+//   2: every operand loaded a step ahead, 12 warps per SM (168, some spills)
+//   3: constants loaded at the visit, 8 warps per SM
+constexpr int kFp32wVariants = 4;
+int fp32w_variant_count() { return kFp32wVariants; }
+
+template <int MB, int PF, int MINW>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
-  k_batch_fp32w<MB, PF><<<grid, 128, 0, st>>>(a);
+  k_batch_fp32w<MB, PF, MINW><<<grid, 32, 0, st>>>(a);
 }
 
-template <int MB, int PF>
+template <int MB, int PF, int MINW>
 static int occupancy_w() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF, MINW>, 32, 0);
   return n;
 }
 
-void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int pf, cudaStream_t st) {
-  if (pf) {
-    switch (bands) {
-      case 1: launch_w<1, 1>(a, grid, st); break;
-      case 2: launch_w<2, 1>(a, grid, st); break;
-      case 3: launch_w<3, 1>(a, grid, st); break;
-      default: launch_w<4, 1>(a, grid, st); break;
-    }
-  } else {
-    switch (bands) {
-      case 1: launch_w<1, 0>(a, grid, st); break;
-      case 2: launch_w<2, 0>(a, grid, st); break;
-      case 3: launch_w<3, 0>(a, grid, st); break;
-      default: launch_w<4, 0>(a, grid, st); break;
-    }
+template <int MB>
+static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st) {
+  switch (variant) {
+    case 0: launch_w<MB, 0, 12>(a, grid, st); break;
+    case 1: launch_w<MB, 1, 8>(a, grid, st); break;
+    case 2: launch_w<MB, 1, 12>(a, grid, st); break;
+    default: launch_w<MB, 0, 8>(a, grid, st); break;
   }
 }
 
-int batch_fp32w_max_blocks_per_sm(int bands, int pf) {
-  if (pf) {
-    switch (bands) {
-      case 1: return occupancy_w<1, 1>();
-      case 2: return occupancy_w<2, 1>();
-      case 3: return occupancy_w<3, 1>();
-      default: return occupancy_w<4, 1>();
-    }
+template <int MB>
+static int occupancy_mb(int variant) {
+  switch (variant) {
+    case 0: return occupancy_w<MB, 0, 12>();
+    case 1: return occupancy_w<MB, 1, 8>();
+    case 2: return occupancy_w<MB, 1, 12>();
+    default: return occupancy_w<MB, 0, 8>();
   }
+}
+
+void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st) {
   switch (bands) {
-    case 1: return occupancy_w<1, 0>();
-    case 2: return occupancy_w<2, 0>();
-    case 3: return occupancy_w<3, 0>();
-    default: return occupancy_w<4, 0>();
+    case 1: launch_mb<1>(a, grid, variant, st); break;
+    case 2: launch_mb<2>(a, grid, variant, st); break;
+    case 3: launch_mb<3>(a, grid, variant, st); break;
+    default: launch_mb<4>(a, grid, variant, st); break;
+  }
+}
+
+int batch_fp32w_max_blocks_per_sm(int bands, int variant) {
+  switch (bands) {
+    case 1: return occupancy_mb<1>(variant);
+    case 2: return occupancy_mb<2>(variant);
+    case 3: return occupancy_mb<3>(variant);
+    default: return occupancy_mb<4>(variant);
   }
 }
 

@@ -24,22 +24,21 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
   }
 }
 
-std::vector<std::pair<int, int>> plan_candidates(const EvalShape& sh, int prec) {
-  std::vector<std::pair<int, int>> c;
+std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
+  std::vector<KernelChoice> c;
   if (prec == 0) {
     c.push_back({KK_FP64, 0});
     return c;
   }
-  if (sh.max_ny <= 128 && sh.max_nx <= 4096) {
-    c.push_back({KK_FP32_WARP, 1});
-    c.push_back({KK_FP32_WARP, 0});
-  }
+  if (sh.max_ny <= 128 && sh.max_nx <= 4096)
+    for (int v = 0; v < fp32w_variant_count(); ++v)
+      c.push_back({KK_FP32_WARP, v});
   if (sh.max_diag <= kFp32MaxThreads) c.push_back({KK_FP32_BLOCK, 0});
   return c;
 }
 
 int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan,
-                    int force_kind, int force_pf) {
+                    const KernelChoice& force) {
   int nsm = 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
     return ST_CUDA_ERROR;
@@ -49,19 +48,22 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.block = 128;
     p.per_sm = batch_fp64_max_blocks_per_sm(p.block);
     p.ws_doubles = batch_fp64_ws_doubles(sh.max_cells);
-  } else if (force_kind != KK_FP32_BLOCK && sh.max_ny <= 128 && sh.max_nx <= 4096) {
+  } else if (force.kind == KK_FP32_WARP && !(sh.max_ny <= 128 && sh.max_nx <= 4096)) {
+    return ST_BAD_ARG;  // the warp kernel holds at most 128 rows
+  } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= 128 && sh.max_nx <= 4096) {
     // one warp per solve, lanes own the rows
     p.kind = KK_FP32_WARP;
-    p.block = 128;
-    p.slots_per_block = 4;
+    p.block = 32;
+    p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
-    p.pf = force_pf >= 0 ? force_pf : 1;
+    p.pf = force.variant >= 0 && force.variant < fp32w_variant_count() ? force.variant : 1;
     p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
     p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
   } else {
     // one block per solve, one thread per cell of the longest anti-diagonal
     if (sh.max_diag > kFp32MaxThreads) return ST_BAD_ARG;
     p.kind = KK_FP32_BLOCK;
+    p.pf = 0;
     p.block = std::max(32, (sh.max_diag + 31) / 32 * 32);
     p.smem = batch_fp32_smem_bytes(sh.max_pitched, sh.max_nx, &p.smem_tau);
     p.per_sm = batch_fp32_max_blocks_per_sm(p.block, p.smem, p.smem_tau);
@@ -90,13 +92,22 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   A.smem_bytes = plan.smem;
   int launches = 0;
   if (cudaMemsetAsync(queue, 0, sizeof(int), st) != cudaSuccess) return -ST_CUDA_ERROR;
+  if (A.phase_cycles &&
+      cudaMemsetAsync(A.phase_cycles, 0, PH_COUNT * sizeof(unsigned long long), st) != cudaSuccess)
+    return -ST_CUDA_ERROR;
   if (sh.npath > 0 &&
       cudaMemsetAsync(A.tt_fwd, 0, (size_t)sh.npath * sizeof(double), st) != cudaSuccess)
     return -ST_CUDA_ERROR;
   if (A.adj_updates && sh.nsolve > 0 &&
       cudaMemsetAsync(A.adj_updates, 0, (size_t)sh.nsolve * sizeof(double), st) != cudaSuccess)
     return -ST_CUDA_ERROR;
-  if (ev_k0) cudaEventRecord(ev_k0, st);
+  // Inside a stream capture the timing events become event-record nodes of
+  // the graph (recorded at every replay).
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cap);
+  const unsigned ev_flags =
+      cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+  if (ev_k0) cudaEventRecordWithFlags(ev_k0, st, ev_flags);
   (void)prec;
   if (sh.nsolve > 0) {
     if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
@@ -104,7 +115,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
     else launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
     ++launches;
   }
-  if (ev_k1) cudaEventRecord(ev_k1, st);
+  if (ev_k1) cudaEventRecordWithFlags(ev_k1, st, ev_flags);
   if (mode >= 2) {
     const int nf = mode == 3 ? 2 : 1;
     for (int f = 0; f < nf; ++f) {

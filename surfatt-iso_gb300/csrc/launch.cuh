@@ -37,6 +37,12 @@ struct EvalDev {
 // (any grid), FP32 one warp per solve (grids of at most 128 rows).
 enum KernelKind { KK_FP64 = 0, KK_FP32_BLOCK = 1, KK_FP32_WARP = 2 };
 
+// A solve-kernel choice; -1 fields are picked automatically.  `variant`
+// indexes the warp kernel's operand-prefetch / register-cap variants.
+struct KernelChoice {
+  int kind = -1, variant = -1;
+};
+
 struct LaunchPlan {
   int kind = KK_FP64;
   int grid = 0, block = 0, per_sm = 0, smem_tau = 0, bands = 0, pf = 1;
@@ -48,13 +54,13 @@ struct LaunchPlan {
 // Launch configuration for `prec` (0 FP64, 1 FP32) on `device`; grid capped
 // at `max_grid` (0 = resident capacity of the device).  Returns ST_BAD_ARG
 // when a grid's diagonal exceeds the FP32 kernel's block limit.
-// `force_kind` / `force_pf` (-1: automatic) select a kernel variant, as the
-// autotuner does when it times the candidates.
+// `force` selects a kernel variant, as the autotuner does when it times the
+// candidates.
 int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan,
-                    int force_kind = -1, int force_pf = -1);
+                    const KernelChoice& force = KernelChoice());
 
 // Kernel variants the autotuner times for an evaluation of this shape.
-std::vector<std::pair<int, int>> plan_candidates(const EvalShape& sh, int prec);
+std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec);
 
 // Enqueue the evaluation on `st`: queue reset, tt_fwd reset, solve kernel,
 // per-period reductions (modes 2, 3) and the misfit sum.  `ws` must hold

@@ -42,6 +42,8 @@ EXPORTED = [
     "surfatt_engine_update_velocity", "surfatt_engine_run", "surfatt_engine_sync",
     "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
     "surfatt_engine_launch_config", "surfatt_engine_autotune", "surfatt_engine_kernel_variant",
+    "surfatt_engine_set_graphs", "surfatt_engine_set_kernel", "surfatt_engine_set_profile",
+    "surfatt_engine_phase_cycles",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
     "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
     "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
@@ -417,21 +419,56 @@ class Engine:
         L = lib()
         L.surfatt_engine_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip,
                                               _ip, _dp]
-        k, p, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        k, v, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
         st = L.surfatt_engine_autotune(self._h, int(mode), int(precision), ctypes.byref(k),
-                                       ctypes.byref(p), ctypes.byref(ms))
+                                       ctypes.byref(v), ctypes.byref(ms))
         if st != OK:
             raise SurfattError(st, "engine_autotune")
-        return dict(kind=k.value, prefetch=p.value, kernel_ms=ms.value)
+        return dict(kind=k.value, variant=v.value, kernel_ms=ms.value)
 
     def kernel_variant(self):
         L = lib()
         L.surfatt_engine_kernel_variant.argtypes = [ctypes.c_void_p, _ip, _ip]
-        k, p = ctypes.c_int(0), ctypes.c_int(0)
-        st = L.surfatt_engine_kernel_variant(self._h, ctypes.byref(k), ctypes.byref(p))
+        k, v = ctypes.c_int(0), ctypes.c_int(0)
+        st = L.surfatt_engine_kernel_variant(self._h, ctypes.byref(k), ctypes.byref(v))
         if st != OK:
             raise SurfattError(st, "engine_kernel_variant")
-        return dict(kind=k.value, prefetch=p.value)
+        return dict(kind=k.value, variant=v.value)
+
+    def set_kernel(self, precision, kind=-1, variant=-1):
+        """Fix the solve kernel of later runs (-1: automatic)."""
+        L = lib()
+        L.surfatt_engine_set_kernel.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 3
+        st = L.surfatt_engine_set_kernel(self._h, int(precision), int(kind), int(variant))
+        if st != OK:
+            raise SurfattError(st, "engine_set_kernel")
+
+    PHASES = ("setup", "forward", "receivers", "adjoint_setup", "adjoint", "slot")
+
+    def set_profile(self, enable):
+        """Per-phase cycle counters of the FP32 warp kernel (default off)."""
+        L = lib()
+        L.surfatt_engine_set_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        st = L.surfatt_engine_set_profile(self._h, 1 if enable else 0)
+        if st != OK:
+            raise SurfattError(st, "engine_set_profile")
+
+    def phase_cycles(self):
+        c = np.zeros(6)
+        L = lib()
+        L.surfatt_engine_phase_cycles.argtypes = [ctypes.c_void_p, _dp]
+        st = L.surfatt_engine_phase_cycles(self._h, _d(c))
+        if st != OK:
+            raise SurfattError(st, "engine_phase_cycles")
+        return dict(zip(self.PHASES, c.tolist()))
+
+    def set_graphs(self, enable):
+        """Capture/replay evaluations as CUDA graphs (default on)."""
+        L = lib()
+        L.surfatt_engine_set_graphs.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        st = L.surfatt_engine_set_graphs(self._h, 1 if enable else 0)
+        if st != OK:
+            raise SurfattError(st, "engine_set_graphs")
 
     def work(self):
         f, a = ctypes.c_double(0), ctypes.c_double(0)

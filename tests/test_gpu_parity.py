@@ -255,3 +255,46 @@ def test_engine_source_on_boundary_status(sg, oracle):
     assert got["status"][1] == sg.SOURCE_ON_BOUNDARY == ref["status"][1]
     assert rel_max(got["adj_s"], ref["adj_s"]) <= KER_TOL
     eng.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_fp32_warp_variants(sg, oracle, variant):
+    """Every warp-kernel variant agrees with the oracle within the FP32
+    tolerances, and all variants give the same bits (they differ only in when
+    operands are loaded and in register allocation)."""
+    pb = W.flat_case(nx=100, ny=90, nsta=6, nperiod=2, mode=3, seed=31)
+    ref = oracle.gradient_eval(pb, mode=3, nthreads=4)
+    eng = sg.Engine(0)
+    eng.load(pb)
+    eng.set_kernel(sg.PREC_FP32, kind=2, variant=0)
+    eng.run(3, sg.PREC_FP32)
+    assert eng.sync() == sg.OK
+    base = eng.results()
+    eng.set_kernel(sg.PREC_FP32, kind=2, variant=variant)
+    eng.run(3, sg.PREC_FP32)
+    assert eng.sync() == sg.OK
+    assert eng.kernel_variant() == dict(kind=2, variant=variant)
+    o = eng.results()
+    assert np.array_equal(o["tt_fwd"], base["tt_fwd"])
+    assert np.array_equal(o["adj_s"], base["adj_s"])
+    assert np.array_equal(o["adj_density"], base["adj_density"])
+    assert np.all(o["status"] == ref["status"])
+    assert rel_pointwise(o["tt_fwd"], ref["tt_fwd"]) <= TT_TOL_F32
+    for p in range(pb.nperiod):
+        sl = slice(int(pb.goff[p]), int(pb.goff[p] + pb.nx[p] * pb.ny[p]))
+        assert rel_max(o["adj_s"][sl], ref["adj_s"][sl]) <= KER_TOL_F32
+        assert rel_max(o["adj_density"][sl], ref["adj_density"][sl]) <= KER_TOL_F32
+    eng.close()
+
+
+def test_forced_warp_kernel_rejects_tall_grid(sg):
+    pb = W.flat_case(nx=40, ny=140, nsta=3, nperiod=1, mode=2, seed=32)
+    eng = sg.Engine(0)
+    eng.load(pb)
+    eng.set_kernel(sg.PREC_FP32, kind=2)
+    with pytest.raises(sg.SurfattError):
+        eng.run(2, sg.PREC_FP32)
+    eng.set_kernel(sg.PREC_FP32)
+    eng.run(2, sg.PREC_FP32)
+    assert eng.sync() == sg.OK
+    eng.close()
