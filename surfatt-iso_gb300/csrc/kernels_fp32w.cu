@@ -22,12 +22,10 @@
 // in FP64 with the reference's own formula within two cells of the source.
 // Misfit, receiver times, the convergence decisions (FP64 reduction of the
 // lanes' partial sums) and the per-period kernel sums are FP64.
-#include "kernels.cuh"
-#include "solver_fp64.cuh"
+#include "warp_common.cuh"
 
 namespace sgb {
 
-constexpr unsigned FULL = 0xffffffffu;
 
 // Workspace per warp slot: S (float4: T0, T0x, T0y, -), W (float4 adjoint
 // weights), tau, old, 1/d, two scaled adjoint sources.
@@ -60,85 +58,12 @@ __device__ inline WSlot wcarve(double* base, size_t N) {
   return V;
 }
 
-struct WSolve {
-  int status;
-  double fun0;
-  Box box;   // frozen source box
-  Box mbox;  // mask box (|x-x0| < 1.5 dx, |y-y0| < 1.5 dy)
-  int si, sj;  // source cell
-};
-
-__device__ __forceinline__ double shfl_d(double v, int src) {
-  return __shfl_sync(FULL, v, src);
-}
-
-
-// ---------------------------------------------------------------------------
-// setup
-// ---------------------------------------------------------------------------
-__device__ inline WSolve w_locate(const PeriodDev& P, double x0, double y0, double xd0,
-                                  double yd0, int lane) {
-  WSolve w;
-  const int nx = P.nx, ny = P.ny;
-  if (lane == 0) {
-    w.status = ST_OK;
-    w.fun0 = 0;
-    float r1 = 0.f, r2 = 0.f;
-    const int i0 = locate_cell(P.xs, nx - 1, P.dx, x0, &r1);
-    const int j0 = locate_cell(P.ys, ny - 1, P.dy, y0, &r2);
-    if (i0 < 0 || j0 < 0) {
-      w.status = ST_BAD_ARG;
-      w.si = w.sj = 0;
-    } else {
-      float w00 = (1 - r1) * (1 - r2), w01 = (1 - r1) * r2, w10 = r1 * (1 - r2), w11 = r1 * r2;
-      const size_t k00 = i0 + (size_t)nx * j0;
-      w.fun0 = (double)w00 * P.fun[k00] + (double)w01 * P.fun[k00 + nx] +
-               (double)w10 * P.fun[k00 + 1] + (double)w11 * P.fun[k00 + nx + 1];
-      w.si = i0;
-      w.sj = j0;
-    }
-    int a0 = nx, a1 = -1, b0 = ny, b1 = -1, c0 = nx, c1 = -1, e0 = ny, e1 = -1;
-    const double ddx = P.xdeg[1] - P.xdeg[0], ddy = P.ydeg[1] - P.ydeg[0];
-    for (int i = 0; i < nx; ++i) {
-      if (fabs((P.xs[i] - x0) / P.dx) <= 1.0) { a0 = min(a0, i); a1 = max(a1, i); }
-      if (fabs(P.xdeg[i] - xd0) < 1.5 * ddx) { c0 = min(c0, i); c1 = max(c1, i); }
-    }
-    for (int j = 0; j < ny; ++j) {
-      if (fabs((P.ys[j] - y0) / P.dy) <= 1.0) { b0 = min(b0, j); b1 = max(b1, j); }
-      if (fabs(P.ydeg[j] - yd0) < 1.5 * ddy) { e0 = min(e0, j); e1 = max(e1, j); }
-    }
-    w.box = Box{a0, a1, b0, b1};
-    w.mbox = Box{c0, c1, e0, e1};
-    if (w.status == ST_OK && a0 <= a1 && b0 <= b1 &&
-        (a0 == 0 || a1 == nx - 1 || b0 == 0 || b1 == ny - 1))
-      w.status = ST_SOURCE_ON_BOUNDARY;
-  }
-  w.status = __shfl_sync(FULL, w.status, 0);
-  w.fun0 = shfl_d(w.fun0, 0);
-  w.si = __shfl_sync(FULL, w.si, 0);
-  w.sj = __shfl_sync(FULL, w.sj, 0);
-  w.box.i0 = __shfl_sync(FULL, w.box.i0, 0);
-  w.box.i1 = __shfl_sync(FULL, w.box.i1, 0);
-  w.box.j0 = __shfl_sync(FULL, w.box.j0, 0);
-  w.box.j1 = __shfl_sync(FULL, w.box.j1, 0);
-  w.mbox.i0 = __shfl_sync(FULL, w.mbox.i0, 0);
-  w.mbox.i1 = __shfl_sync(FULL, w.mbox.i1, 0);
-  w.mbox.j0 = __shfl_sync(FULL, w.mbox.j0, 0);
-  w.mbox.j1 = __shfl_sync(FULL, w.mbox.j1, 0);
-  return w;
-}
 
 // T0, T0x, T0y of every cell into S; tau initialised (1 in the frozen box).
-// d = 2 asin(sqrt(h)), h = sin^2(dy/2) + cos y cos y0 sin^2(dx/2), is the
-// reference's acos(sin y sin y0 + cos y cos y0 cos dx) without its
-// cancellation; sin d = 2 sqrt(h (1-h)).
 __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSolve& w,
                             const WSlot& V, int lane) {
   const int nx = P.nx, ny = P.ny;
-  const double rf = R_EARTH * w.fun0;
-  const float rff = (float)rf;
-  const float cy0 = (float)cos(y0);
-  const double cy0d = cos(y0), sy0d = sin(y0);
+  const T0Src src = t0_source(w, x0, y0);
   for (int i = lane; i < nx; i += 32) {
     const float hx = (float)((P.xs[i] - x0) * 0.5);
     V.col[i] = sinf(hx);
@@ -146,124 +71,16 @@ __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSol
   }
   __syncwarp();
   for (int j = 0; j < ny; ++j) {
-    const float hy = (float)((P.ys[j] - y0) * 0.5);
-    const float shy = sinf(hy), chy = cosf(hy);
-    const float cy = (float)P.cosy[j], sy = (float)P.siny[j];
+    const T0Row row = t0_row(P, src, j);
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
-      const float shx = V.col[i], chx = V.col[nx + i];
-      float t0, gx, gy;
-      if (abs(i - w.si) <= 2 && abs(j - w.sj) <= 2) {
-        // near the source: the reference's FP64 expressions (:847-856)
-        const double cyy = P.cosy[j], syy = P.siny[j];
-        const double cdx = cos(P.xs[i] - x0), sdx = sin(P.xs[i] - x0);
-        const double tmp = syy * sy0d + cyy * cy0d * cdx;
-        double cl = tmp < 1.0 ? tmp : 1.0;
-        cl = cl > -1.0 ? cl : -1.0;
-        const double td = acos(cl) * R_EARTH * w.fun0;
-        double tx = 0, ty = 0;
-        if (td != 0) {
-          const double rs = 1.0 / sqrt(1 - tmp * tmp);
-          tx = -(rs * cyy * cy0d * (-1.0) * sdx * R_EARTH * w.fun0);
-          ty = -(rs * (cyy * sy0d - syy * cy0d * cdx) * R_EARTH * w.fun0);
-        }
-        t0 = (float)td;
-        gx = (float)tx;
-        gy = (float)ty;
-      } else {
-        const float h = shy * shy + cy * cy0 * (shx * shx);
-        const float sh = sqrtf(h);
-        const float d = 2.f * asinf(fminf(sh, 1.f));
-        const float sind = 2.f * sh * sqrtf(fmaxf(1.f - h, 0.f));
-        t0 = rff * d;
-        if (sind > 0.f) {
-          const float inv = rff / sind;
-          gx = inv * cy * cy0 * (2.f * shx * chx);
-          // -(cos y sin y0 - sin y cos y0 cos dx) = -(sin(y0-y) + 2 sin y cos y0 sin^2(dx/2))
-          gy = -inv * (-2.f * shy * chy + 2.f * sy * cy0 * (shx * shx));
-        } else {
-          gx = 0.f;
-          gy = 0.f;
-        }
-      }
-      V.S[k] = make_float4(t0, gx, gy, 0.f);
+      V.S[k] = t0_cell(P, src, row, i, j, V.col[i], V.col[nx + i]);
       V.tau[k] = w.box.has(i, j) ? 1.0f : 10.0f;
     }
   }
   __syncwarp();
 }
 
-// ---------------------------------------------------------------------------
-// forward sweep visit (tau = tau_X + delta form, FP32x2 pairs)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float2 wbc(float x) { return make_float2(x, x); }
-__device__ __forceinline__ float2 wadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 wmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 wfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 wneg(float2 a) { return make_float2(-a.x, -a.y); }
-
-__device__ __forceinline__ float w_pick(float r, float chx, float chy, float sx, float sy, bool ok) {
-  const bool cx = sx > 0.f ? chx >= 0.f : chx <= 0.f;
-  const bool cy = sy > 0.f ? chy >= 0.f : chy <= 0.f;
-  return (ok && cx && cy) ? r : __int_as_float(0x7f800000);
-}
-
-__device__ __forceinline__ float w_two_sided(float2 px, float2 tX, float2 U0, float py, float tY,
-                                             float sY, float gy, float cy, float a, float b,
-                                             float c, float f2, bool okx, bool oky) {
-  const float2 A = wfma(px, wfma(wbc(a), px, wbc(-2.f * c * py)), wbc(b * py * py));
-  const float2 bx = wfma(wbc(a), px, wbc(-c * py));
-  const float2 by = wfma(wbc(-c), px, wbc(b * py));
-  const float2 V0 = wfma(wbc(gy), tX, wmul(wbc(-sY * cy), wadd(tX, wbc(-tY))));
-  const float2 CU = wfma(wbc(a), U0, wmul(wbc(-c), V0));
-  const float2 CV = wfma(wbc(b), V0, wmul(wbc(-c), U0));
-  const float2 C = wfma(U0, CU, wfma(V0, CV, wbc(-f2)));
-  const float2 H = wfma(bx, U0, wmul(by, V0));
-  const float2 D = wfma(H, H, wmul(wneg(A), C));
-  const bool vx = okx && D.x >= 0.f, vy = oky && D.y >= 0.f;
-  const float2 sq = make_float2(fsqrt_fast(D.x), fsqrt_fast(D.y));
-  const float2 ia = make_float2(frcp_fast(A.x), frcp_fast(A.y));
-  const float2 d1 = wmul(wadd(sq, wneg(H)), ia);
-  const float2 d2 = wmul(wadd(wneg(sq), wneg(H)), ia);
-  const float2 x1 = wfma(bx, d1, CU), y1 = wfma(by, d1, CV);
-  const float2 x2 = wfma(bx, d2, CU), y2 = wfma(by, d2, CV);
-  const float2 r1 = wadd(tX, d1), r2 = wadd(tX, d2);
-  const float sy = -sY;
-  float m = w_pick(r1.x, x1.x, y1.x, 1.f, sy, vx);
-  m = fminf(m, w_pick(r2.x, x2.x, y2.x, 1.f, sy, vx));
-  m = fminf(m, w_pick(r1.y, x1.y, y1.y, -1.f, sy, vy));
-  m = fminf(m, w_pick(r2.y, x2.y, y2.y, -1.f, sy, vy));
-  return m;
-}
-
-__device__ __forceinline__ float w_one_sided(float2 p, float2 tnb, float2 t0nb, float g,
-                                             float dis, float t0, bool okx, bool oky) {
-  const float2 ip = make_float2(frcp_fast(p.x), frcp_fast(p.y));
-  const float2 gt = wmul(wbc(g), tnb);
-  const float2 r1 = wfma(wadd(wbc(dis), wneg(gt)), ip, tnb);
-  const float2 r2 = wfma(wadd(wbc(-dis), wneg(gt)), ip, tnb);
-  const float2 lim = wmul(tnb, t0nb), half = wmul(tnb, wbc(0.5f));
-  const float2 s1 = wmul(r1, wbc(t0)), s2 = wmul(r2, wbc(t0));
-  const float inf = __int_as_float(0x7f800000);
-  float m = (okx && s1.x >= lim.x && r1.x > half.x) ? r1.x : inf;
-  m = fminf(m, (okx && s2.x >= lim.x && r2.x > half.x) ? r2.x : inf);
-  m = fminf(m, (oky && s1.y >= lim.y && r1.y > half.y) ? r1.y : inf);
-  m = fminf(m, (oky && s2.y >= lim.y && r2.y > half.y) ? r2.y : inf);
-  return m;
-}
-
-// Operands of one forward visit, loaded a step ahead.  The downstream
-// neighbours are not loaded here: the logical east cell (u+1, v) is this
-// band's next cell and the logical north cell (u, v+1) is the next cell of
-// the lane above, so their old tau and T0 come from `nxt` (own register or
-// __shfl_down); the south T0 comes from the lane below (__shfl_up).
-struct WFwd {
-  bool on, frz;
-  float own, old;  // old tau of the cell; tau at the start of the iteration
-  float t0, gx, gy;
-  float4 pa;       // a, b, c, fun^2
-  float dsx, dsy;
-};
 
 // The cell's constants (T0 gradient, metric, slowness, one-sided terms).
 __device__ __forceinline__ void wf_load_heavy(WFwd& o, int k, const PeriodDev& P, const WSlot& V) {
@@ -295,57 +112,12 @@ __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, i
   o.frz = box.has(i, j);
   o.own = V.tau[k];
   o.t0 = reinterpret_cast<const float*>(V.S)[4 * k];
-  if (HEAVY) wf_load_heavy(o, k, P, V);
-  if (last) o.old = V.old[k];
-}
-
-// Visit with logical neighbours mapped to the physical W/E/S/N of the
-// reference's update.  west/south: new values; east/north: old values.
-__device__ __forceinline__ float wf_visit(const WFwd& o, float west, float east, float south,
-                                          float north, float t0w, float t0e, float t0s, float t0n,
-                                          bool hasw, bool hass, bool hase, bool hasn, int xdir,
-                                          int ydir, float idx, float idy) {
-  const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
-  const float ts = ydir > 0 ? south : north, tn = ydir > 0 ? north : south;
-  const bool hw = xdir > 0 ? hasw : hase, he = xdir > 0 ? hase : hasw;
-  const bool hs = ydir > 0 ? hass : hasn, hn = ydir > 0 ? hasn : hass;
-  const float t0wp = xdir > 0 ? t0w : t0e, t0ep = xdir > 0 ? t0e : t0w;
-  const float t0sp = ydir > 0 ? t0s : t0n, t0np = ydir > 0 ? t0n : t0s;
-  const float t0 = o.t0, gx = o.gx, gy = o.gy;
-  const float a = o.pa.x, b = o.pa.y, c = o.pa.z, f2 = o.pa.w;
-  const float cx = t0 * idx, cy = t0 * idy;
-  const float2 px = make_float2(gx + cx, gx - cx);
-  const float2 tX = make_float2(tw, te);
-  const float2 U0 = wmul(wbc(gx), tX);
-  float m = w_two_sided(px, tX, U0, gy + cy, ts, -1.f, gy, cy, a, b, c, f2, hw && hs, he && hs);
-  m = fminf(m, w_two_sided(px, tX, U0, gy - cy, tn, 1.f, gy, cy, a, b, c, f2, hw && hn, he && hn));
-  m = fminf(m, w_one_sided(px, tX, make_float2(t0wp, t0ep), gx, o.dsx, t0, hw, he));
-  m = fminf(m, w_one_sided(make_float2(gy + cy, gy - cy), make_float2(ts, tn),
-                           make_float2(t0sp, t0np), gy, o.dsy, t0, hs, hn));
-  return fminf(o.own, m);
-}
-
-// Value of row v-1 held by the lane below (lane 31 of the band below for lane 0).
-template <int MB>
-__device__ __forceinline__ void w_from_below(const float (&x)[MB], float (&out)[MB], int lane) {
-#pragma unroll
-  for (int m = 0; m < MB; ++m) {
-    const float up = __shfl_up_sync(FULL, x[m], 1);
-    const float wr = __shfl_sync(FULL, x[m > 0 ? m - 1 : 0], 31);
-    out[m] = lane > 0 ? up : wr;
+  if (HEAVY) {
+    wf_load_heavy(o, k, P, V);
+    if (last) o.old = V.old[k];
   }
 }
 
-// Value of row v+1 held by the lane above (lane 0 of the band above for lane 31).
-template <int MB>
-__device__ __forceinline__ void w_from_above(const float (&x)[MB], float (&out)[MB], int lane) {
-#pragma unroll
-  for (int m = 0; m < MB; ++m) {
-    const float dn = __shfl_down_sync(FULL, x[m], 1);
-    const float wr = __shfl_sync(FULL, x[m + 1 < MB ? m + 1 : m], 0);
-    out[m] = lane < 31 ? dn : wr;
-  }
-}
 
 // PF = 1: every operand of the next step is loaded a step ahead; PF = 0:
 // only the values exchanged between lanes are, the cell's constants are
@@ -377,18 +149,17 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
 #pragma unroll
         for (int m = 0; m < MB; ++m)
           wf_load<PF == 1>(nxt[m], t + 1, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
-        float south[MB], t0s[MB], north[MB], t0n[MB], nown[MB], nt0[MB];
+        // Bands in descending order: band m's south neighbours include lane 31
+        // of band m-1, whose value must still be the previous step's.  Each
+        // band exchanges its values right before its visit, which keeps the
+        // live registers to one band's worth.
+        float dds[MB];
 #pragma unroll
-        for (int m = 0; m < MB; ++m) {
-          nown[m] = nxt[m].own;
-          nt0[m] = nxt[m].t0;
-        }
-        w_from_below<MB>(res, south, lane);
-        w_from_below<MB>(t0prev, t0s, lane);
-        w_from_above<MB>(nown, north, lane);
-        w_from_above<MB>(nt0, t0n, lane);
-#pragma unroll
-        for (int m = 0; m < MB; ++m) {
+        for (int mm = 0; mm < MB; ++mm) {
+          const int m = MB - 1 - mm;
+          const float south = w_below<MB>(res, m, lane), t0s = w_below<MB>(t0prev, m, lane);
+          const float north = w_above_own<MB>(nxt, m, lane), t0n = w_above_t0<MB>(nxt, m, lane);
+          dds[m] = 0.f;
           if (cur[m].on) {
             const int v = lane + 32 * m, u = t - v;
             const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? v : ny - 1 - v);
@@ -396,22 +167,28 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
             if (cur[m].frz) {
               nv = cur[m].own;
             } else {
-              if (PF == 0) wf_load_heavy(cur[m], k, P, V);
-              nv = wf_visit(cur[m], res[m], nown[m], south[m], north[m], t0prev[m], nt0[m],
-                            t0s[m], t0n[m], u > 0, v > 0, u < nx - 1, v < ny - 1, xdir, ydir,
-                            idx, idy);
+              if (PF == 0) {
+                wf_load_heavy(cur[m], k, P, V);
+                if (last) cur[m].old = V.old[k];
+              }
+              nv = wf_visit(cur[m], res[m], nxt[m].own, south, north, t0prev[m], nxt[m].t0, t0s,
+                            t0n, u > 0, v > 0, u < nx - 1, v < ny - 1, xdir, ydir, idx, idy);
             }
             V.tau[k] = nv;
             if (s == 0) V.old[k] = cur[m].own;
-            if (last && !cur[m].frz) {
-              const float dd = fabsf(nv - cur[m].old) * cur[m].t0;
-              l1 += dd;
-              lmax = fmaxf(lmax, dd);
-            }
+            if (last && !cur[m].frz) dds[m] = fabsf(nv - cur[m].old) * cur[m].t0;
             res[m] = nv;
             t0prev[m] = cur[m].t0;
           }
           cur[m] = nxt[m];
+        }
+        if (last) {
+          // in band order (the order of the row-major visit of a lane)
+#pragma unroll
+          for (int m = 0; m < MB; ++m) {
+            l1 += dds[m];
+            lmax = fmaxf(lmax, dds[m]);
+          }
         }
         __syncwarp();
       }
@@ -456,26 +233,9 @@ __device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, int lane)
       const float4 pk = PA[k], pw = PA[w], pe = PA[e], ps = PA[s], pn = PA[n];
       const float Tk = T(k), Tw = T(w), Te = T(e), Ts = T(s), Tn = T(n);
       const float Twn = T(w + nx), Tws = T(w - nx), Ten = T(e + nx), Tes = T(e - nx);
-      const float Tse = T(s + 1), Tsw = T(s - 1), Tne = T(n + 1), Tnw = T(n - 1);
-      const float a1 = -((Tk - Tw) * idx * (pk.x + pw.x) * 0.5f) +
-                       (Tn - Ts + Twn - Tws) * (0.25f * idy) * (pk.z + pw.z) * 0.5f;
-      const float a2 = -((Te - Tk) * idx * (pe.x + pk.x) * 0.5f) +
-                       (Ten - Tes + Tn - Ts) * (0.25f * idy) * (pe.z + pk.z) * 0.5f;
-      const float b1 = -((Tk - Ts) * idy * (pk.y + ps.y) * 0.5f) +
-                       (Te - Tw + Tse - Tsw) * (0.25f * idx) * (pk.z + ps.z) * 0.5f;
-      const float b2 = -((Tn - Tk) * idy * (pn.y + pk.y) * 0.5f) +
-                       (Tne - Tnw + Te - Tw) * (0.25f * idx) * (pn.z + pk.z) * 0.5f;
-      const float a1m = fminf(a1, 0.f), a1p = fmaxf(a1, 0.f);
-      const float a2m = fminf(a2, 0.f), a2p = fmaxf(a2, 0.f);
-      const float b1m = fminf(b1, 0.f), b1p = fmaxf(b1, 0.f);
-      const float b2m = fminf(b2, 0.f), b2p = fmaxf(b2, 0.f);
-      const float d = (a2p - a1m) * idx + (b2p - b1m) * idy;
-      float id = 0.f;
-      float4 W = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (!(fabsf(d) < (float)EPS14)) {
-        id = __frcp_rn(d);
-        W = make_float4(a1p * idx * id, -(a2m * idx) * id, b1p * idy * id, -(b2m * idy) * id);
-      }
+      float4 W;
+      const float id = adj_weights(Tk, Tw, Te, Ts, Tn, Twn, Tws, Ten, Tes, pk, pw, pe, ps, pn, idx,
+                                   idy, &W);
       V.W[k] = W;
       V.id[k] = id;
     }
@@ -489,6 +249,9 @@ struct WAdj {
   float4 w;  // ww, we, ws, wn
 };
 
+// HEAVY: the weights, source and iteration-start value too (a step ahead of
+// the visit); otherwise only the value the lanes exchange.
+template <bool HEAVY>
 __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, int nx, int xdir,
                                         int ydir, const WSlot& V, const float* src, bool last) {
   const int u = t - v;
@@ -501,15 +264,17 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
   const int j = ydir > 0 ? 1 + v : nv - v;
   const int k = i + nx * j;
   o.own = V.tau[k];
-  o.w = V.W[k];
-  o.src = src[k];
-  if (last) o.old = V.old[k];
+  if (HEAVY) {
+    o.w = V.W[k];
+    o.src = src[k];
+    if (last) o.old = V.old[k];
+  }
 }
 
 // Sweeps one adjoint field (held in V.tau) to convergence: the reference's
 // absolute rule (:1429) or no change beyond the FP32 resolution of the field.
 // Neighbours outside the interior are the boundary's zeros.
-template <int MB>
+template <int MB, int PF>
 __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src, int lane,
                                     int* status_out, int* iters_out) {
   const int nx = P.nx, ny = P.ny;
@@ -533,13 +298,13 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
-        wa_load(cur[m], 0, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+        wa_load<PF == 1>(cur[m], 0, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
       }
       for (int t = 0; t < nsteps; ++t) {
         WAdj nxt[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m)
-          wa_load(nxt[m], t + 1, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+          wa_load<PF == 1>(nxt[m], t + 1, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
         float south[MB], north[MB], nown[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m) nown[m] = nxt[m].own;
@@ -556,8 +321,12 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
             const float nth = v < nv - 1 ? north[m] : 0.f;
             const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
             const float ts = ydir > 0 ? sth : nth, tn = ydir > 0 ? nth : sth;
-            const float4 W = cur[m].w;
-            const float val = cur[m].src + W.x * tw + W.y * te + W.z * ts + W.w * tn;
+            if (PF == 0) {
+              cur[m].w = V.W[k];
+              cur[m].src = src[k];
+              if (last) cur[m].old = V.old[k];
+            }
+            const float val = adj_update(cur[m].src, cur[m].w, tw, te, ts, tn);
             V.tau[k] = val;
             if (s == 0) V.old[k] = cur[m].own;
             if (last) {
@@ -757,7 +526,7 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
       int its[2] = {0, 0};
       for (int f = 0; f < nf; ++f) {
         int ast = ST_OK;
-        w_adj_sweeps<MB>(P, V, V.src[f], lane, &ast, &its[f]);
+        w_adj_sweeps<MB, PF>(P, V, V.src[f], lane, &ast, &its[f]);
         mark(PH_ADJ);
         if (ast != ST_OK && st == ST_OK) st = ast;
         // mask (:1449-1467) and the slot adj/svel**k (:314-315), FP32 here,

@@ -11,7 +11,7 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
   nperiod = np;
   nsolve = ns;
   npath = npth;
-  ncell = max_cells = max_pitched = 0;
+  ncell = max_cells = max_pitched = max_dcells = 0;
   max_nx = max_ny = max_diag = 0;
   for (int p = 0; p < np; ++p) {
     const long long N = (long long)nxs[p] * nys[p];
@@ -21,6 +21,7 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
     max_ny = std::max(max_ny, nys[p]);
     max_diag = std::max(max_diag, std::min(nxs[p], nys[p]));
     max_pitched = std::max(max_pitched, (long long)batch_fp32_pitch(nxs[p]) * nys[p]);
+    max_dcells = std::max(max_dcells, diag_cells(nxs[p], nys[p]));
   }
 }
 
@@ -30,9 +31,11 @@ std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
     c.push_back({KK_FP64, 0});
     return c;
   }
-  if (sh.max_ny <= 128 && sh.max_nx <= 4096)
-    for (int v = 0; v < fp32w_variant_count(); ++v)
-      c.push_back({KK_FP32_WARP, v});
+  if (sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)
+  {
+    for (int v = 0; v < fp32d_variant_count(); ++v) c.push_back({KK_FP32_DIAG, v});
+    for (int v = 0; v < fp32w_variant_count(); ++v) c.push_back({KK_FP32_WARP, v});
+  }
   if (sh.max_diag <= kFp32MaxThreads) c.push_back({KK_FP32_BLOCK, 0});
   return c;
 }
@@ -48,17 +51,25 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.block = 128;
     p.per_sm = batch_fp64_max_blocks_per_sm(p.block);
     p.ws_doubles = batch_fp64_ws_doubles(sh.max_cells);
-  } else if (force.kind == KK_FP32_WARP && !(sh.max_ny <= 128 && sh.max_nx <= 4096)) {
-    return ST_BAD_ARG;  // the warp kernel holds at most 128 rows
-  } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= 128 && sh.max_nx <= 4096) {
+  } else if ((force.kind == KK_FP32_WARP || force.kind == KK_FP32_DIAG) &&
+             !(sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)) {
+    return ST_BAD_ARG;  // the warp kernels hold at most 128 rows
+  } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= kWarpMaxRows &&
+             sh.max_nx <= kWarpMaxCols) {
     // one warp per solve, lanes own the rows
-    p.kind = KK_FP32_WARP;
+    p.kind = force.kind == KK_FP32_WARP ? KK_FP32_WARP : KK_FP32_DIAG;
     p.block = 32;
     p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
-    p.pf = force.variant >= 0 && force.variant < fp32w_variant_count() ? force.variant : 1;
-    p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
-    p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
+    const int nvar = p.kind == KK_FP32_WARP ? fp32w_variant_count() : fp32d_variant_count();
+    p.pf = force.variant >= 0 && force.variant < nvar ? force.variant : (p.kind == KK_FP32_WARP ? 1 : 0);
+    if (p.kind == KK_FP32_WARP) {
+      p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
+      p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
+    } else {
+      p.per_sm = batch_fp32d_max_blocks_per_sm(p.bands, p.pf);
+      p.ws_doubles = batch_fp32d_ws_doubles(sh.max_dcells, sh.max_nx);
+    }
   } else {
     // one block per solve, one thread per cell of the longest anti-diagonal
     if (sh.max_diag > kFp32MaxThreads) return ST_BAD_ARG;
@@ -112,7 +123,8 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   if (sh.nsolve > 0) {
     if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_BLOCK) launch_batch_fp32(A, plan.grid, plan.block, st);
-    else launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
+    else if (plan.kind == KK_FP32_WARP) launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
+    else launch_batch_fp32d(A, plan.grid, plan.bands, plan.pf, st);
     ++launches;
   }
   if (ev_k1) cudaEventRecordWithFlags(ev_k1, st, ev_flags);
@@ -121,7 +133,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
     for (int f = 0; f < nf; ++f) {
       double* kc = f == 0 ? A.kcontrib : A.kcontrib_den;
       double* out = f == 0 ? dev.adj_s : dev.adj_density;
-      if (plan.kind == KK_FP32_WARP)
+      if (plan.kind == KK_FP32_WARP || plan.kind == KK_FP32_DIAG)
         launch_kernel_reduce_f32(sh.nperiod, dev.plist_off, dev.plist, A.kslot,
                                  reinterpret_cast<const float*>(kc), out, dev.goff, dev.nx,
                                  dev.ny, st);

@@ -443,7 +443,7 @@ class Engine:
         if st != OK:
             raise SurfattError(st, "engine_set_kernel")
 
-    PHASES = ("setup", "forward", "receivers", "adjoint_setup", "adjoint", "slot")
+    PHASES = ("setup", "forward", "receivers", "adjoint_setup", "adjoint", "slot", "stage_wait")
 
     def set_profile(self, enable):
         """Per-phase cycle counters of the FP32 warp kernel (default off)."""
@@ -454,7 +454,7 @@ class Engine:
             raise SurfattError(st, "engine_set_profile")
 
     def phase_cycles(self):
-        c = np.zeros(6)
+        c = np.zeros(len(self.PHASES))
         L = lib()
         L.surfatt_engine_phase_cycles.argtypes = [ctypes.c_void_p, _dp]
         st = L.surfatt_engine_phase_cycles(self._h, _d(c))

@@ -298,3 +298,60 @@ def test_forced_warp_kernel_rejects_tall_grid(sg):
     eng.run(2, sg.PREC_FP32)
     assert eng.sync() == sg.OK
     eng.close()
+
+
+def _run_kernel(sg, pb, mode, kind, variant):
+    eng = sg.Engine(0)
+    eng.load(pb)
+    eng.set_kernel(sg.PREC_FP32, kind=kind, variant=variant)
+    eng.run(mode, sg.PREC_FP32)
+    st = eng.sync()
+    kv = eng.kernel_variant()
+    out = eng.results()
+    eng.close()
+    return st, kv, out
+
+
+@pytest.mark.parametrize("case", ["square", "mixed", "mode2", "mode0"])
+def test_fp32_diagonal_layout_kernel(sg, oracle, case):
+    """The staged diagonal-layout kernel computes the row-per-lane kernel's
+    values (same visits in the same order, arithmetic without compiler
+    contraction: bitwise) and meets the FP32 tolerances against the oracle,
+    on one grid and on uneven grids of one evaluation."""
+    if case == "mixed":
+        pb = W.config4(nsrc=3, nperiod=4, nmax=120, nmin=36, span_deg=2.0)
+        mode = 3
+    else:
+        mode = {"square": 3, "mode2": 2, "mode0": 0}[case]
+        pb = W.flat_case(nx=97, ny=75, nsta=5, nperiod=2, mode=mode, seed=41)
+    st_d, kv_d, d = _run_kernel(sg, pb, mode, 3, 1)
+    st_w, kv_w, w = _run_kernel(sg, pb, mode, 2, 1)
+    assert kv_d["kind"] == 3 and kv_w["kind"] == 2
+    assert st_d == st_w
+    assert np.array_equal(d["status"], w["status"])
+    assert np.array_equal(d["fwd_iters"], w["fwd_iters"])
+    assert np.array_equal(d["tt_fwd"], w["tt_fwd"])
+    if mode >= 2:
+        assert np.array_equal(d["adj_iters"], w["adj_iters"])
+        for key in ("adj_s", "adj_density") if mode == 3 else ("adj_s",):
+            assert np.array_equal(d[key], w[key]), (key, rel_max(d[key], w[key]))
+    ref = oracle.gradient_eval(pb, mode=mode, nthreads=4)
+    assert np.all(d["status"] == ref["status"])
+    assert rel_pointwise(d["tt_fwd"], ref["tt_fwd"]) <= TT_TOL_F32
+    if mode >= 2:
+        for p in range(pb.nperiod):
+            sl = slice(int(pb.goff[p]), int(pb.goff[p] + pb.nx[p] * pb.ny[p]))
+            assert rel_max(d["adj_s"][sl], ref["adj_s"][sl]) <= KER_TOL_F32
+            if mode == 3:
+                assert rel_max(d["adj_density"][sl], ref["adj_density"][sl]) <= KER_TOL_F32
+
+
+@pytest.mark.parametrize("variant", [0, 2])
+def test_fp32_diagonal_variants(sg, variant):
+    pb = W.flat_case(nx=64, ny=100, nsta=4, nperiod=2, mode=3, seed=42)
+    _, _, base = _run_kernel(sg, pb, 3, 3, 1)
+    st, kv, o = _run_kernel(sg, pb, 3, 3, variant)
+    assert kv == dict(kind=3, variant=variant)
+    assert np.array_equal(o["tt_fwd"], base["tt_fwd"])
+    assert np.array_equal(o["adj_s"], base["adj_s"])
+    assert np.array_equal(o["adj_density"], base["adj_density"])
