@@ -37,7 +37,7 @@ sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
 # this workload by `python oracle/count_flops.py config2 32`.
 FWD_FLOPS_PER_VISIT = 351.8
 ADJ_FLOPS_PER_VISIT = 16.0
-KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w"}
+KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w", 3: "k_batch_fp32d"}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
 
 

@@ -493,6 +493,7 @@ struct surfatt_engine {
   };
   Captured graphs[4][2];
   long long gen = 0;
+  std::vector<long long> shape_sig;  // sizes of the loaded problem (see load)
   bool use_graphs = true;
   bool profile = false;  // per-phase cycle counters of the FP32 warp kernel
   void drop_graphs() {
@@ -597,7 +598,6 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   CK(cudaSetDevice(e->device));
   e->loaded = false;
   e->ran = false;
-  ++e->gen;
   e->tuned[0] = e->tuned[1] = KernelChoice();
   const int np = pb->nperiod, ns = pb->nsolve;
   e->nperiod = np;
@@ -741,6 +741,18 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   if (r) return (surfatt_status_t)r;
   r = run_prep_all(e);
   if (r) return (surfatt_status_t)r;
+  // Captured evaluations hold the problem's sizes: capture again only when
+  // they change (buffers that had to grow have moved `gen` already).
+  std::vector<long long> sig = {np, ns, pb->npath, nrec_total, e->ncell, e->kslot_total};
+  for (int p = 0; p < np; ++p) {
+    sig.push_back(e->nx[p]);
+    sig.push_back(e->ny[p]);
+    sig.push_back(e->goff[p]);
+  }
+  if (sig != e->shape_sig) {
+    ++e->gen;
+    e->shape_sig = sig;
+  }
   e->loaded = true;
   return SURFATT_OK;
 }
@@ -767,8 +779,7 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, const KernelChoice& fo
   LaunchPlan plan;
   int r = plan_evaluation(sh, prec, e->device, 0, &plan, force);
   if (r) return (surfatt_status_t)r;
-  r = eng_ensure(e, e->d_ws,
-                 (size_t)plan.grid * plan.slots_per_block * plan.ws_doubles * sizeof(double));
+  r = eng_ensure(e, e->d_ws, (size_t)plan_ws_doubles(plan, e->nsolve) * sizeof(double));
   if (r) return (surfatt_status_t)r;
   e->grid = plan.grid;
   e->per_sm = plan.per_sm;

@@ -69,6 +69,8 @@ struct BatchArgs {
   int smem_tau;            // FP32 kernel: 1 = tau / Ta in shared memory
   size_t smem_bytes;       // FP32 kernel: dynamic shared memory per block
   unsigned long long* phase_cycles = nullptr;  // optional: SM cycles per solve phase, summed
+  int items = 1;           // FP32 warp kernel: items per solve (1: whole solves)
+  int* sstate = nullptr;   // FP32 warp kernel with items > 1: per-solve state records
 };
 
 // Solve phases timed when BatchArgs::phase_cycles is set (FP32 warp kernel).
@@ -130,6 +132,11 @@ void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plis
 void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st);
 int batch_fp32w_max_blocks_per_sm(int bands, int variant);
 int fp32w_variant_count();
+// Whether a variant cuts solves into work items (one workspace slot per
+// solve), and the items per solve of an evaluation mode.
+bool fp32w_variant_items(int variant);
+int fp32w_items_for_mode(int mode);
+constexpr int kSolveStateInts = 5;
 // The same solve on the diagonal layouts (PeriodDev::qa / qd prepared), its
 // operands staged in shared memory; `variant` < fp32d_variant_count().
 void launch_batch_fp32d(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st);

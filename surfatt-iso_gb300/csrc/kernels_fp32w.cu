@@ -123,14 +123,17 @@ __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, i
 // only the values exchanged between lanes are, the cell's constants are
 // loaded at the visit (they stream along the lane's row and hit in L1),
 // which frees registers for more resident warps.
+// Iterations it0 .. it1 (1-based; the reference runs 1 .. MaxIter): status
+// ST_OK and the iteration count when one of them converges, otherwise
+// ST_NOT_CONVERGED and it1.
 template <int MB, int PF>
 __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w, int lane,
-                                    int* status_out, int* iters_out) {
+                                    int it0, int it1, int* status_out, int* iters_out) {
   const int nx = P.nx, ny = P.ny;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const int nsteps = nx + ny - 1;
   int iter, status = ST_NOT_CONVERGED;
-  for (iter = 1; iter <= MAXITER_UW; ++iter) {
+  for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f;
     for (int s = 0; s < 4; ++s) {
       int xdir, ydir;
@@ -207,7 +210,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
     }
   }
   *status_out = status;
-  *iters_out = iter > MAXITER_UW ? MAXITER_UW : iter;
+  *iters_out = iter > it1 ? it1 : iter;
 }
 
 // ---------------------------------------------------------------------------
@@ -398,29 +401,173 @@ __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, d
 }
 
 // ---------------------------------------------------------------------------
+// the tail of a solve
+// ---------------------------------------------------------------------------
+// Receiver times, misfit, outlier weights (src/measadj.f90:71-72, 82-84);
+// returns the status (ST_BAD_ARG for a receiver outside the grid).
+__device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const WSlot& V, int s,
+                                  int r0, int nr, int lane, int st) {
+  int bad = 0;
+  for (int r = lane; r < nr; r += 32) {
+    double v = 0.0;
+    if (!w_interp(P, V, A.recx[r0 + r], A.recy[r0 + r], &v)) bad = 1;
+    A.tekio[r0 + r] = v;
+    A.tt_fwd[A.path[r0 + r]] = v;
+  }
+  bad = __any_sync(FULL, bad);
+  __syncwarp();
+  if (lane == 0) {
+    double ssum = 0;
+    for (int r = 0; r < nr; ++r) {
+      const double d = A.tekio[r0 + r] - A.tt[r0 + r];
+      ssum = ssum + A.weight[r0 + r] * (d * d);
+    }
+    A.chi[s] = 0.5 * ssum;
+    for (int r = 0; r < nr; ++r) {
+      double wt = A.weight[r0 + r];
+      if (fabs(A.tekio[r0 + r] - A.tt[r0 + r]) / A.tt[r0 + r] > 0.5) wt = 0.;
+      A.wgt_eff[r0 + r] = wt;
+    }
+  }
+  __syncwarp();
+  return (bad && st == ST_OK) ? ST_BAD_ARG : st;
+}
+
+// Adjoint coefficients and the scaled sources of nf fields: weight*(tekio-tt)
+// (src/measadj.f90:88) and -weight (:102), splat bilinearly over the cell
+// area (src/eikon_solver_2d.f90:1328-1336) and scaled by 1/d.
+__device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, const WSlot& V,
+                                    int r0, int nr, int nf, int lane, int st) {
+  const int nx = P.nx, ny = P.ny;
+  const size_t N = (size_t)nx * ny;
+  w_adj_setup(P, V, lane);
+  for (int f = 0; f < nf; ++f)
+    for (size_t k = lane; k < N; k += 32) V.src[f][k] = 0.f;
+  __syncwarp();
+  if (lane == 0) {
+    for (int f = 0; f < nf && st != ST_BAD_ARG; ++f)
+      for (int r = 0; r < nr; ++r) {
+        const double wt = A.wgt_eff[r0 + r];
+        const double sv = f == 0 ? wt * (A.tekio[r0 + r] - A.tt[r0 + r]) : -1.0 * wt;
+        const double xr = A.recx[r0 + r] / 180.0 * PI_S, yr = A.recy[r0 + r] / 180.0 * PI_S;
+        float r1 = 0.f, r2 = 0.f;
+        const int i0 = locate_cell(P.xs, nx, P.dx, xr, &r1);
+        const int j0 = locate_cell(P.ys, ny, P.dy, yr, &r2);
+        if (i0 < 0 || j0 < 0) {
+          st = ST_BAD_ARG;
+          break;
+        }
+        const double den = P.dx * R_EARTH * cos(yr) * P.dy * R_EARTH;
+        const size_t k = i0 + (size_t)nx * j0;
+        float* sf = V.src[f];
+        sf[k] += (float)(sv * (double)(1 - r1) * (double)(1 - r2) / den) * V.id[k];
+        if (j0 + 1 < ny)
+          sf[k + nx] += (float)(sv * (double)(1 - r1) * (double)r2 / den) * V.id[k + nx];
+        if (i0 + 1 < nx)
+          sf[k + 1] += (float)(sv * (double)r1 * (double)(1 - r2) / den) * V.id[k + 1];
+        if (i0 + 1 < nx && j0 + 1 < ny)
+          sf[k + nx + 1] += (float)(sv * (double)r1 * (double)r2 / den) * V.id[k + nx + 1];
+      }
+  }
+  st = __shfl_sync(FULL, st, 0);
+  __syncwarp();
+  return st;
+}
+
+// Mask (src/eikon_solver_2d.f90:1449-1467) and the kernel slot adj/svel**k
+// (src/acqui.f90:314-315) of adjoint field f, FP32 here, summed per period
+// in FP64.
+__device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlot& V,
+                              const WSolve& w, int s, int f, int lane) {
+  const int nx = P.nx, ny = P.ny;
+  float* out = reinterpret_cast<float*>(f == 0 ? A.kcontrib : A.kcontrib_den) + A.kslot[s];
+  for (int j = 0; j < ny; ++j)
+    for (int i = lane; i < nx; i += 32) {
+      const size_t k = i + (size_t)nx * j;
+      const float4 pb = P.p4b[k];
+      const float isv = A.mode == 3 ? pb.w : pb.z;
+      out[k] = w.mbox.has(i, j) ? 0.f : V.tau[k] * isv;
+    }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
 // One warp per block; MINW resident warps per SM is the launch bound.  The
 // register file is split between the SM's four schedulers, so 8 warps (two
 // per scheduler) allow 255 registers a thread and 12 warps (three) 168.
+//
+// Work items.  With A.items == 1 a warp takes whole solves.  With A.items > 1
+// each solve is cut into consecutive items -- kFwdItems forward items of
+// kSplitIter iterations each (the first also computes T0, the last runs to
+// convergence and adds receivers, misfit, adjoint coefficients and
+// sources), then one item per adjoint field and its kernel slot -- each
+// solve has its own workspace slot and state record, and the queue hands out
+// every solve's item 0, then every item 1, and so on, so that the last round
+// of a batch is a short item rather than a whole solve.  An item waits
+// (bounded) for the previous item of its solve, which a resident warp took
+// earlier, so the waits cannot form a cycle.
+constexpr int kSplitIter = 2;
+constexpr int kFwdItems = 3;
+// Per-solve state record (ints): items done (-1: failed), forward
+// iterations, forward status, running status, adjoint iterations of field 0.
+enum { SS_DONE = 0, SS_FIT, SS_FST, SS_ST, SS_ITS0 };
+// Bounded wait for the previous item (polls, each followed by a short sleep).
+constexpr int kItemWaitLimit = 1 << 24;
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Items per solve for `mode` when solves are cut.
+__host__ __device__ inline int w_items_for_mode(int mode) {
+  return kFwdItems + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
+}
+
 template <int MB, int PF, int MINW>
 __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
   const int lane = threadIdx.x & 31;
-  const long long gw = blockIdx.x;
-  double* base = A.ws + gw * A.ws_doubles;
+  const bool cut = A.items > 1;
+  const int nitem = cut ? A.items : 1;
   float* kf = reinterpret_cast<float*>(A.kcontrib);
   float* kdf = reinterpret_cast<float*>(A.kcontrib_den);
   for (;;) {
     int q = 0;
     if (lane == 0) q = atomicAdd(A.queue, 1);
     q = __shfl_sync(FULL, q, 0);
-    if (q >= A.nsolve) break;
-    const int s = A.order[q];
+    if (q >= A.nsolve * nitem) break;
+    const int item = q / A.nsolve;
+    const int s = A.order[q % A.nsolve];
+    int* const ss = cut ? A.sstate + (size_t)kSolveStateInts * s : nullptr;
+    if (cut && item > 0) {
+      // the previous item of this solve (taken earlier by a resident warp)
+      int d = ld_acquire(ss + SS_DONE), it = 0;
+      while (d >= 0 && d < item && it < kItemWaitLimit) {
+        __nanosleep(128);
+        d = ld_acquire(ss + SS_DONE);
+        ++it;
+      }
+      if (d < 0) continue;  // the solve failed in an earlier item
+      if (d < item) {       // wait limit: report and drop the solve
+        if (lane == 0) {
+          A.status[s] = ST_TIMEOUT;
+          st_release(ss + SS_DONE, -1);
+        }
+        __syncwarp();
+        continue;
+      }
+    }
     const PeriodDev P = A.periods[A.pidx[s]];
     const int nx = P.nx, ny = P.ny;
     const size_t N = (size_t)nx * ny;
     const int r0 = A.rec_off[s], nr = A.nrec[s];
-    const WSlot V = wcarve(base, N);
+    const WSlot V = wcarve(A.ws + (cut ? (long long)s : (long long)blockIdx.x) * A.ws_doubles, N);
     const double xd0 = A.srcx[s], yd0 = A.srcy[s];
     const double x0 = xd0 / 180.0 * PI_S, y0 = yd0 / 180.0 * PI_S;
     unsigned long long* const pc = A.phase_cycles;
@@ -433,17 +580,44 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
         c0 = c1;
       }
     };
+    // this warp's writes of the item become visible, then the item is done
+    auto finish_item = [&](int done) {
+      if (cut) {
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(ss + SS_DONE, done);
+      }
+      __syncwarp();
+    };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
-    if (w.status != ST_OK) {
+    const int nf = A.mode == 3 ? 2 : 1;
+    const int nitems_mode = w_items_for_mode(A.mode);
+    const int first = cut ? item : 0;                 // first item done here
+    const int lastit = cut ? item : nitems_mode - 1;  // last item done here
+    int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0;
+    if (cut && first > 0) {
+      int v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+      if (lane == 0) {
+        v0 = ss[SS_FIT];
+        v1 = ss[SS_FST];
+        v2 = ss[SS_ST];
+        v3 = ss[SS_ITS0];
+      }
+      fit = __shfl_sync(FULL, v0, 0);
+      fst = __shfl_sync(FULL, v1, 0);
+      st = __shfl_sync(FULL, v2, 0);
+      its0 = __shfl_sync(FULL, v3, 0);
+    }
+    if (first == 0 && w.status != ST_OK) {
       for (int r = lane; r < nr; r += 32) {
         A.tekio[r0 + r] = 0.0;
         A.wgt_eff[r0 + r] = 0.0;
         A.tt_fwd[A.path[r0 + r]] = 0.0;
       }
       if (A.mode >= 2)
-        for (size_t k = lane; k < N; k += 32) {
-          kf[A.kslot[s] + k] = 0.f;
-          if (A.mode == 3) kdf[A.kslot[s] + k] = 0.f;
+        for (size_t kk = lane; kk < N; kk += 32) {
+          kf[A.kslot[s] + kk] = 0.f;
+          if (A.mode == 3) kdf[A.kslot[s] + kk] = 0.f;
         }
       if (lane == 0) {
         A.chi[s] = 0.0;
@@ -452,118 +626,96 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
         A.adj_iters[s] = 0;
         if (A.fwd_updates) A.fwd_updates[s] = 0;
       }
-      __syncwarp();
+      finish_item(-1);
       continue;
     }
-    w_t0(P, x0, y0, w, V, lane);
-    mark(PH_SETUP);
-    int fst = ST_OK, fit = 0;
-    w_fwd_sweeps<MB, PF>(P, V, w, lane, &fst, &fit);
-    mark(PH_FWD);
-    if (A.fwd_updates && lane == 0) {
-      const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
-      A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
+    // forward sweeps: forward item k runs iterations k*kSplitIter+1 ..
+    // (k+1)*kSplitIter, the last one (a whole solve: all) up to MaxIter,
+    // unless an earlier item converged
+    if (first == 0) {
+      w_t0(P, x0, y0, w, V, lane);
+      mark(PH_SETUP);
     }
-    // receiver times, misfit, outlier weights (src/measadj.f90:71-72, 82-84)
-    int bad = 0;
-    for (int r = lane; r < nr; r += 32) {
-      double v = 0.0;
-      if (!w_interp(P, V, A.recx[r0 + r], A.recy[r0 + r], &v)) bad = 1;
-      A.tekio[r0 + r] = v;
-      A.tt_fwd[A.path[r0 + r]] = v;
+    if (first < kFwdItems && (first == 0 || (fst != ST_OK && fit < MAXITER_UW))) {
+      const int it0 = first == 0 ? 1 : fit + 1;
+      const int it1 = (cut && first < kFwdItems - 1) ? (first + 1) * kSplitIter : MAXITER_UW;
+      int n = 0;
+      w_fwd_sweeps<MB, PF>(P, V, w, lane, it0, it1, &fst, &n);
+      fit = n;
+      mark(PH_FWD);
     }
-    bad = __any_sync(FULL, bad);
-    __syncwarp();
-    if (lane == 0) {
-      double ssum = 0;
-      for (int r = 0; r < nr; ++r) {
-        const double d = A.tekio[r0 + r] - A.tt[r0 + r];
-        ssum = ssum + A.weight[r0 + r] * (d * d);
-      }
-      A.chi[s] = 0.5 * ssum;
-      for (int r = 0; r < nr; ++r) {
-        double wt = A.weight[r0 + r];
-        if (fabs(A.tekio[r0 + r] - A.tt[r0 + r]) / A.tt[r0 + r] > 0.5) wt = 0.;
-        A.wgt_eff[r0 + r] = wt;
-      }
-    }
-    __syncwarp();
-    mark(PH_RECV);
-    int st = fst;
-    if (bad && st == ST_OK) st = ST_BAD_ARG;
-    int aiters = 0;
-    if (A.mode >= 2) {
-      const int nf = A.mode == 3 ? 2 : 1;
-      w_adj_setup(P, V, lane);
-      for (int f = 0; f < nf; ++f)
-        for (size_t k = lane; k < N; k += 32) V.src[f][k] = 0.f;
-      __syncwarp();
+    if (cut && first < kFwdItems - 1) {
       if (lane == 0) {
-        // adjoint sources weight*(tekio-tt) (src/measadj.f90:88) and -weight
-        // (:102), bilinear splat over the cell area (:1328-1336), scaled by 1/d
-        for (int f = 0; f < nf && st != ST_BAD_ARG; ++f)
-          for (int r = 0; r < nr; ++r) {
-            const double wt = A.wgt_eff[r0 + r];
-            const double sv = f == 0 ? wt * (A.tekio[r0 + r] - A.tt[r0 + r]) : -1.0 * wt;
-            const double xr = A.recx[r0 + r] / 180.0 * PI_S, yr = A.recy[r0 + r] / 180.0 * PI_S;
-            float r1 = 0.f, r2 = 0.f;
-            const int i0 = locate_cell(P.xs, nx, P.dx, xr, &r1);
-            const int j0 = locate_cell(P.ys, ny, P.dy, yr, &r2);
-            if (i0 < 0 || j0 < 0) { st = ST_BAD_ARG; break; }
-            const double den = P.dx * R_EARTH * cos(yr) * P.dy * R_EARTH;
-            const size_t k = i0 + (size_t)nx * j0;
-            float* sf = V.src[f];
-            sf[k] += (float)(sv * (double)(1 - r1) * (double)(1 - r2) / den) * V.id[k];
-            if (j0 + 1 < ny) sf[k + nx] += (float)(sv * (double)(1 - r1) * (double)r2 / den) * V.id[k + nx];
-            if (i0 + 1 < nx) sf[k + 1] += (float)(sv * (double)r1 * (double)(1 - r2) / den) * V.id[k + 1];
-            if (i0 + 1 < nx && j0 + 1 < ny)
-              sf[k + nx + 1] += (float)(sv * (double)r1 * (double)r2 / den) * V.id[k + nx + 1];
-          }
+        ss[SS_FIT] = fit;
+        ss[SS_FST] = fst;
       }
-      st = __shfl_sync(FULL, st, 0);
-      __syncwarp();
-      mark(PH_ADJ_SETUP);
-      int its[2] = {0, 0};
-      for (int f = 0; f < nf; ++f) {
-        int ast = ST_OK;
-        w_adj_sweeps<MB, PF>(P, V, V.src[f], lane, &ast, &its[f]);
-        mark(PH_ADJ);
-        if (ast != ST_OK && st == ST_OK) st = ast;
-        // mask (:1449-1467) and the slot adj/svel**k (:314-315), FP32 here,
-        // summed per period in FP64
-        float* out = (f == 0 ? kf : kdf) + A.kslot[s];
-        for (int j = 0; j < ny; ++j)
-          for (int i = lane; i < nx; i += 32) {
-            const size_t k = i + (size_t)nx * j;
-            const float4 pb = P.p4b[k];
-            const float isv = A.mode == 3 ? pb.w : pb.z;
-            out[k] = w.mbox.has(i, j) ? 0.f : V.tau[k] * isv;
-          }
-        __syncwarp();
-        mark(PH_SLOT);
-      }
-      aiters = its[0] > its[1] ? its[0] : its[1];
-      if (A.adj_updates && lane == 0)
-        A.adj_updates[s] = (double)(its[0] + its[1]) * 4.0 * (nx - 2) * (ny - 2);
+      finish_item(first + 1);
+      continue;
     }
+    if (first <= kFwdItems - 1) {
+      if (A.fwd_updates && lane == 0) {
+        const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
+        A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
+      }
+      st = w_receivers(A, P, V, s, r0, nr, lane, fst);
+      mark(PH_RECV);
+      if (A.mode >= 2) {
+        st = w_adj_sources(A, P, V, r0, nr, nf, lane, st);
+        mark(PH_ADJ_SETUP);
+      }
+      if (cut && A.mode >= 2) {
+        if (lane == 0) {
+          ss[SS_FIT] = fit;
+          ss[SS_ST] = st;
+        }
+        finish_item(kFwdItems);
+        continue;
+      }
+    }
+    // adjoint field(s) f0 .. f1
+    const int f0 = cut ? (first > kFwdItems ? first - kFwdItems : 0) : 0;
+    const int f1 = A.mode >= 2 ? (cut ? lastit - kFwdItems : nf - 1) : -1;
+    for (int f = f0; f <= f1; ++f) {
+      int ast = ST_OK, n = 0;
+      w_adj_sweeps<MB, PF>(P, V, f ? V.src[1] : V.src[0], lane, &ast, &n);
+      mark(PH_ADJ);
+      if (f == 0) its0 = n; else its1 = n;
+      if (ast != ST_OK && st == ST_OK) st = ast;
+      w_slot(A, P, V, w, s, f, lane);
+      mark(PH_SLOT);
+    }
+    if (cut && lastit < nitems_mode - 1) {
+      if (lane == 0) {
+        ss[SS_ST] = st;
+        ss[SS_ITS0] = its0;
+      }
+      finish_item(lastit + 1);
+      continue;
+    }
+    // the solve's last item: its outputs
     if (lane == 0) {
       A.status[s] = st;
       A.fwd_iters[s] = fit;
-      A.adj_iters[s] = aiters;
+      A.adj_iters[s] = its0 > its1 ? its0 : its1;
+      if (A.adj_updates && A.mode >= 2)
+        A.adj_updates[s] = (double)(its0 + its1) * 4.0 * (nx - 2) * (ny - 2);
     }
-    __syncwarp();
+    finish_item(nitems_mode);
   }
 }
 
 int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 
-// Variants of the warp kernel: operand prefetch and resident warps per SM.
-//   0: constants loaded at the visit, 12 warps per SM (168 registers)
-//   1: every operand loaded a step ahead, 8 warps per SM (255 registers)
-//   2: every operand loaded a step ahead, 12 warps per SM (168, some spills)
-//   3: constants loaded at the visit, 8 warps per SM
+// Variants of the warp kernel: operand loads, resident warps per SM, whole
+// solves or solves cut into items.
+//   0: every operand loaded a step ahead into registers, 8 warps per SM, items
+//   1: the same, whole solves
+//   2: cell constants loaded at the visit, 12 warps per SM, items
+//   3: cell constants loaded at the visit, 8 warps per SM, whole solves
 constexpr int kFp32wVariants = 4;
 int fp32w_variant_count() { return kFp32wVariants; }
+bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2; }
+int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
 
 template <int MB, int PF, int MINW>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
@@ -580,9 +732,9 @@ static int occupancy_w() {
 template <int MB>
 static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st) {
   switch (variant) {
-    case 0: launch_w<MB, 0, 12>(a, grid, st); break;
+    case 0:
     case 1: launch_w<MB, 1, 8>(a, grid, st); break;
-    case 2: launch_w<MB, 1, 12>(a, grid, st); break;
+    case 2: launch_w<MB, 0, 12>(a, grid, st); break;
     default: launch_w<MB, 0, 8>(a, grid, st); break;
   }
 }
@@ -590,9 +742,9 @@ static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st
 template <int MB>
 static int occupancy_mb(int variant) {
   switch (variant) {
-    case 0: return occupancy_w<MB, 0, 12>();
+    case 0:
     case 1: return occupancy_w<MB, 1, 8>();
-    case 2: return occupancy_w<MB, 1, 12>();
+    case 2: return occupancy_w<MB, 0, 12>();
     default: return occupancy_w<MB, 0, 8>();
   }
 }

@@ -57,15 +57,17 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
   } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= kWarpMaxRows &&
              sh.max_nx <= kWarpMaxCols) {
     // one warp per solve, lanes own the rows
-    p.kind = force.kind == KK_FP32_WARP ? KK_FP32_WARP : KK_FP32_DIAG;
+    // automatic: the row-per-lane kernel (the faster on the measured shapes)
+    p.kind = force.kind == KK_FP32_DIAG ? KK_FP32_DIAG : KK_FP32_WARP;
     p.block = 32;
     p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
     const int nvar = p.kind == KK_FP32_WARP ? fp32w_variant_count() : fp32d_variant_count();
-    p.pf = force.variant >= 0 && force.variant < nvar ? force.variant : (p.kind == KK_FP32_WARP ? 1 : 0);
+    p.pf = force.variant >= 0 && force.variant < nvar ? force.variant : 0;
     if (p.kind == KK_FP32_WARP) {
       p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
       p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
+      p.cut = fp32w_variant_items(p.pf);
     } else {
       p.per_sm = batch_fp32d_max_blocks_per_sm(p.bands, p.pf);
       p.ws_doubles = batch_fp32d_ws_doubles(sh.max_dcells, sh.max_nx);
@@ -83,10 +85,18 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
   if (p.per_sm < 1) p.per_sm = 1;
   p.grid = nsm * p.per_sm;
   if (max_grid > 0) p.grid = std::min(p.grid, max_grid);
-  const int need = (std::max(1, sh.nsolve) + p.slots_per_block - 1) / p.slots_per_block;
+  const int units = std::max(1, sh.nsolve) * (p.cut ? fp32w_items_for_mode(3) : 1);
+  const int need = (units + p.slots_per_block - 1) / p.slots_per_block;
   p.grid = std::max(1, std::min(p.grid, need));
   *plan = p;
   return ST_OK;
+}
+
+long long plan_ws_doubles(const LaunchPlan& plan, int nsolve) {
+  const long long n = std::max(1, nsolve);
+  const long long slots = plan.cut ? n : (long long)plan.grid * plan.slots_per_block;
+  const long long state = plan.cut ? (n * kSolveStateInts + 1) / 2 : 0;
+  return slots * plan.ws_doubles + state;
 }
 
 int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan& plan, int mode,
@@ -101,6 +111,15 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   A.max_nx = sh.max_nx;
   A.smem_tau = plan.smem_tau;
   A.smem_bytes = plan.smem;
+  A.items = 1;
+  A.sstate = nullptr;
+  if (plan.kind == KK_FP32_WARP && plan.cut) {
+    const long long n = std::max(1, sh.nsolve);
+    A.items = fp32w_items_for_mode(mode);
+    A.sstate = reinterpret_cast<int*>(ws + n * plan.ws_doubles);
+    if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
+      return -ST_CUDA_ERROR;
+  }
   int launches = 0;
   if (cudaMemsetAsync(queue, 0, sizeof(int), st) != cudaSuccess) return -ST_CUDA_ERROR;
   if (A.phase_cycles &&

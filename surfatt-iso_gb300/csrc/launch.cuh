@@ -49,6 +49,7 @@ struct LaunchPlan {
   int kind = KK_FP64;
   int grid = 0, block = 0, per_sm = 0, smem_tau = 0, bands = 0, pf = 1;
   int slots_per_block = 1;   // solves resident per block (warps for KK_FP32_WARP)
+  bool cut = false;          // solves cut into work items: one workspace slot per solve
   size_t smem = 0;
   long long ws_doubles = 0;  // per resident solve
 };
@@ -60,6 +61,10 @@ struct LaunchPlan {
 // candidates.
 int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, LaunchPlan* plan,
                     const KernelChoice& force = KernelChoice());
+
+// Doubles of workspace an evaluation of `nsolve` solves needs under `plan`
+// (slots, then the per-solve state records of a cut evaluation).
+long long plan_ws_doubles(const LaunchPlan& plan, int nsolve);
 
 // Kernel variants the autotuner times for an evaluation of this shape.
 std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec);

@@ -294,7 +294,12 @@ int start_request(surfatt_server* S, Request& r) {
   Model& M = *S->models[L.model];
   const bool own_vel = !r.svel.empty();
   r.shape.from_grids(M.nx.data(), M.ny.data(), M.goff.data(), M.nperiod, L.nsolve, L.npath);
-  int e = plan_evaluation(r.shape, r.prec, S->device, 0, &r.plan);
+  // Whole solves per warp: requests run side by side and share the SMs, so
+  // the short last round that cut solves buy a single evaluation is not
+  // what limits a request here.
+  KernelChoice choice;
+  choice.variant = 1;
+  int e = plan_evaluation(r.shape, r.prec, S->device, 0, &r.plan, choice);
   if (e) return e;
   auto layout = [&](Carver& cv) {
     if (own_vel) carve_periods(cv, M.nxs, M.nys, M.ncell, M.nperiod, M.qcells, &r.d);
@@ -314,7 +319,7 @@ int start_request(surfatt_server* S, Request& r) {
     r.fit = cv.take<int>(ns);
     r.ait = cv.take<int>(ns);
     r.queue = cv.take<int>(1);
-    r.ws = cv.take<double>((size_t)r.plan.grid * r.plan.slots_per_block * r.plan.ws_doubles);
+    r.ws = cv.take<double>((size_t)plan_ws_doubles(r.plan, L.nsolve));
   };
   Carver sizer;
   layout(sizer);

@@ -62,3 +62,24 @@ def test_reload_recaptures(sg):
     assert len(outs[0]["tt_fwd"]) == a.npath and len(outs[2]["tt_fwd"]) == b.npath
     eng.close()
     ref.close()
+
+
+def test_reload_same_shape_reuses_capture(sg):
+    """A load of a problem with the same sizes keeps the captured graph (its
+    sizes and buffers are unchanged); the replay computes the new problem."""
+    a = W.flat_case(nx=72, ny=66, nsta=5, nperiod=2, mode=3, seed=24)
+    b = W.flat_case(nx=72, ny=66, nsta=5, nperiod=2, mode=3, seed=25, vel=3.3)
+    assert a.nsolve == b.nsolve and a.npath == b.npath
+    eng = sg.Engine(0)
+    eng.load(a)
+    first = _run(eng, 3, sg.PREC_FP32)
+    eng.load(b)
+    replay = _run(eng, 3, sg.PREC_FP32)
+    ref = sg.Engine(0)
+    ref.set_graphs(False)
+    ref.load(b)
+    direct = _run(ref, 3, sg.PREC_FP32)
+    assert _same(replay, direct)
+    assert not np.array_equal(first["tt_fwd"], replay["tt_fwd"])
+    eng.close()
+    ref.close()
