@@ -38,7 +38,28 @@ sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
 FWD_FLOPS_PER_VISIT = 351.8
 ADJ_FLOPS_PER_VISIT = 16.0
 KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w", 3: "k_batch_fp32d"}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# FP32 solve kernel, from one ncu capture of the 320-solve case (1.955 GB),
+# scaled by the solves for the 1280-solve workload (the per-solve workspace
+# and operands are the same for every solve): profiles/k_batch_fp32w_config2s.md.
+DRAM_BYTES_PER_LAUNCH = {"config2": 7.82e9, "config2s": 1.955e9}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
+
+
+def _hbm_view(traffic, kernel_ms):
+    """The same launch against the HBM roof: its DRAM bytes (ncu) per
+    CUDA-event second, over the measured copy bandwidth of this machine."""
+    if not traffic:
+        return None
+    peak = None
+    try:
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        source = "MEASURED_PEAKS.json hbm_gbs (measured)"
+    except (OSError, ValueError, KeyError):
+        peak, source = 6800.0, "fallback 6.8 TB/s"
+    achieved = traffic / (kernel_ms * 1e-3) / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": source}
 
 
 def _args():
@@ -312,13 +333,16 @@ def run_ours(args):
     k64_ms = statistics.mean(k64)
     ach32 = flops32 / (k32_ms * 1e-3) / 1e12
     ach64 = flops64 / (k64_ms * 1e-3) / 1e12
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get(args.workload, {}).get("fp32")
-        except (OSError, ValueError):
-            traffic = None
+    traffic = DRAM_BYTES_PER_LAUNCH.get(args.workload)
+
+    # where the solve kernel's time goes: one more evaluation with the
+    # per-phase SM cycle counters on (outside the timed region)
+    eng.set_profile(True)
+    eng.run(pb.mode, sg.PREC_FP32)
+    eng.sync()
+    ph = eng.phase_cycles()
+    eng.set_profile(False)
+    phases = {k: v / max(pb.nsolve, 1) / 1e6 for k, v in ph.items()}
 
     cpu = None
     parity = {}
@@ -362,8 +386,10 @@ def run_ours(args):
                          "peak_source": "surfatt_measure_peaks (FP32 FMA chains), this run",
                          "kernel": KERNEL_NAMES.get(launch32.get("kind"), "k_batch_fp32"),
                          "kernel_ms": k32_ms,
-                         "flops_per_launch": flops32},
+                         "flops_per_launch": flops32,
+                         "hbm_view": _hbm_view(traffic, k32_ms)},
             "cpu_baseline": cpu, "parity": parity,
+            "phase_mcycles_per_solve": phases,
             "launch": {"fp32": launch32, "fp64": launch64, "autotune": tuned},
             "iterations": {"fwd_mean": float(np.mean(r32["fwd_iters"])),
                            "adj_mean": float(np.mean(r32["adj_iters"]))},
