@@ -467,7 +467,7 @@ __device__ inline void d_adj_setup(const PeriodDev& P, const DGeom& g, const DSl
       }
       // node (i + di, j + dj) of family 0
       auto at = [&](int di, int dj) { return k + (di + dj) * pitch + dj; };
-      auto T = [&](int q) { return tau[q] * T0[q]; };
+      auto T = [&](int q) { return __fmul_rn(tau[q], T0[q]); };
       const int w = at(-1, 0), e = at(1, 0), s = at(0, -1), n = at(0, 1);
       const float4 pk = PA[k], pw = PA[w], pe = PA[e], ps = PA[s], pn = PA[n];
       const float Tk = T(k), Tw = T(w), Te = T(e), Ts = T(s), Tn = T(n);

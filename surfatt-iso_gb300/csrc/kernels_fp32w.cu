@@ -223,7 +223,8 @@ __device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, int lane)
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const float* T0 = reinterpret_cast<const float*>(V.S);
   const float4* PA = P.p4a;
-  auto T = [&](size_t k) { return V.tau[k] * T0[4 * k]; };
+  // T = tau*T0 rounded on its own (no contraction with the differences below)
+  auto T = [&](size_t k) { return __fmul_rn(V.tau[k], T0[4 * k]); };
   for (int j = 0; j < ny; ++j) {
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
@@ -481,12 +482,28 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlo
                               const WSolve& w, int s, int f, int lane) {
   const int nx = P.nx, ny = P.ny;
   float* out = reinterpret_cast<float*>(f == 0 ? A.kcontrib : A.kcontrib_den) + A.kslot[s];
+  // groups of G cells: loads first, then stores (as in w_adj_setup)
+  constexpr int G = 4;
   for (int j = 0; j < ny; ++j)
-    for (int i = lane; i < nx; i += 32) {
-      const size_t k = i + (size_t)nx * j;
-      const float4 pb = P.p4b[k];
-      const float isv = A.mode == 3 ? pb.w : pb.z;
-      out[k] = w.mbox.has(i, j) ? 0.f : V.tau[k] * isv;
+    for (int i0 = lane; i0 < nx; i0 += 32 * G) {
+      float isv[G], ta[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int i = i0 + 32 * g;
+        isv[g] = 0.f;
+        ta[g] = 0.f;
+        if (i < nx) {
+          const size_t k = i + (size_t)nx * j;
+          const float4 pb = P.p4b[k];
+          isv[g] = A.mode == 3 ? pb.w : pb.z;
+          ta[g] = V.tau[k];
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int i = i0 + 32 * g;
+        if (i < nx) out[i + (size_t)nx * j] = w.mbox.has(i, j) ? 0.f : ta[g] * isv[g];
+      }
     }
   __syncwarp();
 }
