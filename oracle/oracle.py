@@ -129,6 +129,18 @@ def interp2(x, y, v, xq, yq):
     return out.value
 
 
+def gaussian_smooth_geo_2(data, lons, lats, sigma):
+    """gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225) of one (nx, ny)
+    field; lons / lats in degrees, sigma in degrees.  Returns (nx, ny)."""
+    lons, lats = _f64(lons), _f64(lats)
+    d = _fortran2d(data)
+    nx, ny = d.shape
+    out = np.zeros((nx, ny), order="F")
+    lib().orc_gaussian_smooth_geo_2(_d(d), nx, ny, _d(lons), _d(lats), ctypes.c_double(sigma),
+                                    _d(out))
+    return out
+
+
 class _Problem(ctypes.Structure):
     _fields_ = [("nperiod", ctypes.c_int), ("nx", _ip), ("ny", _ip), ("xoff", _llp),
                 ("yoff", _llp), ("goff", _llp), ("xgrid", _dp), ("ygrid", _dp),

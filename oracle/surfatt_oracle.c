@@ -901,3 +901,52 @@ void orc_flop_counts(long long* out5) {
   cnt_visit = cnt_two = cnt_delta = cnt_one = cnt_adj = 0;
 }
 #endif
+
+/* ---------------------------------------------------------------------------
+ * gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225), the per-period 2-D
+ * kernel smoothing of tomo2d's optimize step (src/tomo2d.f90:221), with
+ * gps2dist_2 (utils.f90:1280-1294) and the constants of
+ * src/shared/shared_par.f90:11-15 (pi is a single-precision literal there:
+ * 3.14159265359 rounded to REAL(4), then widened).  data, out: (nx, ny),
+ * x fastest; lons (nx), lats (ny) in degrees, uniformly spaced; sigma in
+ * degrees.  The window half-widths are the reference's integer truncations
+ * nx_w = sigma3/dx and ny_w = sigma3/cosd(lat_j)/dy; cosd is evaluated as
+ * cos(lat * pi/180) with the double-precision pi.  Both sums run over the
+ * window in column order (i fastest), as SUM over data(m1:m2, n1:n2).
+ * ------------------------------------------------------------------------- */
+static double orc_gps2dist(double lat0, double lon0, double lat1, double lon1) {
+  const double pi = (double)3.14159265359f;
+  const double deg2rad = pi / 180.0;
+  const double radius = 6371.0;
+  const double dlat = (lat0 - lat1) * deg2rad;
+  const double dlon = (lon1 - lon0) * deg2rad;
+  const double s1 = sin(dlat * 0.5), s2 = sin(dlon * 0.5);
+  const double a = s1 * s1 + s2 * s2 * cos(lat0 * deg2rad) * cos(lat1 * deg2rad);
+  const double deg = 2.0 * atan2(sqrt(a), sqrt(1.0 - a));
+  return radius * deg;
+}
+
+void orc_gaussian_smooth_geo_2(const double* data, int nx, int ny, const double* lons,
+                               const double* lats, double sigma, double* out) {
+  const double pi = (double)3.14159265359f;
+  const double km2deg = 1.0 / (6371.0 * pi / 180.0);
+  const double sigma3 = sigma * 3.0, sigma_sq = sigma * sigma;
+  const double dx = lons[1] - lons[0], dy = lats[1] - lats[0];
+  const int nxw = (int)(sigma3 / dx);
+  for (int j = 0; j < ny; ++j) {
+    const int nyw = (int)(sigma3 / cos(lats[j] * (3.14159265358979323846 / 180.0)) / dy);
+    for (int i = 0; i < nx; ++i) {
+      const int m1 = i - nxw > 0 ? i - nxw : 0, m2 = i + nxw < nx - 1 ? i + nxw : nx - 1;
+      const int n1 = j - nyw > 0 ? j - nyw : 0, n2 = j + nyw < ny - 1 ? j + nyw : ny - 1;
+      double swd = 0.0, sw = 0.0;
+      for (int j1 = n1; j1 <= n2; ++j1)
+        for (int i1 = m1; i1 <= m2; ++i1) {
+          const double delta = orc_gps2dist(lats[j], lons[i], lats[j1], lons[i1]) * km2deg;
+          const double w = exp(-(delta * delta) / (2.0 * sigma_sq));
+          swd = swd + w * data[i1 + (size_t)nx * j1];
+          sw = sw + w;
+        }
+      out[i + (size_t)nx * j] = (0.0 + swd) / sw;
+    }
+  }
+}

@@ -151,6 +151,11 @@ int orc_gradient_eval_range(const orc_problem* pb, int mode, int nthreads, int s
 /* scatter_all_i (src/shared/parallel.f90:1877-1903), 1-based istart/iend */
 void orc_scatter_all_i(int countval, int size, int rank, int* istart, int* iend);
 
+/* gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225) of one (nx, ny)
+ * field, x fastest; lons / lats in degrees (uniform), sigma in degrees. */
+void orc_gaussian_smooth_geo_2(const double* data, int nx, int ny, const double* lons,
+                               const double* lats, double sigma, double* out);
+
 #ifdef __cplusplus
 }
 #endif

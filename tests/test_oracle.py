@@ -152,3 +152,68 @@ def test_weno3_homogeneous(oracle):
     X, Y = np.meshgrid(xx, yy, indexing="ij")
     ref = np.hypot(X - 1.73, Y - 1.41) / 2.0
     assert rel_pointwise(T, ref) <= 1e-6
+
+
+# ---------------------------------------------------------------------------
+# gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225)
+# ---------------------------------------------------------------------------
+_PI_S = float(np.float32(3.14159265359))  # shared_par.f90 pi: a REAL(4) literal
+
+
+def _smooth_numpy(data, lons, lats, sigma):
+    """Second restatement of gaussian_smooth_geo_2, written as the reference's
+    array expression: per cell, meshgrid of the clamped window, gps2dist_2
+    (utils.f90:1280-1294), w = exp(-delta^2/(2 sigma^2)), sum(w*data)/sum(w)."""
+    nx, ny = data.shape
+    deg2rad = _PI_S / 180.0
+    km2deg = 1.0 / (6371.0 * _PI_S / 180.0)
+    sigma3, sigma_sq = sigma * 3, sigma ** 2
+    dx, dy = lons[1] - lons[0], lats[1] - lats[0]
+    nxw = int(sigma3 / dx)
+    out = np.zeros_like(data)
+    for j in range(ny):
+        nyw = int(sigma3 / math.cos(lats[j] * (math.pi / 180.0)) / dy)
+        for i in range(nx):
+            m1, m2 = max(0, i - nxw), min(nx - 1, i + nxw)
+            n1, n2 = max(0, j - nyw), min(ny - 1, j + nyw)
+            lolo, lala = np.meshgrid(lons[m1:m2 + 1], lats[n1:n2 + 1], indexing="ij")
+            dlat = (lats[j] - lala) * deg2rad
+            dlon = (lolo - lons[i]) * deg2rad
+            a = np.sin(dlat * 0.5) ** 2 + np.sin(dlon * 0.5) ** 2 * np.cos(lats[j] * deg2rad) * \
+                np.cos(lala * deg2rad)
+            delta = 6371.0 * (2.0 * np.arctan2(np.sqrt(a), np.sqrt(1.0 - a))) * km2deg
+            w = np.exp(-delta ** 2 / (2.0 * sigma_sq))
+            out[i, j] = np.sum(w * data[m1:m2 + 1, n1:n2 + 1]) / np.sum(w)
+    return out
+
+
+def _smooth_grid(nx, ny, x0=100.0, y0=30.0, d=0.05):
+    return x0 + d * np.arange(nx), y0 + d * np.arange(ny)
+
+
+def test_smooth_matches_array_restatement(oracle):
+    lons, lats = _smooth_grid(23, 19)
+    rng = np.random.default_rng(5)
+    data = rng.standard_normal((23, 19))
+    got = oracle.gaussian_smooth_geo_2(data, lons, lats, 0.12)
+    ref = _smooth_numpy(data, lons, lats, 0.12)
+    assert rel_max(got, ref) <= 1e-13
+
+
+def test_smooth_constant_field(oracle):
+    lons, lats = _smooth_grid(31, 27, y0=-10.0, d=0.02)
+    got = oracle.gaussian_smooth_geo_2(np.full((31, 27), 2.5), lons, lats, 0.07)
+    assert np.max(np.abs(got - 2.5)) <= 1e-13
+
+
+def test_smooth_window_truncation(oracle):
+    """The x half-width is the integer truncation of 3 sigma / dx: a spike at
+    column c reaches exactly the columns |i - c| <= int(3 sigma / dx)."""
+    lons, lats = _smooth_grid(41, 9, d=0.05)
+    sigma = 0.1
+    nxw = int(sigma * 3 / (lons[1] - lons[0]))
+    spike = np.zeros((41, 9))
+    spike[20, 4] = 1.0
+    got = oracle.gaussian_smooth_geo_2(spike, lons, lats, sigma)
+    cols = np.nonzero(got[:, 4])[0]
+    assert cols.min() == 20 - nxw and cols.max() == 20 + nxw
