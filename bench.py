@@ -69,11 +69,13 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=["config1", "config2", "config2s", "config4", "serving"])
+                    choices=["config1", "config2", "config2s", "config4", "serving", "smooth"])
     ap.add_argument("--requests", type=int, default=40,
                     help="serving: requests in the Poisson stream")
     ap.add_argument("--load", type=float, default=0.7,
                     help="serving: offered load as a fraction of the closed-loop capacity")
+    ap.add_argument("--sigma", type=float, default=0.2,
+                    help="smooth: smoothing length in degrees (the example's sigma_2d)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -411,6 +413,8 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
+    if args.workload == "smooth":
+        return _run_reference_smooth(args, O, dist)
     pb, desc = _workload(args.workload)
     nthr = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -434,6 +438,45 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0},
             "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
                     "is timed through the C restatement in oracle/ on all host threads"}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _run_reference_smooth(args, O, dist):
+    """Reference arm of the smoothing workload: the oracle's
+    gaussian_smooth_geo_2 of every period's adj_s, periods spread over
+    worker processes as the reference spreads them over MPI ranks."""
+    import multiprocessing as mp
+    from surfatt_gb300 import workloads as W
+    nthr = min(os.cpu_count() or 1, 16)
+    pool = mp.get_context("spawn").Pool(nthr)
+    pb = W.config2(mode=2)
+    adj = O.gradient_eval(pb, mode=2, nthreads=os.cpu_count() or 1)["adj_s"]
+    jobs = [(f, *_period_axes(pb, p), args.sigma) for p, f in enumerate(_period_views(pb, adj))]
+    ts = []
+    for i in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        pool.map(_oracle_smooth_one, jobs)
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - a)
+    pool.close()
+    pool.join()
+    s = statistics.mean(ts)
+    v = pb.nperiod / s
+    line = {"impl": "reference",
+            "metric": "kernel smoothing periods/s (gaussian_smooth_geo_2 of every period's adj_s)",
+            "value": v, "unit": "periods/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tomo2d kernel smoothing on config 2's grids: 16 periods, "
+                                   "120x120 at 0.05 deg", "sigma_deg": args.sigma},
+            "cpu_baseline": {"value": v, "unit": "periods/s", "cores": nthr, "kind": "port",
+                             "sample": f"all {pb.nperiod} periods per step, one per process"},
+            "e2e": {"value": v, "unit": "periods/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
+                    "is timed through the C restatement in oracle/"}
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -499,11 +542,155 @@ def run_serving(args):
         dist.destroy_process_group()
 
 
+def _oracle_smooth_one(job):
+    """One period of the oracle's gaussian_smooth_geo_2 (a pool worker)."""
+    if os.path.join(ROOT, "oracle") not in sys.path:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    data, lons, lats, sigma = job
+    return O.gaussian_smooth_geo_2(data, lons, lats, sigma)
+
+
+def _period_views(pb, a):
+    out = []
+    for p in range(pb.nperiod):
+        nx, ny, g = int(pb.nx[p]), int(pb.ny[p]), int(pb.goff[p])
+        out.append(a[g:g + nx * ny].reshape((nx, ny), order="F"))
+    return out
+
+
+def _period_axes(pb, p):
+    return (pb.xgrid[pb.xoff[p]:pb.xoff[p] + pb.nx[p]],
+            pb.ygrid[pb.yoff[p]:pb.yoff[p] + pb.ny[p]])
+
+
+def run_smooth(args):
+    """Kernel smoothing of tomo2d's optimize step (gaussian_smooth_geo_2 of
+    every period's adj_s, src/tomo2d.f90:216-222) on config 2's grids:
+    16 periods of 120x120 at 0.05 deg, sigma 0.2 deg.  value: periods/s from
+    the device time of the engine's two smoothing kernels on the resident
+    adj_s; e2e: the drop-in call per period with host buffers."""
+    import multiprocessing as mp
+    import torch
+    import surfatt_gb300 as sg
+    from surfatt_gb300 import workloads as W
+    dist, rank, world, local = _dist()
+    # the oracle's process pool starts before the first GPU call
+    pool = None
+    nthr = os.cpu_count() or 1
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pool = mp.get_context("spawn").Pool(min(nthr, 16))
+    sg.build()
+    dev = local
+    torch.cuda.set_device(dev)
+    pb = W.config2(mode=2)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    fp64_peak, _ = sg.measure_peaks(dev)
+    eng = sg.Engine(dev)
+    eng.load(pb)
+    eng.run(2, sg.PREC_FP64)
+    eng.sync()
+    adj = eng.results()["adj_s"]
+    ker = eng.smooth(args.sigma)
+    for _ in range(args.warmup):
+        eng.smooth(args.sigma, host=False)
+        eng.sync()
+    clocks = Clocks(dev)
+    _barrier(dist, dev)
+    clocks.start()
+    kms = []
+    for _ in range(args.steps):
+        _flush_l2(flush)
+        eng.smooth(args.sigma, host=False)
+        eng.sync()
+        ms, taps, n = eng.smooth_timing()
+        kms.append(ms)
+    _barrier(dist, dev)
+    ck = clocks.stop()
+    ms_step = _max_over_ranks(dist, statistics.mean(kms), dev)
+    value = pb.nperiod * world / (ms_step / 1e3)
+    ach = 2.0 * taps / (statistics.mean(kms) * 1e-3) / 1e12
+
+    # end to end: the drop-in per period, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        keep, jobs = [], []
+        for p, f in enumerate(_period_views(pb, adj)):
+            lons, lats = _period_axes(pb, p)
+            d = torch.empty(f.size, dtype=torch.float64, pin_memory=True)
+            d.numpy()[:] = f.ravel(order="F")
+            keep.append(d)
+            jobs.append((d.numpy().reshape(f.shape, order="F"), lons, lats))
+        h2d = sum(j[0].nbytes + j[1].nbytes + j[2].nbytes for j in jobs)
+        d2h = sum(j[0].nbytes for j in jobs)
+        ts = []
+        for i in range(args.warmup + args.steps):
+            _flush_l2(flush)
+            a = time.perf_counter()
+            for data, lons, lats in jobs:
+                sg.gaussian_smooth_geo_2(data, lons, lats, args.sigma)
+            b = time.perf_counter()
+            if i >= args.warmup:
+                ts.append(b - a)
+        e2e_s = _max_over_ranks(dist, statistics.mean(ts), dev)
+        e2e = {"value": pb.nperiod * world / e2e_s, "unit": "periods/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned input, pageable output",
+               "call": "surfatt_gaussian_smooth_geo_2 once per period"}
+
+    cpu, parity = None, {}
+    if pool is not None:
+        jobs = [(f, *_period_axes(pb, p), args.sigma)
+                for p, f in enumerate(_period_views(pb, adj))]
+        a = time.perf_counter()
+        refs = pool.map(_oracle_smooth_one, jobs)
+        b = time.perf_counter()
+        pool.close()
+        pool.join()
+        cpu = {"value": pb.nperiod / (b - a), "unit": "periods/s", "cores": min(nthr, 16),
+               "kind": "port", "seconds": b - a,
+               "sample": f"all {pb.nperiod} periods, one per worker process (the reference "
+                         "splits periods over MPI ranks, src/tomo2d.f90:210)"}
+        worst = 0.0
+        for p, (g, r) in enumerate(zip(_period_views(pb, ker), refs)):
+            worst = max(worst, float(np.max(np.abs(g - r)) / np.max(np.abs(r))))
+        parity = {"ker_s_rel_max_per_period_vs_oracle": worst}
+
+    if rank == 0:
+        line = {
+            "metric": "kernel smoothing periods/s (gaussian_smooth_geo_2 of every period's adj_s)",
+            "value": value, "unit": "periods/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tomo2d kernel smoothing on config 2's grids: 16 periods, "
+                                   "120x120 at 0.05 deg, adj_s of an FP64 gradient evaluation "
+                                   "(80 stations)", "sigma_deg": args.sigma,
+                       "window_taps_per_step": taps,
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "clocks": ck, "e2e": e2e, "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "fp64", "bound_note": "FP64 issue: one fma per window tap "
+                         "(2 flops) after the weight table; table work not counted",
+                         "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": ach / fp64_peak, "traffic": None,
+                         "peak_source": "surfatt_measure_peaks (FP64 FMA chains), this run",
+                         "kernel": "k_smooth_table + k_smooth_apply",
+                         "kernel_ms": statistics.mean(kms)},
+            "cpu_baseline": cpu, "parity": parity,
+        }
+        print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 if __name__ == "__main__":
     a = _args()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "serving":
         run_serving(a)
+    elif a.workload == "smooth":
+        run_smooth(a)
     else:
         run_ours(a)

@@ -149,6 +149,23 @@ surfatt_status_t surfatt_measadj_run_adjoint_density(
     const double* recx, const double* recy, const double* weight, const double* timetable,
     double* density);
 
+/* gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225): great-circle
+ * Gaussian smoothing of one (nx, ny) field, column-major, on the lon/lat grid
+ * lons (nx) x lats (ny) in degrees, sigma in degrees.  Output node (i, j) is
+ * sum(w * data) / sum(w) over the window |i1-i| <= int(3 sigma/dx),
+ * |j1-j| <= int(3 sigma/cosd(lat_j)/dy) clamped to the grid, with
+ * w = exp(-delta^2/(2 sigma^2)) and delta the gps2dist_2 distance in degrees
+ * (utils.f90:1280-1294).  The reference function returns the array; the
+ * binding is a subroutine writing smdata (host memory, nx*ny).  Like the
+ * reference it takes dx, dy from the first two nodes and assumes uniform
+ * spacing; SURFATT_BAD_ARG where the reference would read outside its
+ * inputs or divide by zero: nx or ny < 2, spacing not increasing or not
+ * uniform (relative 1e-9), sigma <= 0 (tomo2d rejects sigma_2d = 0,
+ * src/tomo2d.f90:48-50), |lat| >= 90. */
+surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int ny,
+                                               const double* lons, const double* lats,
+                                               double sigma, double* smdata);
+
 /* ---------------------------------------------------------------------------
  * 3. Batched gradient evaluation
  * ------------------------------------------------------------------------- */
@@ -234,6 +251,20 @@ surfatt_status_t surfatt_engine_results(surfatt_engine_t* engine, surfatt_result
  * its solve kernel alone; number of kernel launches it issued. */
 surfatt_status_t surfatt_engine_timing(surfatt_engine_t* engine, double* total_ms,
                                        double* solve_kernel_ms, int* launches);
+
+/* Kernel smoothing of tomo2d's optimize step (src/tomo2d.f90:203-233, the
+ * loop at :216-222): ker_s of period p = gaussian_smooth_geo_2(adj_s of
+ * period p, its lon/lat axes, sigma) for every period of the last run's
+ * adj_s (mode 2 or 3), computed on the device from the engine's resident
+ * adj_s.  ker_s (host, ncell doubles, the adj_s layout) may be NULL: the
+ * smoothing is then only enqueued (surfatt_engine_sync waits for it) and the
+ * result stays on the device.  SURFATT_BAD_ARG before a mode-2/3 run and for
+ * the arguments surfatt_gaussian_smooth_geo_2 rejects. */
+surfatt_status_t surfatt_engine_smooth(surfatt_engine_t* engine, double sigma, double* ker_s);
+/* Device time (ms) of the last surfatt_engine_smooth, its window taps over
+ * all output nodes, and its kernel launches (2: weight table, apply). */
+surfatt_status_t surfatt_engine_smooth_timing(surfatt_engine_t* engine, double* kernel_ms,
+                                              double* taps, int* launches);
 
 /* Launch configuration of the last run's solve kernel: blocks, threads per
  * block, resident blocks per SM, dynamic shared memory per block. */

@@ -14,6 +14,7 @@
 #include "../../include/surfatt_gb300.h"
 #include "kernels.cuh"
 #include "launch.cuh"
+#include "smooth.cuh"
 
 using namespace sgb;
 
@@ -130,11 +131,14 @@ struct ThreadCtx {
   cudaStream_t st = nullptr;
   PeriodBufs pb;
   DBuf ws, T, Ta, rx, ry, sa, out, si;
+  DBuf sm_lon, sm_lat, sm_in, sm_out, sm_tab, sm_nyw, sm_per;  // kernel smoothing
   int* si_host = nullptr;  // pinned {status, iters}
   ~ThreadCtx() {
     if (!init) return;
     pb.release();
-    for (DBuf* d : {&ws, &T, &Ta, &rx, &ry, &sa, &out, &si}) d->release();
+    for (DBuf* d : {&ws, &T, &Ta, &rx, &ry, &sa, &out, &si, &sm_lon, &sm_lat, &sm_in, &sm_out,
+                    &sm_tab, &sm_nyw, &sm_per})
+      d->release();
     if (si_host) cudaFreeHost(si_host);
     if (st) cudaStreamDestroy(st);
   }
@@ -452,6 +456,43 @@ surfatt_status_t surfatt_measadj_run_adjoint_density(
   return (surfatt_status_t)record(st, it);
 }
 
+// gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225) of one (nx, ny) field.
+surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int ny,
+                                               const double* lons, const double* lats,
+                                               double sigma, double* smdata) {
+  if (!data || !lons || !lats || !smdata || nx < 2 || ny < 2)
+    return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+  SmoothPlan plan;
+  const long long zero = 0;
+  if (smooth_plan(1, &nx, &ny, &zero, &zero, &zero, lons, lats, sigma, &plan) != ST_OK)
+    return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+  ThreadCtx& c = g_ctx;
+  int e = c.setup();
+  if (e) return (surfatt_status_t)record(e, 0);
+  const size_t N = (size_t)nx * ny;
+  if (c.sm_lon.ensure(nx * sizeof(double)) || c.sm_lat.ensure(ny * sizeof(double)) ||
+      c.sm_in.ensure(N * sizeof(double)) || c.sm_out.ensure(N * sizeof(double)) ||
+      c.sm_tab.ensure((size_t)plan.table_doubles * sizeof(double)) ||
+      c.sm_nyw.ensure((size_t)plan.nyw_count * sizeof(int)) ||
+      c.sm_per.ensure(sizeof(SmoothPeriod)))
+    return (surfatt_status_t)record(SURFATT_OOM, 0);
+  CK(cudaMemcpyAsync(c.sm_lon.p, lons, nx * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.sm_lat.p, lats, ny * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.sm_in.p, data, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.sm_nyw.p, plan.nyw.data(), plan.nyw_count * sizeof(int),
+                     cudaMemcpyHostToDevice, c.st));
+  CK(cudaMemcpyAsync(c.sm_per.p, plan.per.data(), sizeof(SmoothPeriod), cudaMemcpyHostToDevice,
+                     c.st));
+  SmoothArgs A{c.sm_per.as<SmoothPeriod>(), 1, c.sm_lon.as<double>(), c.sm_lat.as<double>(),
+               c.sm_nyw.as<int>(), c.sm_in.as<double>(), c.sm_out.as<double>(),
+               c.sm_tab.as<double>(), sigma};
+  launch_smooth(A, plan, c.st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(smdata, c.sm_out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  CK(cudaStreamSynchronize(c.st));
+  return (surfatt_status_t)record(SURFATT_OK, 0);
+}
+
 }  // extern "C"
 
 // ===========================================================================
@@ -480,6 +521,13 @@ struct surfatt_engine {
       d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
   DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
       d_fupd, d_aupd, d_ws, d_queue, d_phase, d_q;
+  // kernel smoothing of adj_s (gaussian_smooth_geo_2 per period)
+  DBuf d_ker, d_smtab, d_smnyw, d_smper;
+  std::vector<double> hx, hy;  // host copies of the grid axes (window plan)
+  SmoothPlan smplan;
+  double sm_sigma = -1.0;      // sigma of smplan / of the uploaded plan (-1: none)
+  bool smoothed = false;
+  cudaEvent_t evs0 = nullptr, evs1 = nullptr;
   int grid = 0, block = 128, per_sm = 0, last_block = 0, last_kind = 0, last_pf = 0;
   size_t last_smem = 0;
   KernelChoice tuned[2];  // per precision; -1 fields: automatic
@@ -509,7 +557,7 @@ struct surfatt_engine {
             &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
             &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
             &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
-            &d_aupd, &d_ws, &d_queue, &d_phase, &d_q};
+            &d_aupd, &d_ws, &d_queue, &d_phase, &d_q, &d_ker, &d_smtab, &d_smnyw, &d_smper};
   }
 };
 
@@ -571,7 +619,8 @@ surfatt_status_t surfatt_engine_create(surfatt_engine_t** out, int device, size_
   e->budget = budget;
   if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess ||
-      cudaEventCreate(&e->evk0) != cudaSuccess || cudaEventCreate(&e->evk1) != cudaSuccess) {
+      cudaEventCreate(&e->evk0) != cudaSuccess || cudaEventCreate(&e->evk1) != cudaSuccess ||
+      cudaEventCreate(&e->evs0) != cudaSuccess || cudaEventCreate(&e->evs1) != cudaSuccess) {
     delete e;
     return SURFATT_CUDA_ERROR;
   }
@@ -589,6 +638,8 @@ void surfatt_engine_destroy(surfatt_engine_t* e) {
   cudaEventDestroy(e->ev1);
   cudaEventDestroy(e->evk0);
   cudaEventDestroy(e->evk1);
+  cudaEventDestroy(e->evs0);
+  cudaEventDestroy(e->evs1);
   cudaStreamDestroy(e->st);
   delete e;
 }
@@ -655,6 +706,10 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   const size_t NC = (size_t)e->ncell;
   int r = 0;
   r |= up(e, e->d_xdeg, pb->xgrid, nxs) | up(e, e->d_ydeg, pb->ygrid, nys);
+  e->hx.assign(pb->xgrid, pb->xgrid + nxs);
+  e->hy.assign(pb->ygrid, pb->ygrid + nys);
+  e->sm_sigma = -1.0;
+  e->smoothed = false;
   r |= up(e, e->d_xs, (double*)nullptr, nxs) | up(e, e->d_ys, (double*)nullptr, nys);
   r |= up(e, e->d_cosy, (double*)nullptr, nys) | up(e, e->d_siny, (double*)nullptr, nys);
   r |= up(e, e->d_A, pb->m11, NC) | up(e, e->d_B, pb->m22, NC) | up(e, e->d_C, pb->m12, NC) |
@@ -1017,6 +1072,51 @@ surfatt_status_t surfatt_engine_timing(surfatt_engine_t* e, double* total_ms,
   if (total_ms) *total_ms = a;
   if (solve_kernel_ms) *solve_kernel_ms = b;
   if (launches) *launches = e->launches;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_smooth(surfatt_engine_t* e, double sigma, double* ker_s) {
+  if (!e || !e->ran || e->last_mode < 2) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  if (sigma != e->sm_sigma) {
+    e->sm_sigma = -1.0;
+    if (smooth_plan(e->nperiod, e->nx.data(), e->ny.data(), e->goff.data(), e->xoff.data(),
+                    e->yoff.data(), e->hx.data(), e->hy.data(), sigma, &e->smplan) != ST_OK)
+      return SURFATT_BAD_ARG;
+    const SmoothPlan& P = e->smplan;
+    int r = up(e, e->d_ker, (double*)nullptr, (size_t)e->ncell);
+    r |= up(e, e->d_smtab, (double*)nullptr, (size_t)P.table_doubles);
+    r |= up(e, e->d_smnyw, P.nyw.data(), (size_t)P.nyw_count);
+    r |= up(e, e->d_smper, P.per.data(), P.per.size());
+    if (r) return SURFATT_OOM;
+    e->sm_sigma = sigma;
+  }
+  SmoothArgs A{e->d_smper.as<SmoothPeriod>(), e->nperiod, e->d_xdeg.as<double>(),
+               e->d_ydeg.as<double>(), e->d_smnyw.as<int>(), e->d_adj.as<double>(),
+               e->d_ker.as<double>(), e->d_smtab.as<double>(), sigma};
+  CK(cudaEventRecord(e->evs0, e->st));
+  launch_smooth(A, e->smplan, e->st);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(e->evs1, e->st));
+  e->smoothed = true;
+  if (ker_s) {
+    CK(cudaMemcpyAsync(ker_s, e->d_ker.p, (size_t)e->ncell * sizeof(double),
+                       cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+  }
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_smooth_timing(surfatt_engine_t* e, double* kernel_ms,
+                                              double* taps, int* launches) {
+  if (!e || !e->smoothed) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaEventSynchronize(e->evs1));
+  float a = 0;
+  CK(cudaEventElapsedTime(&a, e->evs0, e->evs1));
+  if (kernel_ms) *kernel_ms = a;
+  if (taps) *taps = e->smplan.taps;
+  if (launches) *launches = 2;
   return SURFATT_OK;
 }
 

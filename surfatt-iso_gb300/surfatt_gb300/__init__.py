@@ -43,7 +43,8 @@ EXPORTED = [
     "surfatt_engine_results", "surfatt_engine_timing", "surfatt_engine_work", "surfatt_version",
     "surfatt_engine_launch_config", "surfatt_engine_autotune", "surfatt_engine_kernel_variant",
     "surfatt_engine_set_graphs", "surfatt_engine_set_kernel", "surfatt_engine_set_profile",
-    "surfatt_engine_phase_cycles",
+    "surfatt_engine_phase_cycles", "surfatt_gaussian_smooth_geo_2", "surfatt_engine_smooth",
+    "surfatt_engine_smooth_timing",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
     "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
     "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
@@ -216,6 +217,27 @@ def mask(xx, yy, table, x0, y0):
     if st != OK:
         raise SurfattError(st, "mask")
     return t
+
+
+def gaussian_smooth_geo_2(data, lons, lats, sigma):
+    """gaussian_smooth_geo_2 (src/shared/utils.f90:1194-1225): great-circle
+    Gaussian smoothing of an (nx, ny) field on the lon/lat grid lons x lats
+    (degrees, uniform), sigma in degrees.  Returns the smoothed (nx, ny)
+    field (Fortran order)."""
+    lons, lats = _c64(lons), _c64(lats)
+    d = _f2(data)
+    nx, ny = d.shape
+    if len(lons) != nx or len(lats) != ny:
+        raise ValueError("gaussian_smooth_geo_2: axes do not match the field")
+    out = np.zeros((nx, ny), order="F")
+    L = lib()
+    L.surfatt_gaussian_smooth_geo_2.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                                ctypes.c_double, _dp]
+    st = L.surfatt_gaussian_smooth_geo_2(_d(d), nx, ny, _d(lons), _d(lats), float(sigma),
+                                         _d(out))
+    if st != OK:
+        raise SurfattError(st, "gaussian_smooth_geo_2")
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -469,6 +491,31 @@ class Engine:
         st = L.surfatt_engine_set_graphs(self._h, 1 if enable else 0)
         if st != OK:
             raise SurfattError(st, "engine_set_graphs")
+
+    def smooth(self, sigma, host=True):
+        """ker_s of tomo2d's optimize step (src/tomo2d.f90:216-222): every
+        period's adj_s of the last mode-2/3 run smoothed by
+        gaussian_smooth_geo_2 with `sigma` (degrees), on the device.  Returns
+        ker_s (ncell, the adj_s layout), or None with host=False (the result
+        stays on the device; sync() waits for it)."""
+        L = lib()
+        L.surfatt_engine_smooth.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp]
+        out = np.zeros(self.pb.ncell) if host else None
+        st = L.surfatt_engine_smooth(self._h, float(sigma), _d(out) if host else None)
+        if st != OK:
+            raise SurfattError(st, "engine_smooth")
+        return out
+
+    def smooth_timing(self):
+        """(kernel ms, window taps, launches) of the last smooth()."""
+        L = lib()
+        L.surfatt_engine_smooth_timing.argtypes = [ctypes.c_void_p, _dp, _dp, _ip]
+        ms, taps, n = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_int(0)
+        st = L.surfatt_engine_smooth_timing(self._h, ctypes.byref(ms), ctypes.byref(taps),
+                                            ctypes.byref(n))
+        if st != OK:
+            raise SurfattError(st, "engine_smooth_timing")
+        return ms.value, taps.value, n.value
 
     def work(self):
         f, a = ctypes.c_double(0), ctypes.c_double(0)

@@ -33,3 +33,33 @@ def test_library_reports_no_device_without_gpu(sg):
     h = ctypes.c_void_p()
     st = sg.lib().surfatt_engine_create(ctypes.byref(h), 0, 0)
     assert st == sg.CUDA_ERROR
+
+
+def test_smooth_rejects_bad_grids_before_the_device(sg):
+    """gaussian_smooth_geo_2's argument checks run on the host, before any
+    device call: grids the reference would read outside of or divide by zero
+    on are SURFATT_BAD_ARG (no GPU needed)."""
+    import numpy as np
+    L = sg.lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.surfatt_gaussian_smooth_geo_2.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp, dp,
+                                                ctypes.c_double, dp]
+
+    def call(lons, lats, sigma):
+        lons, lats = np.asarray(lons, float), np.asarray(lats, float)
+        d = np.zeros(len(lons) * len(lats))
+        o = np.zeros_like(d)
+        p = lambda a: a.ctypes.data_as(dp)
+        return L.surfatt_gaussian_smooth_geo_2(p(d), len(lons), len(lats), p(lons), p(lats),
+                                               sigma, p(o))
+
+    x, y = 100 + 0.05 * np.arange(8), 30 + 0.05 * np.arange(6)
+    assert call(x[::-1], y, 0.1) == sg.BAD_ARG          # decreasing longitudes
+    assert call(x, y[::-1], 0.1) == sg.BAD_ARG          # decreasing latitudes
+    xn = x.copy()
+    xn[5] += 0.01
+    assert call(xn, y, 0.1) == sg.BAD_ARG               # non-uniform spacing
+    assert call(x, y, 0.0) == sg.BAD_ARG                # sigma = 0 (0/0 weights)
+    assert call(x, y, float("nan")) == sg.BAD_ARG
+    assert call(x[:1], y, 0.1) == sg.BAD_ARG            # one column: no dx
+    assert call(x, 85 + 1.0 * np.arange(6), 0.1) == sg.BAD_ARG  # reaches the pole
