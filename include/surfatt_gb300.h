@@ -161,7 +161,9 @@ surfatt_status_t surfatt_measadj_run_adjoint_density(
  * spacing; SURFATT_BAD_ARG where the reference would read outside its
  * inputs or divide by zero: nx or ny < 2, spacing not increasing or not
  * uniform (relative 1e-9), sigma <= 0 (tomo2d rejects sigma_2d = 0,
- * src/tomo2d.f90:48-50), |lat| >= 90. */
+ * src/tomo2d.f90:48-50), |lat| >= 90.  The great-circle weights depend on
+ * the grid and sigma only; a host thread's call with the same nx, ny, lons,
+ * lats and sigma as its previous call reuses them from the device. */
 surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int ny,
                                                const double* lons, const double* lats,
                                                double sigma, double* smdata);
@@ -258,11 +260,15 @@ surfatt_status_t surfatt_engine_timing(surfatt_engine_t* engine, double* total_m
  * adj_s (mode 2 or 3), computed on the device from the engine's resident
  * adj_s.  ker_s (host, ncell doubles, the adj_s layout) may be NULL: the
  * smoothing is then only enqueued (surfatt_engine_sync waits for it) and the
- * result stays on the device.  SURFATT_BAD_ARG before a mode-2/3 run and for
- * the arguments surfatt_gaussian_smooth_geo_2 rejects. */
+ * result stays on the device.  The weight table is built on the first call
+ * after a load or a change of sigma and kept for later calls (an inversion
+ * smooths every iteration's adj_s on the same grids with the same sigma).
+ * SURFATT_BAD_ARG before a mode-2/3 run and for the arguments
+ * surfatt_gaussian_smooth_geo_2 rejects. */
 surfatt_status_t surfatt_engine_smooth(surfatt_engine_t* engine, double sigma, double* ker_s);
 /* Device time (ms) of the last surfatt_engine_smooth, its window taps over
- * all output nodes, and its kernel launches (2: weight table, apply). */
+ * all output nodes, and its kernel launches (2 when it built the weight
+ * table, else 1: apply only). */
 surfatt_status_t surfatt_engine_smooth_timing(surfatt_engine_t* engine, double* kernel_ms,
                                               double* taps, int* launches);
 

@@ -132,6 +132,8 @@ struct ThreadCtx {
   PeriodBufs pb;
   DBuf ws, T, Ta, rx, ry, sa, out, si;
   DBuf sm_lon, sm_lat, sm_in, sm_out, sm_tab, sm_nyw, sm_per;  // kernel smoothing
+  SmoothPlan sm_plan;            // plan of the table on the device
+  std::vector<double> sm_key;    // nx, ny, sigma, lons, lats of that table
   int* si_host = nullptr;  // pinned {status, iters}
   ~ThreadCtx() {
     if (!init) return;
@@ -462,34 +464,55 @@ surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int n
                                                double sigma, double* smdata) {
   if (!data || !lons || !lats || !smdata || nx < 2 || ny < 2)
     return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
-  SmoothPlan plan;
-  const long long zero = 0;
-  if (smooth_plan(1, &nx, &ny, &zero, &zero, &zero, lons, lats, sigma, &plan) != ST_OK)
-    return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+  // The weight table depends on the grid and sigma only: a call with the
+  // same ones as the previous call of this thread reuses it.
+  std::vector<double> key((size_t)nx + ny + 3);
+  key[0] = nx;
+  key[1] = ny;
+  key[2] = sigma;
+  std::memcpy(key.data() + 3, lons, nx * sizeof(double));
+  std::memcpy(key.data() + 3 + nx, lats, ny * sizeof(double));
   ThreadCtx& c = g_ctx;
-  int e = c.setup();
-  if (e) return (surfatt_status_t)record(e, 0);
+  const bool cached = c.init && key.size() == c.sm_key.size() &&
+                      std::memcmp(key.data(), c.sm_key.data(), key.size() * sizeof(double)) == 0;
+  if (!cached) {
+    SmoothPlan plan;
+    const long long zero = 0;
+    if (smooth_plan(1, &nx, &ny, &zero, &zero, &zero, lons, lats, sigma, &plan) != ST_OK)
+      return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
+    int e = c.setup();
+    if (e) return (surfatt_status_t)record(e, 0);
+    c.sm_key.clear();
+    if (c.sm_lon.ensure(nx * sizeof(double)) || c.sm_lat.ensure(ny * sizeof(double)) ||
+        c.sm_tab.ensure((size_t)plan.table_doubles * sizeof(double)) ||
+        c.sm_nyw.ensure((size_t)plan.nyw_count * sizeof(int)) ||
+        c.sm_per.ensure(sizeof(SmoothPeriod)))
+      return (surfatt_status_t)record(SURFATT_OOM, 0);
+    c.sm_plan = plan;
+  }
+  const SmoothPlan& plan = c.sm_plan;
   const size_t N = (size_t)nx * ny;
-  if (c.sm_lon.ensure(nx * sizeof(double)) || c.sm_lat.ensure(ny * sizeof(double)) ||
-      c.sm_in.ensure(N * sizeof(double)) || c.sm_out.ensure(N * sizeof(double)) ||
-      c.sm_tab.ensure((size_t)plan.table_doubles * sizeof(double)) ||
-      c.sm_nyw.ensure((size_t)plan.nyw_count * sizeof(int)) ||
-      c.sm_per.ensure(sizeof(SmoothPeriod)))
+  if (c.sm_in.ensure(N * sizeof(double)) || c.sm_out.ensure(N * sizeof(double)))
     return (surfatt_status_t)record(SURFATT_OOM, 0);
-  CK(cudaMemcpyAsync(c.sm_lon.p, lons, nx * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.sm_lat.p, lats, ny * sizeof(double), cudaMemcpyHostToDevice, c.st));
   CK(cudaMemcpyAsync(c.sm_in.p, data, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.sm_nyw.p, plan.nyw.data(), plan.nyw_count * sizeof(int),
-                     cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.sm_per.p, plan.per.data(), sizeof(SmoothPeriod), cudaMemcpyHostToDevice,
-                     c.st));
   SmoothArgs A{c.sm_per.as<SmoothPeriod>(), 1, c.sm_lon.as<double>(), c.sm_lat.as<double>(),
                c.sm_nyw.as<int>(), c.sm_in.as<double>(), c.sm_out.as<double>(),
-               c.sm_tab.as<double>(), sigma};
-  launch_smooth(A, plan, c.st);
+               c.sm_tab.as<double>(), sigma, plan.nodes};
+  if (!cached) {
+    CK(cudaMemcpyAsync(c.sm_lon.p, lons, nx * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.sm_lat.p, lats, ny * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.sm_nyw.p, plan.nyw.data(), plan.nyw_count * sizeof(int),
+                       cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.sm_per.p, plan.per.data(), sizeof(SmoothPeriod),
+                       cudaMemcpyHostToDevice, c.st));
+    launch_smooth_table(A, plan, c.st);
+    CK(cudaGetLastError());
+  }
+  launch_smooth_apply(A, plan, c.st);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(smdata, c.sm_out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   CK(cudaStreamSynchronize(c.st));
+  c.sm_key.swap(key);
   return (surfatt_status_t)record(SURFATT_OK, 0);
 }
 
@@ -525,8 +548,9 @@ struct surfatt_engine {
   DBuf d_ker, d_smtab, d_smnyw, d_smper;
   std::vector<double> hx, hy;  // host copies of the grid axes (window plan)
   SmoothPlan smplan;
-  double sm_sigma = -1.0;      // sigma of smplan / of the uploaded plan (-1: none)
+  double sm_sigma = -1.0;      // sigma of the weight table on the device (-1: none)
   bool smoothed = false;
+  int sm_launches = 0;         // kernel launches of the last smoothing
   cudaEvent_t evs0 = nullptr, evs1 = nullptr;
   int grid = 0, block = 128, per_sm = 0, last_block = 0, last_kind = 0, last_pf = 0;
   size_t last_smem = 0;
@@ -1089,13 +1113,19 @@ surfatt_status_t surfatt_engine_smooth(surfatt_engine_t* e, double sigma, double
     r |= up(e, e->d_smnyw, P.nyw.data(), (size_t)P.nyw_count);
     r |= up(e, e->d_smper, P.per.data(), P.per.size());
     if (r) return SURFATT_OOM;
-    e->sm_sigma = sigma;
   }
   SmoothArgs A{e->d_smper.as<SmoothPeriod>(), e->nperiod, e->d_xdeg.as<double>(),
                e->d_ydeg.as<double>(), e->d_smnyw.as<int>(), e->d_adj.as<double>(),
-               e->d_ker.as<double>(), e->d_smtab.as<double>(), sigma};
+               e->d_ker.as<double>(), e->d_smtab.as<double>(), sigma, e->smplan.nodes};
   CK(cudaEventRecord(e->evs0, e->st));
-  launch_smooth(A, e->smplan, e->st);
+  e->sm_launches = 1;
+  if (sigma != e->sm_sigma) {  // the table depends on the grids and sigma only
+    launch_smooth_table(A, e->smplan, e->st);
+    CK(cudaGetLastError());
+    e->sm_sigma = sigma;
+    e->sm_launches = 2;
+  }
+  launch_smooth_apply(A, e->smplan, e->st);
   CK(cudaGetLastError());
   CK(cudaEventRecord(e->evs1, e->st));
   e->smoothed = true;
@@ -1116,7 +1146,7 @@ surfatt_status_t surfatt_engine_smooth_timing(surfatt_engine_t* e, double* kerne
   CK(cudaEventElapsedTime(&a, e->evs0, e->evs1));
   if (kernel_ms) *kernel_ms = a;
   if (taps) *taps = e->smplan.taps;
-  if (launches) *launches = 2;
+  if (launches) *launches = e->sm_launches;
   return SURFATT_OK;
 }
 

@@ -54,16 +54,16 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
     const int nxw = vx >= (double)(X - 1) ? X - 1 : (int)vx;
     if ((long long)P.nyw.size() < yoff[p] + Y) P.nyw.resize(yoff[p] + Y, 0);
     int wmax = 0;
+    // columns summed over a row's nodes: sum_i (min(nxw, i) + min(nxw, X-1-i) + 1)
+    const double side = nxw >= X - 1 ? 0.5 * (double)X * (X - 1)
+                                     : 0.5 * nxw * (nxw + 1.0) + (double)(X - 1 - nxw) * nxw;
+    const double cols = 2.0 * side + X;
     for (int j = 0; j < Y; ++j) {
       const double vy = sigma3 / std::cos(la[j] * kCosdScale) / dy;  // :1213
       const int w = vy >= (double)(Y - 1) ? Y - 1 : (int)vy;
       P.nyw[yoff[p] + j] = w;
       wmax = w > wmax ? w : wmax;
-      // taps of this row: window rows x window columns summed over i
       const int nr = (j + w < Y - 1 ? j + w : Y - 1) - (j - w > 0 ? j - w : 0) + 1;
-      double cols = 0;
-      for (int i = 0; i < X; ++i)
-        cols += (i < nxw ? i : nxw) + (X - 1 - i < nxw ? X - 1 - i : nxw) + 1;
       P.taps += (double)nr * cols;
     }
     SmoothPeriod& s = P.per[p];
@@ -77,7 +77,9 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
     s.xoff = xoff[p];
     s.yoff = yoff[p];
     s.toff = P.table_doubles;
+    s.node0 = P.nodes;
     P.table_doubles += (long long)Y * smooth_row_doubles(s);
+    P.nodes += (long long)X * Y;
     const size_t smem = (size_t)(2 * s.rows + s.dmax + 1) * sizeof(double);
     if (smem > kTableSmemMax) return ST_BAD_ARG;
     P.table_smem = smem > P.table_smem ? smem : P.table_smem;
@@ -98,7 +100,8 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
 // the terms of gps2dist_2 (utils.f90:1280-1294) and of :1220.  The per-row
 // factors sin(dlat/2)^2 and cos(lat_j) cos(lat_j1) and the per-offset
 // sin(dlon/2)^2 are evaluated once in shared memory.  Then one thread per
-// window row writes the prefix sums P[r][k] = w[r][0] + ... + w[r][k].
+// window row writes the prefix sums P[r][k] = w[r][0] + ... + w[r][k], and
+// one thread per clipping k the row's weight sums DL[k], DR[k].
 // Grid (max_ny, nperiod); 128 threads.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_smooth_table(SmoothArgs A) {
@@ -144,48 +147,73 @@ __global__ void __launch_bounds__(128) k_smooth_table(SmoothArgs A) {
       pt[r * W + d] = s;
     }
   }
+  __syncthreads();
+  double* dl = pt + (long long)P.rows * W;
+  double* dr = dl + W;
+  for (int k = threadIdx.x; k < W; k += blockDim.x) {
+    double l = 0.0, r = 0.0;
+    for (int q = 0; q < nr; ++q) {
+      l += pt[q * W + k] - wt[q * W];
+      r += pt[q * W + k];
+    }
+    dl[k] = l;
+    dr[k] = r;
+  }
 }
 
 // ---------------------------------------------------------------------------
-// Apply: one thread per output node (i, j).  Over the window rows in order,
+// Apply: one thread per output node, nodes numbered period by period and row
+// by row (no idle lanes at row ends).  Over the window rows in order,
 //   num += w[r][|d|] * data(i + d, n1 + r)   for d = -kl .. kr (ascending column)
-//   den += P[r][kl] - w[r][0] + P[r][kr]
 // with kl = min(nxw, i), kr = min(nxw, nx-1-i) (the clamped window of
-// :1216-1217); out = num / den (:1222-1223).  Lanes of a warp hold adjacent
-// columns: the table reads are warp-uniform, the data reads coalesced.
-// Grid (ceil(max_nx / 128), max_ny, nperiod); 128 threads.
+// :1216-1217); out = num / (DL[kl] + DR[kr]) (:1222-1223).  Lanes of a warp
+// hold adjacent columns: the table reads are warp-uniform within a row, the
+// data reads coalesced.  Grid ceil(nodes / 128); 128 threads.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_smooth_apply(SmoothArgs A) {
-  const SmoothPeriod P = A.per[blockIdx.z];
-  const int j = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= P.ny || i >= P.nx) return;
-  const int nx = P.nx, nxw = P.nxw, W = P.dmax + 1;
-  const int nyw = A.nyw[P.yoff + j];
-  const int n1 = max(0, j - nyw), n2 = min(P.ny - 1, j + nyw);
+  const long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (n >= A.nodes) return;
+  int lo = 0, hi = A.nperiod - 1;  // period of node n
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&A.per[mid].node0) <= n) lo = mid;
+    else hi = mid - 1;
+  }
+  const SmoothPeriod& P = A.per[lo];
+  const int nx = __ldg(&P.nx), nxw = __ldg(&P.nxw), W = __ldg(&P.dmax) + 1;
+  const int rows = __ldg(&P.rows), ny = __ldg(&P.ny);
+  const int k = (int)(n - __ldg(&P.node0));
+  const int j = k / nx, i = k - j * nx;
+  const int nyw = __ldg(A.nyw + __ldg(&P.yoff) + j);
+  const int n1 = max(0, j - nyw), n2 = min(ny - 1, j + nyw);
   const int kl = min(nxw, i), kr = min(nxw, nx - 1 - i);
-  const double* wt = A.table + P.toff + (long long)j * smooth_row_doubles(P);
-  const double* pt = wt + (long long)P.rows * W;
-  const double* col = A.data + P.goff + i;
-  double num = 0.0, den = 0.0;
+  const double* wt = A.table + __ldg(&P.toff) + (long long)j * (2LL * (rows + 1) * W);
+  const double* dl = wt + 2LL * rows * W;
+  const double den = __ldg(dl + kl) + __ldg(dl + W + kr);
+  const double* col = A.data + __ldg(&P.goff) + i;
+  double num = 0.0;
   for (int r = 0; r <= n2 - n1; ++r) {
     const double* w = wt + r * W;
     const double* x = col + (long long)(n1 + r) * nx;
-    den += (__ldg(pt + r * W + kl) - __ldg(w)) + __ldg(pt + r * W + kr);
 #pragma unroll 4
     for (int d = kl; d >= 1; --d) num = fma(__ldg(w + d), __ldg(x - d), num);
 #pragma unroll 4
     for (int d = 0; d <= kr; ++d) num = fma(__ldg(w + d), __ldg(x + d), num);
   }
-  A.out[P.goff + i + (long long)nx * j] = num / den;
+  A.out[__ldg(&P.goff) + k] = num / den;
 }
 
-void launch_smooth(const SmoothArgs& A, const SmoothPlan& plan, cudaStream_t st) {
-  if (A.nperiod <= 0 || plan.max_nx <= 0) return;
+void launch_smooth_table(const SmoothArgs& A, const SmoothPlan& plan, cudaStream_t st) {
+  if (A.nperiod <= 0 || plan.max_ny <= 0) return;
   if (plan.table_smem > 48 * 1024)
     cudaFuncSetAttribute(k_smooth_table, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)plan.table_smem);
   k_smooth_table<<<dim3(plan.max_ny, A.nperiod), 128, plan.table_smem, st>>>(A);
-  k_smooth_apply<<<dim3((plan.max_nx + 127) / 128, plan.max_ny, A.nperiod), 128, 0, st>>>(A);
+}
+
+void launch_smooth_apply(const SmoothArgs& A, const SmoothPlan& plan, cudaStream_t st) {
+  if (A.nperiod <= 0 || plan.nodes <= 0) return;
+  k_smooth_apply<<<(unsigned)((plan.nodes + 127) / 128), 128, 0, st>>>(A);
 }
 
 }  // namespace sgb

@@ -9,8 +9,11 @@
 // grids the reference assumes (dx, dy from the first two nodes) w depends on
 // (j, j1, |i1 - i|) only, so the GPU form evaluates each weight once per
 // (period, row, window row, column offset) in a table kernel and the apply
-// kernel spends one FP64 fma per window tap.  The weight sums come from
-// per-window-row prefix sums of the table.
+// kernel spends one FP64 fma per window tap.  A node's weight sum depends
+// on its row and on how far the window is clipped at either side, so the
+// table kernel also stores, per row, the sums for every clipping, and the
+// apply kernel reads its sum with one add.  The table depends on the grid
+// and sigma only: callers keep it while both are unchanged.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -29,6 +32,7 @@ struct SmoothPeriod {
   long long xoff;  // offset of the period's longitudes
   long long yoff;  // offset of the period's latitudes and of its per-row nyw
   long long toff;  // offset of the period's table (doubles)
+  long long node0; // first node of the period in the apply kernel's flat numbering
 };
 
 struct SmoothArgs {
@@ -39,13 +43,18 @@ struct SmoothArgs {
   const int* nyw;      // per row: int(3 sigma / cosd(lat_j) / dy), clamped to ny - 1
   const double* data;
   double* out;
-  double* table;  // per (period, row): rows x (dmax+1) weights, then as many prefix sums
-  double sigma;   // degrees
+  // per (period, row), W = dmax + 1: rows x W weights w[r][d], rows x W
+  // prefix sums P[r][k] = w[r][0] + ... + w[r][k], then the weight sums of a
+  // node clipped to kl columns on the left and kr on the right,
+  // DL[kl] + DR[kr]: DL[k] = sum_r (P[r][k] - w[r][0]), DR[k] = sum_r P[r][k].
+  double* table;
+  double sigma;     // degrees
+  long long nodes;  // output nodes of all periods
 };
 
 // Doubles of one row's table (weights + prefix sums).
 __host__ __device__ inline long long smooth_row_doubles(const SmoothPeriod& p) {
-  return 2LL * p.rows * (p.dmax + 1);
+  return 2LL * (p.rows + 1) * (p.dmax + 1);
 }
 
 // Host-side geometry of one smoothing call.
@@ -54,6 +63,7 @@ struct SmoothPlan {
   std::vector<int> nyw;        // indexed yoff + j
   long long table_doubles = 0;
   long long nyw_count = 0;     // entries of nyw
+  long long nodes = 0;         // output nodes of all periods
   int max_nx = 0, max_ny = 0;
   size_t table_smem = 0;       // dynamic shared memory of the table kernel
   double taps = 0;             // window taps over all output nodes (work count)
@@ -70,7 +80,9 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
                 const long long* xoff, const long long* yoff, const double* lons,
                 const double* lats, double sigma, SmoothPlan* plan);
 
-// Table kernel then apply kernel on `st` (2 launches).
-void launch_smooth(const SmoothArgs& A, const SmoothPlan& plan, cudaStream_t st);
+// Weight-table kernel (depends on the grid and sigma only) and apply kernel
+// (one launch each) on `st`.
+void launch_smooth_table(const SmoothArgs& A, const SmoothPlan& plan, cudaStream_t st);
+void launch_smooth_apply(const SmoothArgs& A, const SmoothPlan& plan, cudaStream_t st);
 
 }  // namespace sgb

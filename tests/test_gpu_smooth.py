@@ -86,14 +86,46 @@ def test_engine_smooth_matches_oracle(sg, oracle, mode):
         lons, lats = _grid(pb, p)
         ref = oracle.gaussian_smooth_geo_2(_f(pb, adj, p), lons, lats, 0.15)
         assert rel_max(_f(pb, ker, p), ref) <= SMOOTH_TOL
-    # device-only form, a second sigma (new window plan), then the first again
+    # device-only form, a second sigma (new window plan and table), then the
+    # same sigma again (table kept: apply only), then the first sigma again
     assert eng.smooth(0.25, host=False) is None
     assert eng.sync() == 0
     ms, taps, n = eng.smooth_timing()
     assert ms > 0 and taps > 0 and n == 2
+    k25 = eng.smooth(0.25)
+    assert eng.smooth_timing()[2] == 1
+    for p in range(pb.nperiod):
+        lons, lats = _grid(pb, p)
+        ref = oracle.gaussian_smooth_geo_2(_f(pb, adj, p), lons, lats, 0.25)
+        assert rel_max(_f(pb, k25, p), ref) <= SMOOTH_TOL
     again = eng.smooth(0.15)
     assert np.array_equal(again, ker)
+    # a new adj_s (velocity update) smoothed with the kept table
+    eng.update_velocity(pb.svel * 1.01)
+    eng.run(mode, sg.PREC_FP64)
+    eng.sync()
+    adj2 = eng.results()["adj_s"]
+    ker2 = eng.smooth(0.15)
+    assert eng.smooth_timing()[2] == 1
+    for p in range(pb.nperiod):
+        lons, lats = _grid(pb, p)
+        ref = oracle.gaussian_smooth_geo_2(_f(pb, adj2, p), lons, lats, 0.15)
+        assert rel_max(_f(pb, ker2, p), ref) <= SMOOTH_TOL
     eng.close()
+
+
+def test_dropin_table_reuse(sg, oracle):
+    """Consecutive drop-in calls on one grid with one sigma reuse the weight
+    table; a change of data, sigma or grid values gives the oracle's answer."""
+    lons, lats = W.arange_grid(100.0, 50, 0.05), W.arange_grid(22.0, 44, 0.05)
+    cases = [(_field(50, 44, 1), lons, lats, 0.2), (_field(50, 44, 2), lons, lats, 0.2),
+             (_field(50, 44, 3), lons, lats, 0.15),
+             (_field(50, 44, 4), lons + 0.5, lats, 0.15),
+             (_field(50, 44, 5), lons + 0.5, lats - 1.0, 0.15)]
+    for data, lo, la, sig in cases:
+        got = sg.gaussian_smooth_geo_2(data, lo, la, sig)
+        ref = oracle.gaussian_smooth_geo_2(data, lo, la, sig)
+        assert rel_max(got, ref) <= SMOOTH_TOL
 
 
 def test_engine_smooth_requires_adjoint_run(sg):
