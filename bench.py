@@ -69,7 +69,8 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=["config1", "config2", "config2s", "config4", "serving", "smooth"])
+                    choices=["config1", "config2", "config2s", "config4", "serving", "smooth",
+                             "kernel3d"])
     ap.add_argument("--requests", type=int, default=40,
                     help="serving: requests in the Poisson stream")
     ap.add_argument("--load", type=float, default=0.7,
@@ -415,6 +416,8 @@ def run_reference(args):
     O.build()
     if args.workload == "smooth":
         return _run_reference_smooth(args, O, dist)
+    if args.workload == "kernel3d":
+        return _run_reference_kernel3d(args, O, dist)
     pb, desc = _workload(args.workload)
     nthr = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -689,6 +692,175 @@ def run_smooth(args):
         dist.destroy_process_group()
 
 
+def _kernel3d_inputs(sg_or_none, O=None):
+    """Config 2's model (60 x 60 x 30, 16 periods) with the adj_s /
+    adj_density of an FP64 3-D-mode gradient evaluation on the model grid
+    (80 stations, forward grid = model grid 60 x 60 at 0.1 deg), from the
+    engine (ours) or the oracle (reference arm); seeded stand-ins for the
+    surfdisp96 depth kernels."""
+    from surfatt_gb300 import workloads as W
+    pb = W.config2(n=60, d=0.1, mode=3)
+    if sg_or_none is not None:
+        eng = sg_or_none.Engine(0)
+        r = eng.evaluate(pb, mode=3, precision=sg_or_none.PREC_FP64)
+        eng.close()
+    else:
+        r = O.gradient_eval(pb, mode=3, nthreads=os.cpu_count() or 1)
+    P = int(pb.nperiod)
+    adj = np.stack([r["adj_s"][int(pb.goff[p]):int(pb.goff[p]) + 3600].reshape((60, 60), order="F")
+                    for p in range(P)])
+    den = np.stack([r["adj_density"][int(pb.goff[p]):int(pb.goff[p]) + 3600]
+                    .reshape((60, 60), order="F") for p in range(P)])
+    k = W.kernel3d_case(adj_s=adj, adj_density=den)
+    k.chi0 = float(r["chi"])
+    return k
+
+
+KERNEL3D_METRIC = "3-D kernel combination + multigrid projection steps/s (combine_kernels + " \
+                  "post_processing_for_kernel)"
+KERNEL3D_DESC = ("config 2's model: 60x60x30 nodes, 16 periods, adj_s / adj_density of an FP64 "
+                 "gradient evaluation, 5 inversion grids of 8x9x8 (ncomponents 5, n_inv_grid "
+                 "[8,9,8]), use_alpha_beta_rho false, kdensity_coe 0")
+
+
+def _kernel3d_bytes(k):
+    """Algorithmic DRAM bytes of one step: combine reads adj_s, adj_density,
+    three sensitivity kernels, vs, vp and writes ker, ker_density; the
+    post-processing reads ker, writes and reads the scaled kernel, reads and
+    writes gradient_s (gk and the tables are L2-sized)."""
+    P, nx, ny, nz = k.sen_vs.shape
+    N2, N3 = nx * ny, nx * ny * nz
+    return 8 * (2 * P * N2 + 3 * P * N3 + 2 * N3 + 2 * N3 + N3 + 2 * N3 + 2 * N3)
+
+
+def run_kernel3d(args):
+    import torch
+    import surfatt_gb300 as sg
+    dist, rank, world, local = _dist()
+    sg.build()
+    dev = local
+    torch.cuda.set_device(dev)
+    k = _kernel3d_inputs(sg)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    # pinned host copies of every input and output of the call
+    keep = []
+
+    def pin(a):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        keep.append(t)
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        return v
+    for f in ("adj_s", "adj_density", "sen_vs", "sen_vp", "sen_rho", "vs3d", "vp3d"):
+        setattr(k, f, pin(np.asfortranarray(getattr(k, f))))
+    out = {n: pin(np.zeros((1, 60, 60, 30), order="F")) for n in ("ker", "ker_density",
+                                                                  "gradient_s")}
+    for _ in range(args.warmup):
+        out["gradient_s"][...] = 0
+        sg.kernel_gradient(k, out=out)
+    clocks = Clocks(dev)
+    _barrier(dist, dev)
+    clocks.start()
+    kms, walls, launches = [], [], 0
+    for _ in range(args.steps):
+        _flush_l2(flush)
+        out["gradient_s"][...] = 0
+        a = time.perf_counter()
+        sg.kernel_gradient(k, out=out)
+        walls.append(time.perf_counter() - a)
+        ms, n = sg.kernel_gradient_timing()
+        kms.append(ms)
+        launches += n
+    _barrier(dist, dev)
+    ck = clocks.stop()
+    ms_step = _max_over_ranks(dist, statistics.mean(kms), dev)
+    e2e_s = _max_over_ranks(dist, statistics.mean(walls), dev)
+    algo = _kernel3d_bytes(k)
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+    except Exception:
+        peak = 6800.0
+    ach = algo / (ms_step * 1e-3) / 1e9
+    cpu, parity = None, {}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        a = time.perf_counter()
+        rk, rkd = O.combine_kernels(k.adj_s, k.adj_density, k.sen_vs, k.sen_vp, k.sen_rho,
+                                    k.vs3d, k.vp3d)
+        rk2, rg = O.post_process_kernels(rk, rkd, 0.0, k.xinv, k.yinv, k.zinv, k.xgrids,
+                                         k.ygrids, k.zgrids, k.chi0, k.weight,
+                                         np.zeros_like(rk))
+        b = time.perf_counter()
+        cpu = {"value": 1.0 / (b - a), "unit": "steps/s", "cores": 1, "kind": "port",
+               "seconds": b - a,
+               "sample": "one full step (the reference runs it on rank 0 alone, "
+                         "src/acqui.f90:208, :258)"}
+        parity = {"bitwise_equal_vs_oracle": bool(np.array_equal(out["ker"], rk2) and
+                                                  np.array_equal(out["ker_density"], rkd) and
+                                                  np.array_equal(out["gradient_s"], rg))}
+    if rank == 0:
+        h2d = sum(getattr(k, f).nbytes for f in ("adj_s", "adj_density", "sen_vs", "sen_vp",
+                                                 "sen_rho", "vs3d", "vp3d", "xinv", "yinv",
+                                                 "zinv"))
+        line = {
+            "metric": KERNEL3D_METRIC, "value": world / (ms_step / 1e3), "unit": "steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": KERNEL3D_DESC,
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "clocks": ck,
+            "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(sum(v.nbytes for v in out.values())),
+                    "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned",
+                    "call": "surfatt_kernel_gradient"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "traffic": None,
+                         "algorithmic_bytes_per_step": algo,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                         "kernel": "k_combine + k_post_prep + k_inv_grid + k_inv2fwd (whole step)",
+                         "kernel_ms": ms_step},
+            "cpu_baseline": cpu, "parity": parity,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _run_reference_kernel3d(args, O, dist):
+    k = _kernel3d_inputs(None, O)
+    ts = []
+    for i in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        rk, rkd = O.combine_kernels(k.adj_s, k.adj_density, k.sen_vs, k.sen_vp, k.sen_rho,
+                                    k.vs3d, k.vp3d)
+        O.post_process_kernels(rk, rkd, 0.0, k.xinv, k.yinv, k.zinv, k.xgrids, k.ygrids,
+                               k.zgrids, k.chi0, k.weight, np.zeros_like(rk))
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - a)
+    s = statistics.mean(ts)
+    line = {"impl": "reference", "metric": KERNEL3D_METRIC, "value": 1.0 / s, "unit": "steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": KERNEL3D_DESC},
+            "cpu_baseline": {"value": 1.0 / s, "unit": "steps/s", "cores": 1, "kind": "port",
+                             "sample": "one full step per timed step (rank 0 alone in the "
+                                       "reference)"},
+            "e2e": {"value": 1.0 / s, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
+                    "is timed through the C restatement in oracle/"}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 if __name__ == "__main__":
     a = _args()
     if a.impl == "reference":
@@ -697,5 +869,7 @@ if __name__ == "__main__":
         run_serving(a)
     elif a.workload == "smooth":
         run_smooth(a)
+    elif a.workload == "kernel3d":
+        run_kernel3d(a)
     else:
         run_ours(a)

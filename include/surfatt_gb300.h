@@ -169,6 +169,74 @@ surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int n
                                                double sigma, double* smdata);
 
 /* ---------------------------------------------------------------------------
+ * Kernel combination and multigrid projection (3-D inversion)
+ *
+ * Layouts are the reference's arrays, Fortran order: adj_s(nperiod, nx, ny),
+ * sen_*(nperiod, nx, ny, nz), vs3d(nx, ny, nz), ker(nker, nx, ny, nz),
+ * xinv(nxinv, nset), gk(nxinv, nyinv, nzinv, nset).  All host memory.  The
+ * results equal the reference's bit for bit (every sum in its order, every
+ * product associated as written), except that the density preconditioner
+ * (kdensity_coe > 0) uses the device's pow().
+ * ------------------------------------------------------------------------- */
+
+/* inv_grid_iso (src/eikon_solver_2d.f90:1541-1614): projection of the model
+ * field adj(nx, ny, nz_3d) onto the nset shifted inversion grids, gk.
+ * A model node that no inversion grid contains prints the reference's
+ * message and ends the process (`stop`), or, with
+ * surfatt_set_exit_on_boundary(0), records SURFATT_BAD_ARG. */
+void inv_grid_iso_(const double* xinv, const double* yinv, const double* zinv, const int* nxinv,
+                   const int* nyinv, const int* nzinv, const int* nset, const double* adj,
+                   const int* nx, const int* ny, const int* nz_3d, double* gk,
+                   const double* vel_x, const double* vel_y, const double* vel_z_3d);
+/* inv2fwd_iso (src/eikon_solver_2d.f90:1617-1691): interpolation of gk back
+ * to the model grid, summed over the sets, into update(nx, ny, nz_3d). */
+void inv2fwd_iso_(const double* xinv, const double* yinv, const double* zinv, const int* nxinv,
+                  const int* nyinv, const int* nzinv, const int* nset, const int* nx,
+                  const int* ny, const int* nz_3d, const double* gk, const double* vel_x,
+                  const double* vel_y, const double* vel_z_3d, double* update);
+
+/* combine_kernels (src/acqui.f90:196-245, after the adj_s / adj_density
+ * sums): ker(k) = -sum_p adj_s(p) * sen(p) per depth, nker = 3 with
+ * use_alpha_beta_rho (rho_scaling: ker(3) = 0.33 ker(1), ker_density(3) =
+ * ker_density(1)), else nker = 1 with the Brocher derivatives of vs3d / vp3d
+ * (dalpha_dbeta, drho_dalpha, src/shared/utils.f90:99-145).  ker and
+ * ker_density are overwritten (the reference zeroes them first,
+ * src/acqui.f90:85-86). */
+surfatt_status_t surfatt_combine_kernels(int nperiod, int nx, int ny, int nz, const double* adj_s,
+                                         const double* adj_density, const double* sen_vs,
+                                         const double* sen_vp, const double* sen_rho,
+                                         const double* vs3d, const double* vp3d,
+                                         int use_alpha_beta_rho, int rho_scaling, double* ker,
+                                         double* ker_density);
+/* post_processing_for_kernel (src/acqui.f90:247-286) for nker kernels: with
+ * kdensity_coe > 0 ker(k) is preconditioned in place by its density
+ * (regularize_ker_density, :288-303); then inv_grid_iso, inv2fwd_iso,
+ * update / nset / chi0, and gradient_s(k) += update * weight (gradient_s is
+ * read and written).  SURFATT_BAD_ARG where the reference would stop
+ * because a model node lies outside the inversion grids. */
+surfatt_status_t surfatt_post_process_kernels(int nker, int nx, int ny, int nz, double* ker,
+                                              const double* ker_density, double kdensity_coe,
+                                              const double* xinv, const double* yinv,
+                                              const double* zinv, int nxinv, int nyinv,
+                                              int nzinv, int nset, const double* xgrids,
+                                              const double* ygrids, const double* zgrids,
+                                              double chi0, double weight, double* gradient_s);
+/* Both steps in one call, the kernels staying on the device in between (the
+ * sequence combine_kernels, post_proc of src/tomo.f90:155-157).  ker and
+ * ker_density (may be NULL) receive the combined kernels as the reference
+ * leaves them (ker after preconditioning). */
+surfatt_status_t surfatt_kernel_gradient(
+    int nperiod, int nx, int ny, int nz, const double* adj_s, const double* adj_density,
+    const double* sen_vs, const double* sen_vp, const double* sen_rho, const double* vs3d,
+    const double* vp3d, int use_alpha_beta_rho, int rho_scaling, double kdensity_coe,
+    const double* xinv, const double* yinv, const double* zinv, int nxinv, int nyinv, int nzinv,
+    int nset, const double* xgrids, const double* ygrids, const double* zgrids, double chi0,
+    double weight, double* ker, double* ker_density, double* gradient_s);
+/* Device time (ms, CUDA events) of the kernels of this host thread's last
+ * combine / post-process / kernel-gradient call, and their launches. */
+surfatt_status_t surfatt_kernel_gradient_timing(double* kernel_ms, int* launches);
+
+/* ---------------------------------------------------------------------------
  * 3. Batched gradient evaluation
  * ------------------------------------------------------------------------- */
 

@@ -40,6 +40,9 @@ def lib():
         _lib.orc_gradient_eval_range.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp,
                                                  _ip, _ip, _ip]
+        _lib.orc_post_process_kernels.argtypes = [ctypes.c_int] * 4 + [
+            _dp, _dp, ctypes.c_double, _dp, _dp, _dp] + [ctypes.c_int] * 4 + [
+            _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp, _dp]
     return _lib
 
 
@@ -190,3 +193,113 @@ def scatter_all_i(countval, size, rank):
     a, b = ctypes.c_int(0), ctypes.c_int(0)
     lib().orc_scatter_all_i(countval, size, rank, ctypes.byref(a), ctypes.byref(b))
     return a.value, b.value
+
+
+# ---------------------------------------------------------------------------
+# Kernel combination and multigrid projection (oracle_project.c)
+# ---------------------------------------------------------------------------
+def _F(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def combine_kernels(adj_s, adj_density, sen_vs, sen_vp, sen_rho, vs3d, vp3d,
+                    use_alpha_beta_rho=False, rho_scaling=False):
+    """combine_kernels (src/acqui.f90:196-245).  adj_s (P, nx, ny), sen_*
+    (P, nx, ny, nz), vs3d / vp3d (nx, ny, nz), Fortran order.  Returns
+    (ker, ker_density), each (nker, nx, ny, nz)."""
+    adj_s, adj_density = _F(adj_s), _F(adj_density)
+    sen_vs, sen_vp, sen_rho = _F(sen_vs), _F(sen_vp), _F(sen_rho)
+    vs3d, vp3d = _F(vs3d), _F(vp3d)
+    P, nx, ny, nz = sen_vs.shape
+    nker = 3 if use_alpha_beta_rho else 1
+    ker = np.zeros((nker, nx, ny, nz), order="F")
+    kd = np.zeros((nker, nx, ny, nz), order="F")
+    lib().orc_combine_kernels(P, nx, ny, nz, _d(adj_s), _d(adj_density), _d(sen_vs), _d(sen_vp),
+                              _d(sen_rho), _d(vs3d), _d(vp3d), int(bool(use_alpha_beta_rho)),
+                              int(bool(rho_scaling)), _d(ker), _d(kd))
+    return ker, kd
+
+
+def dalpha_dbeta(vs):
+    return lib_f("orc_dalpha_dbeta_1")(float(vs))
+
+
+def drho_dalpha(vp):
+    return lib_f("orc_drho_dalpha_1")(float(vp))
+
+
+def lib_f(name):
+    f = getattr(lib(), name)
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double]
+    return f
+
+
+class NotLocated(RuntimeError):
+    """A model node lies outside the inversion grids (the reference stops)."""
+
+
+def inv_grid_iso(xinv, yinv, zinv, adj, vel_x, vel_y, vel_z):
+    """inv_grid_iso (src/eikon_solver_2d.f90:1541-1614).  xinv (nxinv, nset)
+    ..., adj (nx, ny, nz).  Returns gk (nset * nxinv * nyinv * nzinv)."""
+    xinv, yinv, zinv, adj = _F(xinv), _F(yinv), _F(zinv), _F(adj)
+    nx, ny, nz = adj.shape
+    nset = xinv.shape[1]
+    gk = np.zeros(nset * xinv.shape[0] * yinv.shape[0] * zinv.shape[0])
+    bad = np.zeros(3)
+    rc = lib().orc_inv_grid_iso(_d(xinv), _d(yinv), _d(zinv), xinv.shape[0], yinv.shape[0],
+                                zinv.shape[0], nset, _d(adj), nx, ny, nz, _d(gk),
+                                _d(_f64(vel_x)), _d(_f64(vel_y)), _d(_f64(vel_z)), _d(bad))
+    if rc:
+        raise NotLocated(tuple(bad))
+    return gk
+
+
+def inv2fwd_iso(xinv, yinv, zinv, gk, vel_x, vel_y, vel_z):
+    """inv2fwd_iso (src/eikon_solver_2d.f90:1617-1691).  Returns update
+    (nx, ny, nz), Fortran order."""
+    xinv, yinv, zinv = _F(xinv), _F(yinv), _F(zinv)
+    vel_x, vel_y, vel_z = _f64(vel_x), _f64(vel_y), _f64(vel_z)
+    nx, ny, nz = len(vel_x), len(vel_y), len(vel_z)
+    upd = np.zeros((nx, ny, nz), order="F")
+    bad = np.zeros(3)
+    rc = lib().orc_inv2fwd_iso(_d(xinv), _d(yinv), _d(zinv), xinv.shape[0], yinv.shape[0],
+                               zinv.shape[0], xinv.shape[1], nx, ny, nz, _d(_f64(gk)), _d(vel_x),
+                               _d(vel_y), _d(vel_z), _d(upd), _d(bad))
+    if rc:
+        raise NotLocated(tuple(bad))
+    return upd
+
+
+def post_process_kernels(ker, ker_density, kdensity_coe, xinv, yinv, zinv, xgrids, ygrids,
+                         zgrids, chi0, weight, gradient_s):
+    """post_processing_for_kernel (src/acqui.f90:247-286).  ker / ker_density
+    / gradient_s (nker, nx, ny, nz).  Returns (ker after preconditioning,
+    gradient_s after accumulation) as new arrays."""
+    ker = _F(ker).copy(order="F")
+    kd = _F(ker_density)
+    grad = _F(gradient_s).copy(order="F")
+    xinv, yinv, zinv = _F(xinv), _F(yinv), _F(zinv)
+    nker, nx, ny, nz = ker.shape
+    bad = np.zeros(3)
+    rc = lib().orc_post_process_kernels(
+        nker, nx, ny, nz, _d(ker), _d(kd), ctypes.c_double(kdensity_coe), _d(xinv), _d(yinv),
+        _d(zinv), xinv.shape[0], yinv.shape[0], zinv.shape[0], xinv.shape[1],
+        _d(_f64(xgrids)), _d(_f64(ygrids)), _d(_f64(zgrids)), ctypes.c_double(chi0),
+        ctypes.c_double(weight), _d(grad), _d(bad))
+    if rc:
+        raise NotLocated(tuple(bad))
+    return ker, grad
+
+
+def get_inv_grids(xgrids, ygrids, zgrids, n_inv_grid, nset):
+    """get_inv_grids (src/model.f90:127-172): (xinv, yinv, zinv), each
+    (ninv, nset) Fortran order."""
+    xg, yg, zg = _f64(xgrids), _f64(ygrids), _f64(zgrids)
+    nix, niy, niz = (int(v) for v in n_inv_grid)
+    xinv = np.zeros((nix, nset), order="F")
+    yinv = np.zeros((niy, nset), order="F")
+    zinv = np.zeros((niz, nset), order="F")
+    lib().orc_get_inv_grids(_d(xg), len(xg), _d(yg), len(yg), _d(zg), len(zg), nix, niy, niz,
+                            nset, _d(xinv), _d(yinv), _d(zinv))
+    return xinv, yinv, zinv

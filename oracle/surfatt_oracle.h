@@ -156,6 +156,37 @@ void orc_scatter_all_i(int countval, int size, int rank, int* istart, int* iend)
 void orc_gaussian_smooth_geo_2(const double* data, int nx, int ny, const double* lons,
                                const double* lats, double sigma, double* out);
 
+/* Kernel combination and multigrid projection (oracle_project.c):
+ * combine_kernels (src/acqui.f90:196-245), inv_grid_iso / inv2fwd_iso
+ * (src/eikon_solver_2d.f90:1541-1691), post_processing_for_kernel
+ * (src/acqui.f90:247-286), get_inv_grids (src/model.f90:127-172).  The
+ * projections return 1 (and the coordinates in bad[3]) where the reference
+ * prints "I cannot locate the receiver in the domain." and stops. */
+double orc_dalpha_dbeta_1(double vs);
+double orc_drho_dalpha_1(double vp);
+void orc_combine_kernels(int P, int nx, int ny, int nz, const double* adj_s,
+                         const double* adj_density, const double* sen_vs, const double* sen_vp,
+                         const double* sen_rho, const double* vs3d, const double* vp3d,
+                         int use_alpha_beta_rho, int rho_scaling, double* ker,
+                         double* ker_density);
+int orc_inv_grid_iso(const double* xinv, const double* yinv, const double* zinv, int nxinv,
+                     int nyinv, int nzinv, int nset, const double* adj, int nx, int ny, int nz,
+                     double* gk, const double* vx, const double* vy, const double* vz,
+                     double* bad);
+int orc_inv2fwd_iso(const double* xinv, const double* yinv, const double* zinv, int nxinv,
+                    int nyinv, int nzinv, int nset, int nx, int ny, int nz, const double* gk,
+                    const double* vx, const double* vy, const double* vz, double* update,
+                    double* bad);
+int orc_post_process_kernels(int nker, int nx, int ny, int nz, double* ker,
+                             const double* ker_density, double kdensity_coe, const double* xinv,
+                             const double* yinv, const double* zinv, int nxinv, int nyinv,
+                             int nzinv, int nset, const double* xgrids, const double* ygrids,
+                             const double* zgrids, double chi0, double weight, double* gradient_s,
+                             double* bad);
+void orc_get_inv_grids(const double* xgrids, int nx, const double* ygrids, int ny,
+                       const double* zgrids, int nz, int ninvx, int ninvy, int ninvz, int nset,
+                       double* xinv, double* yinv, double* zinv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/surfatt_gb300.h"
+#include "host_buf.cuh"
 #include "kernels.cuh"
 #include "launch.cuh"
 #include "smooth.cuh"
@@ -23,47 +24,6 @@ namespace {
 thread_local int g_last_status = SURFATT_OK;
 thread_local int g_last_iters = 0;
 int g_exit_on_boundary = 1;
-
-#define CK(call)                                                                 \
-  do {                                                                           \
-    cudaError_t e_ = (call);                                                     \
-    if (e_ != cudaSuccess) {                                                     \
-      std::fprintf(stderr, "surfatt_gb300: %s failed: %s (%s:%d)\n", #call,       \
-                   cudaGetErrorString(e_), __FILE__, __LINE__);                  \
-      return SURFATT_CUDA_ERROR;                                                 \
-    }                                                                            \
-  } while (0)
-
-// Grow-only device buffer.
-struct DBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  size_t* counter = nullptr;  // engine allocation counter (budget), may be null
-  int ensure(size_t bytes) {
-    if (bytes <= cap) return SURFATT_OK;
-    release();
-    size_t want = bytes < 256 ? 256 : bytes;
-    if (cudaMalloc(&p, want) != cudaSuccess) {
-      p = nullptr;
-      cap = 0;
-      cudaGetLastError();
-      return SURFATT_OOM;
-    }
-    cap = want;
-    if (counter) *counter += cap;
-    return SURFATT_OK;
-  }
-  void release() {
-    if (p) {
-      cudaFree(p);
-      if (counter) *counter -= cap;
-    }
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T* as() const { return static_cast<T*>(p); }
-};
 
 // ---------------------------------------------------------------------------
 // Per-thread drop-in context: one stream and grow-only scratch per host
@@ -302,6 +262,11 @@ int mask_dropin(const double* xx, const double* yy, int nx, int ny, double* tab,
 }
 
 }  // namespace
+
+namespace sgb {
+int host_record(int status, int iters) { return record(status, iters); }
+bool host_exit_on_stop() { return g_exit_on_boundary != 0; }
+}  // namespace sgb
 
 // ===========================================================================
 // 1. Drop-in symbols

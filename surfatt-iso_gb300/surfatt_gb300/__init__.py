@@ -44,7 +44,8 @@ EXPORTED = [
     "surfatt_engine_launch_config", "surfatt_engine_autotune", "surfatt_engine_kernel_variant",
     "surfatt_engine_set_graphs", "surfatt_engine_set_kernel", "surfatt_engine_set_profile",
     "surfatt_engine_phase_cycles", "surfatt_gaussian_smooth_geo_2", "surfatt_engine_smooth",
-    "surfatt_engine_smooth_timing",
+    "surfatt_engine_smooth_timing", "inv_grid_iso_", "inv2fwd_iso_", "surfatt_combine_kernels",
+    "surfatt_post_process_kernels", "surfatt_kernel_gradient", "surfatt_kernel_gradient_timing",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
     "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
     "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
@@ -238,6 +239,137 @@ def gaussian_smooth_geo_2(data, lons, lats, sigma):
     if st != OK:
         raise SurfattError(st, "gaussian_smooth_geo_2")
     return out
+
+
+# ---------------------------------------------------------------------------
+# Kernel combination and multigrid projection (3-D inversion)
+# ---------------------------------------------------------------------------
+def _F(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def inv_grid_iso(xinv, yinv, zinv, adj, vel_x, vel_y, vel_z):
+    """inv_grid_iso (src/eikon_solver_2d.f90:1541-1614) through the drop-in
+    symbol: xinv (nxinv, nset), ..., adj (nx, ny, nz).  Returns gk
+    (nset*nxinv*nyinv*nzinv).  A model node outside the inversion grids ends
+    the process as the reference's `stop` does, unless
+    set_exit_on_boundary(False), when SurfattError(BAD_ARG) is raised."""
+    xinv, yinv, zinv, adj = _F(xinv), _F(yinv), _F(zinv), _F(adj)
+    vx, vy, vz = _c64(vel_x), _c64(vel_y), _c64(vel_z)
+    nx, ny, nz = adj.shape
+    gk = np.zeros(xinv.shape[1] * xinv.shape[0] * yinv.shape[0] * zinv.shape[0])
+    lib().inv_grid_iso_(_d(xinv), _d(yinv), _d(zinv), _ci(xinv.shape[0]), _ci(yinv.shape[0]),
+                        _ci(zinv.shape[0]), _ci(xinv.shape[1]), _d(adj), _ci(nx), _ci(ny),
+                        _ci(nz), _d(gk), _d(vx), _d(vy), _d(vz))
+    st = last_status()
+    if st != OK:
+        raise SurfattError(st, "inv_grid_iso")
+    return gk
+
+
+def inv2fwd_iso(xinv, yinv, zinv, gk, vel_x, vel_y, vel_z):
+    """inv2fwd_iso (src/eikon_solver_2d.f90:1617-1691) through the drop-in
+    symbol.  Returns update (nx, ny, nz), Fortran order."""
+    xinv, yinv, zinv = _F(xinv), _F(yinv), _F(zinv)
+    vx, vy, vz = _c64(vel_x), _c64(vel_y), _c64(vel_z)
+    gk = _c64(gk)
+    upd = np.zeros((len(vx), len(vy), len(vz)), order="F")
+    lib().inv2fwd_iso_(_d(xinv), _d(yinv), _d(zinv), _ci(xinv.shape[0]), _ci(yinv.shape[0]),
+                       _ci(zinv.shape[0]), _ci(xinv.shape[1]), _ci(len(vx)), _ci(len(vy)),
+                       _ci(len(vz)), _d(gk), _d(vx), _d(vy), _d(vz), _d(upd))
+    st = last_status()
+    if st != OK:
+        raise SurfattError(st, "inv2fwd_iso")
+    return upd
+
+
+def combine_kernels(adj_s, adj_density, sen_vs, sen_vp, sen_rho, vs3d=None, vp3d=None,
+                    use_alpha_beta_rho=False, rho_scaling=False):
+    """combine_kernels (src/acqui.f90:196-245): adj_s / adj_density
+    (P, nx, ny), sen_* (P, nx, ny, nz), vs3d / vp3d (nx, ny, nz).  Returns
+    (ker, ker_density), (nker, nx, ny, nz) Fortran order."""
+    adj_s, adj_density = _F(adj_s), _F(adj_density)
+    sen_vs, sen_vp, sen_rho = _F(sen_vs), _F(sen_vp), _F(sen_rho)
+    P, nx, ny, nz = sen_vs.shape
+    vs3d = _F(vs3d) if vs3d is not None else np.zeros((nx, ny, nz), order="F")
+    vp3d = _F(vp3d) if vp3d is not None else np.zeros((nx, ny, nz), order="F")
+    nker = 3 if use_alpha_beta_rho else 1
+    ker = np.zeros((nker, nx, ny, nz), order="F")
+    kd = np.zeros((nker, nx, ny, nz), order="F")
+    L = lib()
+    L.surfatt_combine_kernels.argtypes = [ctypes.c_int] * 4 + [_dp] * 7 + [ctypes.c_int] * 2 + \
+        [_dp] * 2
+    st = L.surfatt_combine_kernels(P, nx, ny, nz, _d(adj_s), _d(adj_density), _d(sen_vs),
+                                   _d(sen_vp), _d(sen_rho), _d(vs3d), _d(vp3d),
+                                   int(bool(use_alpha_beta_rho)), int(bool(rho_scaling)), _d(ker),
+                                   _d(kd))
+    if st != OK:
+        raise SurfattError(st, "combine_kernels")
+    return ker, kd
+
+
+def post_process_kernels(ker, ker_density, kdensity_coe, xinv, yinv, zinv, xgrids, ygrids,
+                         zgrids, chi0, weight, gradient_s):
+    """post_processing_for_kernel (src/acqui.f90:247-286).  Returns (ker
+    after preconditioning, gradient_s + the kernels' update), new arrays."""
+    ker = _F(ker).copy(order="F")
+    kd = _F(ker_density)
+    grad = _F(gradient_s).copy(order="F")
+    xinv, yinv, zinv = _F(xinv), _F(yinv), _F(zinv)
+    nker, nx, ny, nz = ker.shape
+    L = lib()
+    L.surfatt_post_process_kernels.argtypes = [ctypes.c_int] * 4 + [_dp, _dp, ctypes.c_double,
+                                                                      _dp, _dp, _dp] + \
+        [ctypes.c_int] * 4 + [_dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp]
+    st = L.surfatt_post_process_kernels(nker, nx, ny, nz, _d(ker), _d(kd), float(kdensity_coe),
+                                        _d(xinv), _d(yinv), _d(zinv), xinv.shape[0],
+                                        yinv.shape[0], zinv.shape[0], xinv.shape[1],
+                                        _d(_c64(xgrids)), _d(_c64(ygrids)), _d(_c64(zgrids)),
+                                        float(chi0), float(weight), _d(grad))
+    if st != OK:
+        raise SurfattError(st, "post_process_kernels")
+    return ker, grad
+
+
+def kernel_gradient(k, use_alpha_beta_rho=False, rho_scaling=False, kdensity_coe=0.0,
+                    gradient_s=None, out=None):
+    """combine_kernels + post_processing_for_kernel in one call (kernels
+    stay on the device) for a workloads.Kernel3D `k`.  Returns (ker,
+    ker_density, gradient_s).  `out`: optional dict of preallocated
+    Fortran-order arrays ker / ker_density / gradient_s (e.g. pinned)."""
+    P, nx, ny, nz = k.sen_vs.shape
+    nker = 3 if use_alpha_beta_rho else 1
+    if out is None:
+        out = {n: np.zeros((nker, nx, ny, nz), order="F")
+               for n in ("ker", "ker_density", "gradient_s")}
+        if gradient_s is not None:
+            out["gradient_s"][...] = gradient_s
+    L = lib()
+    L.surfatt_kernel_gradient.argtypes = [ctypes.c_int] * 4 + [_dp] * 7 + [ctypes.c_int] * 2 + \
+        [ctypes.c_double] + [_dp] * 3 + [ctypes.c_int] * 4 + [_dp] * 3 + [ctypes.c_double] * 2 + \
+        [_dp] * 3
+    st = L.surfatt_kernel_gradient(
+        P, nx, ny, nz, _d(k.adj_s), _d(k.adj_density), _d(k.sen_vs), _d(k.sen_vp),
+        _d(k.sen_rho), _d(k.vs3d), _d(k.vp3d), int(bool(use_alpha_beta_rho)),
+        int(bool(rho_scaling)), float(kdensity_coe), _d(k.xinv), _d(k.yinv), _d(k.zinv),
+        k.xinv.shape[0], k.yinv.shape[0], k.zinv.shape[0], k.xinv.shape[1], _d(k.xgrids),
+        _d(k.ygrids), _d(k.zgrids), float(k.chi0), float(k.weight), _d(out["ker"]),
+        _d(out["ker_density"]), _d(out["gradient_s"]))
+    if st != OK:
+        raise SurfattError(st, "kernel_gradient")
+    return out["ker"], out["ker_density"], out["gradient_s"]
+
+
+def kernel_gradient_timing():
+    """(device ms, kernel launches) of this thread's last combine /
+    post-process / kernel-gradient call."""
+    L = lib()
+    L.surfatt_kernel_gradient_timing.argtypes = [_dp, _ip]
+    ms, n = ctypes.c_double(0), ctypes.c_int(0)
+    st = L.surfatt_kernel_gradient_timing(ctypes.byref(ms), ctypes.byref(n))
+    if st != OK:
+        raise SurfattError(st, "kernel_gradient_timing")
+    return ms.value, n.value
 
 
 # ---------------------------------------------------------------------------

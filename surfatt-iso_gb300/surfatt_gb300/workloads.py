@@ -387,3 +387,124 @@ def read_src_rec_tt(fname):
     with open(fname) as f:
         r = csv.DictReader(f)
         return np.array([float(row["tt"]) for row in r])
+
+
+# ---------------------------------------------------------------------------
+# 3-D kernel combination and multigrid projection inputs
+# ---------------------------------------------------------------------------
+def linspace_ref(first: float, last: float, n: int) -> np.ndarray:
+    """linspace_r8r8 (src/shared/utils.f90:592-604): first + step*(i-1),
+    last node set to `last`."""
+    step = (last - first) / (n - 1)
+    v = first + step * np.arange(n, dtype=np.float64)
+    v[-1] = last
+    return v
+
+
+def inv_grids(xgrids, ygrids, zgrids, n_inv_grid, nset):
+    """get_inv_grids (src/model.f90:127-172): the nset shifted inversion
+    grids, (xinv, yinv, zinv), each (ninv, nset) in Fortran order."""
+    nix, niy, niz = (int(v) for v in n_inv_grid)
+    x1, xn = float(xgrids[0]), float(xgrids[-1])
+    y1, yn = float(ygrids[0]), float(ygrids[-1])
+    z1, zn = float(zgrids[0]), float(zgrids[-1])
+    ix = linspace_ref(x1 - (xn - x1) / (nix - 2) / 2.0, xn + (xn - x1) / (nix - 2) / 2.0, nix)
+    iy = linspace_ref(y1 - (yn - y1) / (niy - 2), yn, niy)
+    iz = linspace_ref(z1 - 0.5 * (zn - z1) / (niz - 2), zn + 0.5 * (zn - z1) / (niz - 2), niz)
+    zref = np.concatenate([iz[1:], iz[-1:]])
+    zadd = (zref - iz) / (nset + 1)
+    zadd[0] = 0
+    xinv = np.zeros((nix, nset), order="F")
+    yinv = np.zeros((niy, nset), order="F")
+    zinv = np.zeros((niz, nset), order="F")
+    polar = 1
+    for i in range(nset):
+        if i == 0:
+            xinv[:, 0] = ix
+        else:
+            xinv[:, i] = xinv[:, i - 1] + polar * i * (ix[1] - ix[0]) / (nset + 1)
+            polar = -polar
+        yinv[:, i] = iy + i * (iy[1] - iy[0]) / (nset + 1)
+        zinv[:, i] = iz + i * zadd
+    return xinv, yinv, zinv
+
+
+def brocher_vp(vs):
+    """Brocher (2005) Vp from Vs (km/s), the relation behind the reference's
+    empirical_vp / dalpha_dbeta."""
+    vs = np.asarray(vs, np.float64)
+    return 0.9409 + 2.0947 * vs - 0.8206 * vs ** 2 + 0.2683 * vs ** 3 - 0.0251 * vs ** 4
+
+
+@dataclasses.dataclass
+class Kernel3D:
+    """Inputs of combine_kernels + post_processing_for_kernel for one data
+    type, in the reference's layouts (Fortran order): adj_s / adj_density
+    (P, nx, ny), sen_vs / sen_vp / sen_rho (P, nx, ny, nz), vs3d / vp3d
+    (nx, ny, nz), model axes, inversion grids (ninv, nset)."""
+    name: str
+    xgrids: np.ndarray
+    ygrids: np.ndarray
+    zgrids: np.ndarray
+    adj_s: np.ndarray
+    adj_density: np.ndarray
+    sen_vs: np.ndarray
+    sen_vp: np.ndarray
+    sen_rho: np.ndarray
+    vs3d: np.ndarray
+    vp3d: np.ndarray
+    xinv: np.ndarray
+    yinv: np.ndarray
+    zinv: np.ndarray
+    periods: np.ndarray
+    chi0: float = 1.0
+    weight: float = 1.0
+
+    @property
+    def shape(self):
+        return self.sen_vs.shape
+
+
+def kernel3d_case(nx=60, ny=60, nz=30, nperiod=16, d=0.1, zmax=60.0, n_inv_grid=(8, 9, 8),
+                  nset=5, seed=2, adj_s=None, adj_density=None, name=None):
+    """Config 2's model (60 x 60 x 30 nodes, 0.1 deg, 0-60 km, Vs linear
+    3.2 -> 4.5 km/s with a +-5 % 2x3x2 checkerboard, 16 periods 2-40 s) with
+    the first example's inversion grids (ncomponents 5, n_inv_grid 8 x 9 x 8).
+    The depth sensitivity kernels come from surfdisp96 in the reference
+    (out of scope): seeded stand-ins here, a depth bump per period centred
+    near a third of the wavelength, modulated laterally.  adj_s /
+    adj_density: (P, nx, ny) fields (e.g. an engine evaluation on the model
+    grid, transposed), else seeded smooth fields of both signs."""
+    rng = np.random.default_rng(seed)
+    xg, yg = arange_grid(100.0, nx, d), arange_grid(22.0, ny, d)
+    zg = np.linspace(0.0, zmax, nz)
+    periods = np.geomspace(2.0, 40.0, nperiod)
+    cbxy = checkerboard_2d(nx, ny, 2, 3, 1.0) - 1.0
+    cbz = np.sin(2 * PI_F * np.arange(1, nz + 1) / nz)
+    vs = (3.2 + 1.3 * zg / zmax)[None, None, :] * (1 + 0.05 * cbxy[:, :, None] * cbz[None, None, :])
+    vs = np.asfortranarray(vs)
+    vp = np.asfortranarray(brocher_vp(vs))
+    X = np.linspace(0, 1, nx)[:, None]
+    Y = np.linspace(0, 1, ny)[None, :]
+    if adj_s is None:
+        ph = rng.uniform(0, 2 * np.pi, (nperiod, 2))
+        adj_s = np.stack([1e-3 * np.sin(3 * X + ph[p, 0]) * np.cos(2 * Y + ph[p, 1])
+                          for p in range(nperiod)])
+    if adj_density is None:
+        adj_density = np.abs(adj_s) * (1 + 0.1 * rng.random(adj_s.shape))
+    sen = []
+    for k in range(3):
+        s = np.zeros((nperiod, nx, ny, nz))
+        for p, T in enumerate(periods):
+            zc = 3.5 * T / 3.0
+            w = max(0.25 * 3.5 * T, 2 * (zg[1] - zg[0]))
+            bump = np.exp(-((zg - zc) / w) ** 2) * (0.5 - 0.2 * k)
+            lat = 1 + 0.05 * np.cos(2 * np.pi * (X + 0.3 * k)) * np.sin(2 * np.pi * Y)
+            s[p] = lat[:, :, None] * bump[None, None, :]
+        sen.append(np.asfortranarray(s))
+    xinv, yinv, zinv = inv_grids(xg, yg, zg, n_inv_grid, nset)
+    return Kernel3D(name=name or f"kernel3d_{nx}x{ny}x{nz}_{nperiod}per", xgrids=xg, ygrids=yg,
+                    zgrids=zg, adj_s=np.asfortranarray(adj_s),
+                    adj_density=np.asfortranarray(adj_density), sen_vs=sen[0], sen_vp=sen[1],
+                    sen_rho=sen[2], vs3d=vs, vp3d=vp, xinv=xinv, yinv=yinv, zinv=zinv,
+                    periods=periods, chi0=float(np.sum(np.abs(adj_s))) + 1.0, weight=1.0)

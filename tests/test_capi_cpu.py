@@ -63,3 +63,44 @@ def test_smooth_rejects_bad_grids_before_the_device(sg):
     assert call(x, y, float("nan")) == sg.BAD_ARG
     assert call(x[:1], y, 0.1) == sg.BAD_ARG            # one column: no dx
     assert call(x, 85 + 1.0 * np.arange(6), 0.1) == sg.BAD_ARG  # reaches the pole
+
+
+def test_projection_locate_failure_before_the_device(sg):
+    """inv_grid_iso_ with a model node outside the inversion grids: with the
+    `stop` switch off the status is SURFATT_BAD_ARG, decided on the host
+    before any device call (no GPU needed)."""
+    import numpy as np
+    sg.set_exit_on_boundary(False)
+    try:
+        vx, vy, vz = np.arange(7.0), np.arange(6.0), np.arange(5.0)
+        xinv = np.asfortranarray(np.array([[1.5, 2.0, 3.0, 7.5]]).T)
+        yinv = np.asfortranarray(np.array([[-1.5, 2.0, 4.0, 6.5]]).T)
+        zinv = np.asfortranarray(np.array([[-1.0, 1.0, 3.0, 5.0]]).T)
+        try:
+            sg.inv_grid_iso(xinv, yinv, zinv, np.zeros((7, 6, 5)), vx, vy, vz)
+            raise AssertionError("expected SurfattError")
+        except sg.SurfattError as e:
+            assert e.status == sg.BAD_ARG
+    finally:
+        sg.set_exit_on_boundary(True)
+
+
+def test_projection_locate_failure_stops_like_the_reference(sg):
+    """With the switch on (default) the drop-in prints the reference's
+    message with the node and ends the process with status 0 (`stop`)."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r); import surfatt_gb300 as sg\n"
+        "vx, vy, vz = np.arange(7.0), np.arange(6.0), np.arange(5.0)\n"
+        "xi = np.asfortranarray(np.array([[1.5, 2.0, 3.0, 7.5]]).T)\n"
+        "yi = np.asfortranarray(np.array([[-1.5, 2.0, 4.0, 6.5]]).T)\n"
+        "zi = np.asfortranarray(np.array([[-1.0, 1.0, 3.0, 5.0]]).T)\n"
+        "sg.inv_grid_iso(xi, yi, zi, np.zeros((7, 6, 5)), vx, vy, vz)\n"
+        "print('not reached')\n") % os.path.join(ROOT, "surfatt-iso_gb300")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0
+    assert "I cannot locate the receiver in the domain." in r.stdout
+    assert "not reached" not in r.stdout
+    vals = [float(v) for v in r.stdout.split("domain.")[1].split()]
+    assert vals == [1.0, 1.0, 1.0]
