@@ -70,7 +70,7 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
                     choices=["config1", "config2", "config2s", "config4", "serving", "smooth",
-                             "kernel3d"])
+                             "kernel3d", "worklist"])
     ap.add_argument("--requests", type=int, default=40,
                     help="serving: requests in the Poisson stream")
     ap.add_argument("--load", type=float, default=0.7,
@@ -418,6 +418,8 @@ def run_reference(args):
         return _run_reference_smooth(args, O, dist)
     if args.workload == "kernel3d":
         return _run_reference_kernel3d(args, O, dist)
+    if args.workload == "worklist":
+        return _run_reference_worklist(args, O, dist)
     pb, desc = _workload(args.workload)
     nthr = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -861,6 +863,131 @@ def _run_reference_kernel3d(args, O, dist):
         dist.destroy_process_group()
 
 
+WORKLIST_METRIC = "work-list builds/s (src_rec table -> solves + receiver gathers)"
+WORKLIST_DESC = ("config 2's acquisition as a src_rec table: 80 stations, each an event with "
+                 "the other 79 as receivers, 16 periods (101,120 paths, 1,280 solves)")
+
+
+def _worklist_rows():
+    from surfatt_gb300 import workloads as W
+    return W.config2_srcrec_rows()
+
+
+def _oracle_worklist(O, rows):
+    return O.srcrec_worklist([r["evtname"] for r in rows], [r["staname"] for r in rows],
+                             [r["stla"] for r in rows], [r["stlo"] for r in rows],
+                             [r["evla"] for r in rows], [r["evlo"] for r in rows],
+                             [r["period"] for r in rows], [r["tt"] for r in rows],
+                             [r["weight"] for r in rows])
+
+
+def run_worklist(args):
+    import torch
+    import surfatt_gb300 as sg
+    dist, rank, world, local = _dist()
+    sg.build()
+    dev = local
+    torch.cuda.set_device(dev)
+    rows = _worklist_rows()
+    t0 = time.perf_counter()
+    tab = sg.SrcRec.from_arrays(*[[r[k] for r in rows] for k in
+                                  ("evtname", "staname", "stla", "stlo", "evla", "evlo",
+                                   "period", "tt")], weight=[r["weight"] for r in rows])
+    index_s = time.perf_counter() - t0
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    for _ in range(args.warmup):
+        tab.build_worklist(dev)
+    clocks = Clocks(dev)
+    _barrier(dist, dev)
+    clocks.start()
+    kms, walls, launches = [], [], 0
+    for _ in range(args.steps):
+        _flush_l2(flush)
+        a = time.perf_counter()
+        ns = tab.build_worklist(dev)
+        walls.append(time.perf_counter() - a)
+        ms, n = tab.build_timing()
+        kms.append(ms)
+        launches += n
+    _barrier(dist, dev)
+    ck = clocks.stop()
+    ms_step = _max_over_ranks(dist, statistics.mean(kms), dev)
+    e2e_s = _max_over_ranks(dist, statistics.mean(walls), dev)
+    info = tab.info()
+    cpu, parity = None, {}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        a = time.perf_counter()
+        o = _oracle_worklist(O, rows)
+        b = time.perf_counter()
+        cpu = {"value": 1.0 / (b - a), "unit": "builds/s", "cores": 1, "kind": "port",
+               "seconds": b - a,
+               "sample": "one full build: get_periods, get_sta, scatter_src_gather and a "
+                         "get_evt_gather per solve with the reference's string scans"}
+        wl = tab.worklist()
+        parity = {"equal_to_oracle": bool(all(np.array_equal(wl[k], o[k]) for k in
+                                              ("pidx", "sta", "srcx", "srcy", "rec_off",
+                                               "nrec")) and
+                                          all(np.array_equal(wl[k], o[k][:len(wl[k])]) for k in
+                                              ("recx", "recy", "tt", "weight", "path")))}
+    if rank == 0:
+        n = info["npath"]
+        h2d = n * (3 * 4 + 2 * 8) + info["nsta"] * 16 + info["nperiod"]
+        d2h = ns * (4 * 4 + 2 * 8) + n * (4 + 4 * 8)
+        line = {
+            "metric": WORKLIST_METRIC, "value": world / (ms_step / 1e3), "unit": "builds/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 ids, f64 values", "data": "synthetic",
+            "config": {"workload": WORKLIST_DESC, "paths": n, "solves": ns,
+                       "stations": info["nsta"], "periods": info["nperiod"],
+                       "host_indexing_s": index_s,
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "clocks": ck,
+            "e2e": {"value": world / e2e_s, "unit": "builds/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+                    "call": "surfatt_srcrec_build_worklist (device buffers allocated per call)"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "latency", "achieved": None, "peak": None, "unit": None,
+                         "frac": None, "traffic": None,
+                         "note": "five small integer kernels; one block builds the solve order",
+                         "kernel": "k_wl_count + k_wl_solves + k_wl_scatter + k_wl_gather",
+                         "kernel_ms": ms_step},
+            "cpu_baseline": cpu, "parity": parity,
+        }
+        print(json.dumps(line))
+    tab.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _run_reference_worklist(args, O, dist):
+    rows = _worklist_rows()
+    ts = []
+    for i in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        _oracle_worklist(O, rows)
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - a)
+    s = statistics.mean(ts)
+    line = {"impl": "reference", "metric": WORKLIST_METRIC, "value": 1.0 / s, "unit": "builds/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "strings, f64", "data": "synthetic", "config": {"workload": WORKLIST_DESC},
+            "cpu_baseline": {"value": 1.0 / s, "unit": "builds/s", "cores": 1, "kind": "port",
+                             "sample": "one full build per timed step"},
+            "e2e": {"value": 1.0 / s, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
+                    "is timed through the C restatement in oracle/"}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 if __name__ == "__main__":
     a = _args()
     if a.impl == "reference":
@@ -871,5 +998,7 @@ if __name__ == "__main__":
         run_smooth(a)
     elif a.workload == "kernel3d":
         run_kernel3d(a)
+    elif a.workload == "worklist":
+        run_worklist(a)
     else:
         run_ours(a)

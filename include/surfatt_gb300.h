@@ -237,6 +237,70 @@ surfatt_status_t surfatt_kernel_gradient(
 surfatt_status_t surfatt_kernel_gradient_timing(double* kernel_ms, int* launches);
 
 /* ---------------------------------------------------------------------------
+ * The src_rec table and its work list
+ *
+ * One row per path: travel time, station, event, period, weight
+ * (src/shared/src_rec_parser.f90:20-64).  The reference derives the
+ * distinct periods (ascending), the station table (station names in order
+ * of first appearance with their first coordinates, then event names that
+ * are not stations) and the work list: for each station in that order that
+ * is some path's event, its periods in order of first appearance, each a
+ * (period, source) solve whose receivers are that event's paths at that
+ * period in path order with their station's coordinates
+ * (src/src_rec.f90:126-369, src/measadj.f90:39-53).  The names and periods
+ * are indexed on the host once; the grouping runs on the GPU.  A period of
+ * exactly 0 gets no solve, as in the reference (get_periods_by_src).
+ * ------------------------------------------------------------------------- */
+typedef struct surfatt_srcrec surfatt_srcrec_t;
+
+/* Read a src_rec CSV: header row, columns tt, staname, stla, stlo, evtname,
+ * evla, evlo, period (required; stel / evel ignored), weight (default 1),
+ * dist (default the great-circle distance), vel (default dist / tt).
+ * SURFATT_BAD_ARG for a missing file or column, a short row or a value that
+ * is not a number (the reference prints and stops). */
+surfatt_status_t surfatt_srcrec_read_csv(const char* fname, surfatt_srcrec_t** table);
+/* The same table from arrays (names as C strings; weight may be NULL). */
+surfatt_status_t surfatt_srcrec_create(int npath, const char* const* evtname,
+                                       const char* const* staname, const double* stla,
+                                       const double* stlo, const double* evla,
+                                       const double* evlo, const double* period,
+                                       const double* tt, const double* weight,
+                                       surfatt_srcrec_t** table);
+void surfatt_srcrec_destroy(surfatt_srcrec_t* table);
+/* Sizes; nsolve is -1 before surfatt_srcrec_build_worklist. */
+surfatt_status_t surfatt_srcrec_info(const surfatt_srcrec_t* table, int* npath, int* nperiod,
+                                     int* nsta, int* nsolve);
+surfatt_status_t surfatt_srcrec_periods(const surfatt_srcrec_t* table, double* periods);
+surfatt_status_t surfatt_srcrec_stations(const surfatt_srcrec_t* table, double* stlo,
+                                         double* stla);
+/* Name of station i (valid while the table lives), NULL out of range. */
+const char* surfatt_srcrec_station_name(const surfatt_srcrec_t* table, int i);
+/* Per path: time, weight, period and the station indices of its event and
+ * station and its period index (any pointer may be NULL). */
+surfatt_status_t surfatt_srcrec_paths(const surfatt_srcrec_t* table, double* tt, double* weight,
+                                      double* period, int* evt_station, int* station,
+                                      int* period_index);
+/* Build the work list on `device` (5 kernels); *nsolve receives its size. */
+surfatt_status_t surfatt_srcrec_build_worklist(surfatt_srcrec_t* table, int device, int* nsolve);
+/* The built work list: per solve the period index, source station, source
+ * coordinates and receiver offset / count; per receiver (paths of all
+ * solves, solve by solve) its coordinates, time, weight and path index --
+ * the layout of surfatt_problem_t's work-list fields.  NULL skips a field. */
+surfatt_status_t surfatt_srcrec_worklist(const surfatt_srcrec_t* table, int* pidx, int* sta,
+                                         double* srcx, double* srcy, int* rec_off, int* nrec,
+                                         double* recx, double* recy, double* tt,
+                                         double* weight, int* path);
+/* Device time (ms) of the last build's kernels and their count. */
+surfatt_status_t surfatt_srcrec_build_timing(const surfatt_srcrec_t* table, double* kernel_ms,
+                                             int* launches);
+/* Write the table with the synthetic times tt_fwd (npath) as the reference
+ * writes src_rec_iter files (src/src_rec.f90:285-325): the 11 columns tt,
+ * staname, stla, stlo, evtname, evla, evlo, period, weight, dist, vel with
+ * its F0.6 / F9.4 / F0.4 / F6.4 / F12.4 / F10.6 edits, vel = dist / tt_fwd. */
+surfatt_status_t surfatt_srcrec_write_csv(const surfatt_srcrec_t* table, const char* fname,
+                                          const double* tt_fwd);
+
+/* ---------------------------------------------------------------------------
  * 3. Batched gradient evaluation
  * ------------------------------------------------------------------------- */
 

@@ -303,3 +303,44 @@ def get_inv_grids(xgrids, ygrids, zgrids, n_inv_grid, nset):
     lib().orc_get_inv_grids(_d(xg), len(xg), _d(yg), len(yg), _d(zg), len(zg), nix, niy, niz,
                             nset, _d(xinv), _d(yinv), _d(zinv))
     return xinv, yinv, zinv
+
+
+# ---------------------------------------------------------------------------
+# Work list and receiver gathers from a src_rec table (oracle_srcrec.c)
+# ---------------------------------------------------------------------------
+def srcrec_worklist(evtname, staname, stla, stlo, evla, evlo, period, tt, weight=None):
+    """scatter_src_gather + get_recs over a src_rec table (lists of names,
+    arrays of values).  Returns a dict: periods, station names / lon / lat,
+    and per solve pidx, sta, srcx, srcy, rec_off, nrec; per receiver recx,
+    recy, tt, weight, path (0-based)."""
+    n = len(tt)
+    enc = lambda names: (ctypes.c_char_p * n)(*[str(v).encode() for v in names])
+    ev, st = enc(evtname), enc(staname)
+    f = lambda a: _f64(a)
+    stla, stlo, evla, evlo, period, tt = (f(a) for a in (stla, stlo, evla, evlo, period, tt))
+    w = None if weight is None else f(weight)
+    npr, nst, nso = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    periods = np.zeros(n)
+    sname = (ctypes.c_char_p * (2 * n))()
+    slo, sla = np.zeros(2 * n), np.zeros(2 * n)
+    ints = {k: np.zeros(n, np.int32) for k in ("pidx", "sta", "rec_off", "nrec", "path")}
+    dbl = {k: np.zeros(n) for k in ("srcx", "srcy", "recx", "recy", "tt", "weight")}
+    rc = lib().orc_srcrec_worklist(
+        n, ev, st, _d(stla), _d(stlo), _d(evla), _d(evlo), _d(period), _d(tt),
+        _d(w) if w is not None else None, ctypes.byref(npr), _d(periods), ctypes.byref(nst),
+        sname, _d(slo), _d(sla), ctypes.byref(nso), _i(ints["pidx"]), _i(ints["sta"]),
+        _d(dbl["srcx"]), _d(dbl["srcy"]), _i(ints["rec_off"]), _i(ints["nrec"]),
+        _d(dbl["recx"]), _d(dbl["recy"]), _d(dbl["tt"]), _d(dbl["weight"]), _i(ints["path"]))
+    if rc:
+        raise ValueError("srcrec_worklist: bad table")
+    P, S, NS = npr.value, nst.value, nso.value
+    out = dict(periods=periods[:P], sta_name=[sname[i].decode() for i in range(S)],
+               sta_lo=slo[:S], sta_la=sla[:S])
+    for k in ("pidx", "sta", "rec_off", "nrec"):
+        out[k] = ints[k][:NS]
+    for k in ("srcx", "srcy"):
+        out[k] = dbl[k][:NS]
+    for k in ("recx", "recy", "tt", "weight"):
+        out[k] = dbl[k][:n]
+    out["path"] = ints["path"][:n]
+    return out

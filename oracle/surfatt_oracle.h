@@ -187,6 +187,20 @@ void orc_get_inv_grids(const double* xgrids, int nx, const double* ygrids, int n
                        const double* zgrids, int nz, int ninvx, int ninvy, int ninvz, int nset,
                        double* xinv, double* yinv, double* zinv);
 
+/* Work list and receiver gathers from a src_rec table (oracle_srcrec.c):
+ * get_periods, get_sta, scatter_src_gather, get_periods_by_src,
+ * get_evt_gather, get_sta_pos (src/src_rec.f90:126-369).  0-based outputs;
+ * capacities: periods npath, stations 2*npath, solves and receivers npath.
+ * weight may be NULL (all ones). */
+int orc_srcrec_worklist(int npath, const char* const* evtname, const char* const* staname,
+                        const double* stla, const double* stlo, const double* evla,
+                        const double* evlo, const double* period, const double* tt,
+                        const double* weight, int* nperiod_out, double* periods,
+                        int* nsta_out, const char** sta_name, double* sta_lo, double* sta_la,
+                        int* nsolve_out, int* pidx, int* sta, double* srcx, double* srcy,
+                        int* rec_off, int* nrec, double* recx, double* recy, double* rtt,
+                        double* rweight, int* rpath);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,6 +46,10 @@ EXPORTED = [
     "surfatt_engine_phase_cycles", "surfatt_gaussian_smooth_geo_2", "surfatt_engine_smooth",
     "surfatt_engine_smooth_timing", "inv_grid_iso_", "inv2fwd_iso_", "surfatt_combine_kernels",
     "surfatt_post_process_kernels", "surfatt_kernel_gradient", "surfatt_kernel_gradient_timing",
+    "surfatt_srcrec_read_csv", "surfatt_srcrec_create", "surfatt_srcrec_destroy",
+    "surfatt_srcrec_info", "surfatt_srcrec_periods", "surfatt_srcrec_stations",
+    "surfatt_srcrec_station_name", "surfatt_srcrec_paths", "surfatt_srcrec_build_worklist",
+    "surfatt_srcrec_worklist", "surfatt_srcrec_build_timing", "surfatt_srcrec_write_csv",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
     "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
     "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
@@ -370,6 +374,171 @@ def kernel_gradient_timing():
     if st != OK:
         raise SurfattError(st, "kernel_gradient_timing")
     return ms.value, n.value
+
+
+# ---------------------------------------------------------------------------
+# The src_rec table and its work list
+# ---------------------------------------------------------------------------
+class SrcRec:
+    """A src_rec table (src/shared/src_rec_parser.f90, src/src_rec.f90):
+    read_csv / from_arrays, the period and station tables, the GPU-built
+    work list (scatter_src_gather + get_evt_gather) and write_csv."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def read_csv(cls, fname):
+        h = ctypes.c_void_p()
+        L = lib()
+        L.surfatt_srcrec_read_csv.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+        st = L.surfatt_srcrec_read_csv(str(fname).encode(), ctypes.byref(h))
+        if st != OK:
+            raise SurfattError(st, "srcrec_read_csv")
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, evtname, staname, stla, stlo, evla, evlo, period, tt, weight=None):
+        n = len(tt)
+        enc = lambda names: (ctypes.c_char_p * n)(*[str(v).encode() for v in names])
+        keep = [_c64(a) for a in (stla, stlo, evla, evlo, period, tt)]
+        w = None if weight is None else _c64(weight)
+        h = ctypes.c_void_p()
+        L = lib()
+        L.surfatt_srcrec_create.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p] + \
+            [_dp] * 7 + [ctypes.POINTER(ctypes.c_void_p)]
+        st = L.surfatt_srcrec_create(n, enc(evtname), enc(staname), *[_d(a) for a in keep],
+                                     _d(w) if w is not None else None, ctypes.byref(h))
+        if st != OK:
+            raise SurfattError(st, "srcrec_create")
+        return cls(h)
+
+    def close(self):
+        if self._h:
+            L = lib()
+            L.surfatt_srcrec_destroy.argtypes = [ctypes.c_void_p]
+            L.surfatt_srcrec_destroy.restype = None
+            L.surfatt_srcrec_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        a, b, c, d = (ctypes.c_int(0) for _ in range(4))
+        L = lib()
+        L.surfatt_srcrec_info.argtypes = [ctypes.c_void_p] + [_ip] * 4
+        L.surfatt_srcrec_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                              ctypes.byref(d))
+        return dict(npath=a.value, nperiod=b.value, nsta=c.value, nsolve=d.value)
+
+    def periods(self):
+        out = np.zeros(self.info()["nperiod"])
+        L = lib()
+        L.surfatt_srcrec_periods.argtypes = [ctypes.c_void_p, _dp]
+        L.surfatt_srcrec_periods(self._h, _d(out))
+        return out
+
+    def stations(self):
+        """(names, lon, lat) of the station table."""
+        n = self.info()["nsta"]
+        lo, la = np.zeros(n), np.zeros(n)
+        L = lib()
+        L.surfatt_srcrec_stations.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.surfatt_srcrec_stations(self._h, _d(lo), _d(la))
+        L.surfatt_srcrec_station_name.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.surfatt_srcrec_station_name.restype = ctypes.c_char_p
+        names = [L.surfatt_srcrec_station_name(self._h, i).decode() for i in range(n)]
+        return names, lo, la
+
+    def paths(self):
+        n = self.info()["npath"]
+        d = {k: np.zeros(n) for k in ("tt", "weight", "period")}
+        i = {k: np.zeros(n, np.int32) for k in ("evt_station", "station", "period_index")}
+        L = lib()
+        L.surfatt_srcrec_paths.argtypes = [ctypes.c_void_p] + [_dp] * 3 + [_ip] * 3
+        L.surfatt_srcrec_paths(self._h, _d(d["tt"]), _d(d["weight"]), _d(d["period"]),
+                               i["evt_station"].ctypes.data_as(_ip),
+                               i["station"].ctypes.data_as(_ip),
+                               i["period_index"].ctypes.data_as(_ip))
+        d.update(i)
+        return d
+
+    def build_worklist(self, device=0):
+        ns = ctypes.c_int(0)
+        L = lib()
+        L.surfatt_srcrec_build_worklist.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
+        st = L.surfatt_srcrec_build_worklist(self._h, int(device), ctypes.byref(ns))
+        if st != OK:
+            raise SurfattError(st, "srcrec_build_worklist")
+        return ns.value
+
+    def worklist(self):
+        """The built work list: pidx, sta, srcx, srcy, rec_off, nrec (per
+        solve) and recx, recy, tt, weight, path (per receiver)."""
+        info = self.info()
+        ns, n = info["nsolve"], info["npath"]
+        if ns < 0:
+            raise SurfattError(BAD_ARG, "srcrec_worklist: build_worklist first")
+        wi = {k: np.zeros(ns, np.int32) for k in ("pidx", "sta", "rec_off", "nrec")}
+        wd = {k: np.zeros(ns) for k in ("srcx", "srcy")}
+        nr = 0
+        L = lib()
+        L.surfatt_srcrec_worklist.argtypes = [ctypes.c_void_p] + [_ip, _ip, _dp, _dp, _ip, _ip,
+                                                                  _dp, _dp, _dp, _dp, _ip]
+        L.surfatt_srcrec_worklist(self._h, _i(wi["pidx"]), _i(wi["sta"]), _d(wd["srcx"]),
+                                  _d(wd["srcy"]), _i(wi["rec_off"]), _i(wi["nrec"]), None, None,
+                                  None, None, None)
+        nr = int(wi["nrec"].sum())
+        rd = {k: np.zeros(nr) for k in ("recx", "recy", "tt", "weight")}
+        rp = np.zeros(nr, np.int32)
+        L.surfatt_srcrec_worklist(self._h, None, None, None, None, None, None, _d(rd["recx"]),
+                                  _d(rd["recy"]), _d(rd["tt"]), _d(rd["weight"]), _i(rp))
+        out = dict(wi, **wd, **rd)
+        out["path"] = rp
+        return out
+
+    def build_timing(self):
+        ms, n = ctypes.c_double(0), ctypes.c_int(0)
+        L = lib()
+        L.surfatt_srcrec_build_timing.argtypes = [ctypes.c_void_p, _dp, _ip]
+        st = L.surfatt_srcrec_build_timing(self._h, ctypes.byref(ms), ctypes.byref(n))
+        if st != OK:
+            raise SurfattError(st, "srcrec_build_timing")
+        return ms.value, n.value
+
+    def write_csv(self, fname, tt_fwd):
+        tt_fwd = _c64(tt_fwd)
+        L = lib()
+        L.surfatt_srcrec_write_csv.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _dp]
+        st = L.surfatt_srcrec_write_csv(self._h, str(fname).encode(), _d(tt_fwd))
+        if st != OK:
+            raise SurfattError(st, "srcrec_write_csv")
+
+    def problem(self, grids, fields, mode=MODE_2D, name="src_rec"):
+        """A workloads.Problem whose work list is this table's (built on
+        the GPU): grids[p] = (xx, yy) and fields[p] = dict(svel, m11, m12,
+        m22) of period p (the table's periods, ascending)."""
+        from . import workloads as W
+        wl = self.worklist()
+        nsolve = len(wl["pidx"])
+        solves = []
+        for s in range(nsolve):
+            r0, nr = int(wl["rec_off"][s]), int(wl["nrec"][s])
+            solves.append((int(wl["pidx"][s]), float(wl["srcx"][s]), float(wl["srcy"][s]),
+                           wl["recx"][r0:r0 + nr], wl["recy"][r0:r0 + nr],
+                           wl["tt"][r0:r0 + nr], wl["weight"][r0:r0 + nr]))
+        pb = W._pack(name, grids, fields, solves, self.periods(), mode)
+        pb.path = wl["path"].astype(np.int32)
+        pb.n_paths = self.info()["npath"]
+        return pb
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
 
 
 # ---------------------------------------------------------------------------

@@ -508,3 +508,39 @@ def kernel3d_case(nx=60, ny=60, nz=30, nperiod=16, d=0.1, zmax=60.0, n_inv_grid=
                     adj_density=np.asfortranarray(adj_density), sen_vs=sen[0], sen_vp=sen[1],
                     sen_rho=sen[2], vs3d=vs, vp3d=vp, xinv=xinv, yinv=yinv, zinv=zinv,
                     periods=periods, chi0=float(np.sum(np.abs(adj_s))) + 1.0, weight=1.0)
+
+
+# ---------------------------------------------------------------------------
+# src_rec tables
+# ---------------------------------------------------------------------------
+def srcrec_rows_all_pairs(sx, sy, periods, tt_fn, names=None, weight=1.0):
+    """Rows of a src_rec table (dicts with the CSV's columns) where every
+    station is an event and every other station its receiver, for every
+    period: grouped by event, then period, then station, as the reference's
+    example tables are.  tt_fn(p, e, r) gives the time."""
+    n = len(sx)
+    names = names or [f"ST{i:04d}" for i in range(n)]
+    rows = []
+    for e in range(n):
+        for p, T in enumerate(periods):
+            for r in range(n):
+                if r == e:
+                    continue
+                rows.append(dict(tt=float(tt_fn(p, e, r)), staname=names[r], stla=float(sy[r]),
+                                 stlo=float(sx[r]), evtname=names[e], evla=float(sy[e]),
+                                 evlo=float(sx[e]), period=float(T), weight=float(weight)))
+    return rows
+
+
+def config2_srcrec_rows(nsta=80, nperiod=16, seed=1):
+    """Config 2's acquisition as a src_rec table: 80 stations, each an
+    event with the other 79 as receivers, 16 periods (101,120 paths);
+    times are great-circle distance over 3.5 km/s with 3 % seeded noise."""
+    rng = np.random.default_rng(seed)
+    xx, yy = arange_grid(100.0, 120, 0.05), arange_grid(22.0, 120, 0.05)
+    sx, sy = _stations(rng, nsta, xx[0], xx[-1], yy[0], yy[-1])
+    periods = np.geomspace(2.0, 40.0, nperiod)
+    dist = gps2dist(sy[:, None], sx[:, None], sy[None, :], sx[None, :])
+    noise = rng.normal(0, 0.03, (nperiod, nsta, nsta))
+    return srcrec_rows_all_pairs(sx, sy, periods,
+                                 lambda p, e, r: dist[e, r] / 3.5 * (1 + noise[p, e, r]))
