@@ -70,7 +70,7 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
                     choices=["config1", "config2", "config2s", "config4", "serving", "smooth",
-                             "kernel3d", "worklist"])
+                             "kernel3d", "worklist", "topo"])
     ap.add_argument("--requests", type=int, default=40,
                     help="serving: requests in the Poisson stream")
     ap.add_argument("--load", type=float, default=0.7,
@@ -420,6 +420,8 @@ def run_reference(args):
         return _run_reference_kernel3d(args, O, dist)
     if args.workload == "worklist":
         return _run_reference_worklist(args, O, dist)
+    if args.workload == "topo":
+        return _run_reference_topo(args, O, dist)
     pb, desc = _workload(args.workload)
     nthr = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -988,6 +990,116 @@ def _run_reference_worklist(args, O, dist):
         dist.destroy_process_group()
 
 
+TOPO_METRIC = "surface-metric builds/s (get_topo: smoothing + gradient + metric, all periods)"
+TOPO_DESC = ("config 5's topography: 150x200 grid at 0.02 deg (Gaussian island 4 km, radius "
+             "40 km, 200 m roughness), 15 periods with sigma from 0.04 to 0.4 deg")
+
+
+def _topo_inputs():
+    from surfatt_gb300 import workloads as W
+    xx, yy, topo, *_ = W.config5_model()
+    return xx, yy, topo, np.geomspace(0.04, 0.4, 15)
+
+
+def run_topo(args):
+    import torch
+    import surfatt_gb300 as sg
+    dist, rank, world, local = _dist()
+    sg.build()
+    dev = local
+    torch.cuda.set_device(dev)
+    xx, yy, topo, sig = _topo_inputs()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    for _ in range(args.warmup):
+        sg.topo_metric(topo, xx, yy, sig)
+    clocks = Clocks(dev)
+    _barrier(dist, dev)
+    clocks.start()
+    kms, walls, launches = [], [], 0
+    for _ in range(args.steps):
+        _flush_l2(flush)
+        a = time.perf_counter()
+        out = sg.topo_metric(topo, xx, yy, sig)
+        walls.append(time.perf_counter() - a)
+        ms, n = sg.topo_metric_timing()
+        kms.append(ms)
+        launches += n
+    _barrier(dist, dev)
+    ck = clocks.stop()
+    ms_step = _max_over_ranks(dist, statistics.mean(kms), dev)
+    e2e_s = _max_over_ranks(dist, statistics.mean(walls), dev)
+    cpu, parity = None, {}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import multiprocessing as mp
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        a = time.perf_counter()
+        ref = O.topo_metric(topo, xx, yy, sig[:2])
+        b = time.perf_counter()
+        per_period = (b - a) / 2
+        cpu = {"value": 1.0 / (per_period * len(sig)), "unit": "builds/s", "cores": 1,
+               "kind": "port", "seconds": b - a,
+               "sample": f"2 of the {len(sig)} periods on one core, scaled to all periods "
+                         "(the reference spreads periods over MPI ranks, src/grid.f90:106)"}
+        worst = 0.0
+        for g, r in zip(out, ref):
+            for p in range(2):
+                worst = max(worst, float(np.max(np.abs(g[p] - r[p])) / np.max(np.abs(r[p]))))
+        parity = {"rel_max_vs_oracle_first_two_periods": worst}
+    if rank == 0:
+        nx, ny = topo.shape
+        line = {
+            "metric": TOPO_METRIC, "value": world / (ms_step / 1e3), "unit": "builds/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": TOPO_DESC, "periods": len(sig),
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "clocks": ck,
+            "e2e": {"value": world / e2e_s, "unit": "builds/s",
+                    "h2d_bytes_per_step": int(topo.nbytes + 8 * (nx + ny + len(sig))),
+                    "d2h_bytes_per_step": int(4 * len(sig) * topo.nbytes),
+                    "ms_per_step": e2e_s * 1e3, "call": "surfatt_topo_metric"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": None, "peak": None, "unit": "TFLOP/s",
+                         "frac": None, "traffic": None,
+                         "note": "dominated by the smoothing (see --workload smooth)",
+                         "kernel": "k_smooth_table + k_smooth_apply + k_topo_metric",
+                         "kernel_ms": ms_step},
+            "cpu_baseline": cpu, "parity": parity,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _run_reference_topo(args, O, dist):
+    xx, yy, topo, sig = _topo_inputs()
+    ts = []
+    for i in range(args.warmup + args.steps):
+        a = time.perf_counter()
+        O.topo_metric(topo, xx, yy, sig[:1])
+        if i >= args.warmup:
+            ts.append((time.perf_counter() - a) * len(sig))
+    s = statistics.mean(ts)
+    line = {"impl": "reference", "metric": TOPO_METRIC, "value": 1.0 / s, "unit": "builds/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": TOPO_DESC},
+            "cpu_baseline": {"value": 1.0 / s, "unit": "builds/s", "cores": 1, "kind": "port",
+                             "sample": "one period per timed step on one core, scaled to all "
+                                       "periods"},
+            "e2e": {"value": 1.0 / s, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
+                    "is timed through the C restatement in oracle/"}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 if __name__ == "__main__":
     a = _args()
     if a.impl == "reference":
@@ -1000,5 +1112,7 @@ if __name__ == "__main__":
         run_kernel3d(a)
     elif a.workload == "worklist":
         run_worklist(a)
+    elif a.workload == "topo":
+        run_topo(a)
     else:
         run_ours(a)

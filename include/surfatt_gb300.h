@@ -301,6 +301,32 @@ surfatt_status_t surfatt_srcrec_write_csv(const surfatt_srcrec_t* table, const c
                                           const double* tt_fwd);
 
 /* ---------------------------------------------------------------------------
+ * Surface metric from topography (curved-surface eikonal)
+ * ------------------------------------------------------------------------- */
+
+/* get_topo's per-period loop (src/grid.f90:117-145): for each period p the
+ * topography topo (nx, ny, km, on the lon / lat grid of the model, degrees,
+ * uniform) is smoothed by gaussian_smooth_geo_2 with sigma[p] degrees
+ * (src/topo.f90:74-81), differentiated by gradient_2_geo
+ * (src/shared/utils.f90:1118-1160) into fx, fy, and turned into
+ * m11 = (1+fy^2)/(1+fx^2+fy^2), m22 = (1+fx^2)/(...), m12 = -fx*fy/(...)
+ * and topo_angle = atand(sqrt(fx^2+fy^2)) (calc_dip_angle,
+ * src/topo.f90:119-127).  Outputs (nperiod, nx, ny) Fortran order, as
+ * grid.f90 stores them; any may be NULL.  SURFATT_BAD_ARG for the grids
+ * and sigmas surfatt_gaussian_smooth_geo_2 rejects. */
+surfatt_status_t surfatt_topo_metric(const double* topo, int nx, int ny, const double* lon,
+                                     const double* lat, int nperiod, const double* sigma,
+                                     double* m11, double* m22, double* m12, double* topo_angle);
+/* The reference's smoothing length per period (src/grid.f90:117):
+ * sigma = phase_vel * period * wavelen_factor * km2deg / (2 pi), from the
+ * 1-D model's phase velocities (computed by surfdisp96 in the reference). */
+surfatt_status_t surfatt_topo_sigma(int nperiod, const double* phase_vel, const double* periods,
+                                    double wavelen_factor, double* sigma);
+/* Device time (ms) of this host thread's last surfatt_topo_metric and its
+ * kernel launches (3: weight table, smoothing, metric). */
+surfatt_status_t surfatt_topo_metric_timing(double* kernel_ms, int* launches);
+
+/* ---------------------------------------------------------------------------
  * 3. Batched gradient evaluation
  * ------------------------------------------------------------------------- */
 

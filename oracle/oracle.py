@@ -344,3 +344,32 @@ def srcrec_worklist(evtname, staname, stla, stlo, evla, evlo, period, tt, weight
         out[k] = dbl[k][:n]
     out["path"] = ints["path"][:n]
     return out
+
+
+# ---------------------------------------------------------------------------
+# Surface metric from topography (oracle_topo.c)
+# ---------------------------------------------------------------------------
+def gradient_2_geo(f, lon, lat):
+    """gradient_2_geo (src/shared/utils.f90:1118-1160): (tx, ty), (nx, ny)."""
+    f = _fortran2d(f)
+    nx, ny = f.shape
+    tx = np.zeros((nx, ny), order="F")
+    ty = np.zeros((nx, ny), order="F")
+    lib().orc_gradient_2_geo(_d(f), nx, ny, _d(_f64(lon)), _d(_f64(lat)), _d(tx), _d(ty))
+    return tx, ty
+
+
+def topo_metric(topo, lon, lat, sigma):
+    """get_topo's per-period loop (src/grid.f90:117-145): topo (nx, ny) in
+    km, one sigma (degrees) per period.  Returns (m11, m22, m12, angle), each
+    (nperiod, nx, ny) in Fortran order, as grid.f90 stores them."""
+    topo = _fortran2d(topo)
+    nx, ny = topo.shape
+    sigma = _f64(np.atleast_1d(sigma))
+    P = len(sigma)
+    outs = [np.zeros((P, nx, ny), order="F") for _ in range(4)]
+    rc = lib().orc_topo_metric(_d(topo), nx, ny, _d(_f64(lon)), _d(_f64(lat)), P, _d(sigma),
+                               *[_d(o) for o in outs])
+    if rc:
+        raise ValueError("topo_metric: bad grid")
+    return tuple(outs)

@@ -201,6 +201,16 @@ int orc_srcrec_worklist(int npath, const char* const* evtname, const char* const
                         int* rec_off, int* nrec, double* recx, double* recy, double* rtt,
                         double* rweight, int* rpath);
 
+/* Surface metric from topography (oracle_topo.c): gradient_2_geo
+ * (src/shared/utils.f90:1118-1160) and get_topo's per-period loop
+ * (src/grid.f90:117-145).  Metric outputs (nperiod, nx, ny), period
+ * fastest; any may be NULL. */
+void orc_gradient_2_geo(const double* f, int nx, int ny, const double* lon, const double* lat,
+                        double* tx, double* ty);
+int orc_topo_metric(const double* topo, int nx, int ny, const double* lon, const double* lat,
+                    int nperiod, const double* sigma, double* m11, double* m22, double* m12,
+                    double* angle);
+
 #ifdef __cplusplus
 }
 #endif

@@ -443,7 +443,8 @@ surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int n
   if (!cached) {
     SmoothPlan plan;
     const long long zero = 0;
-    if (smooth_plan(1, &nx, &ny, &zero, &zero, &zero, lons, lats, sigma, &plan) != ST_OK)
+    if (smooth_plan(1, &nx, &ny, &zero, nullptr, &zero, &zero, lons, lats, &sigma, &plan) !=
+        ST_OK)
       return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
     int e = c.setup();
     if (e) return (surfatt_status_t)record(e, 0);
@@ -462,7 +463,7 @@ surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int n
   CK(cudaMemcpyAsync(c.sm_in.p, data, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
   SmoothArgs A{c.sm_per.as<SmoothPeriod>(), 1, c.sm_lon.as<double>(), c.sm_lat.as<double>(),
                c.sm_nyw.as<int>(), c.sm_in.as<double>(), c.sm_out.as<double>(),
-               c.sm_tab.as<double>(), sigma, plan.nodes};
+               c.sm_tab.as<double>(), plan.nodes};
   if (!cached) {
     CK(cudaMemcpyAsync(c.sm_lon.p, lons, nx * sizeof(double), cudaMemcpyHostToDevice, c.st));
     CK(cudaMemcpyAsync(c.sm_lat.p, lats, ny * sizeof(double), cudaMemcpyHostToDevice, c.st));
@@ -1069,8 +1070,10 @@ surfatt_status_t surfatt_engine_smooth(surfatt_engine_t* e, double sigma, double
   CK(cudaSetDevice(e->device));
   if (sigma != e->sm_sigma) {
     e->sm_sigma = -1.0;
-    if (smooth_plan(e->nperiod, e->nx.data(), e->ny.data(), e->goff.data(), e->xoff.data(),
-                    e->yoff.data(), e->hx.data(), e->hy.data(), sigma, &e->smplan) != ST_OK)
+    const std::vector<double> sig(e->nperiod, sigma);
+    if (smooth_plan(e->nperiod, e->nx.data(), e->ny.data(), e->goff.data(), nullptr,
+                    e->xoff.data(), e->yoff.data(), e->hx.data(), e->hy.data(), sig.data(),
+                    &e->smplan) != ST_OK)
       return SURFATT_BAD_ARG;
     const SmoothPlan& P = e->smplan;
     int r = up(e, e->d_ker, (double*)nullptr, (size_t)e->ncell);
@@ -1081,7 +1084,7 @@ surfatt_status_t surfatt_engine_smooth(surfatt_engine_t* e, double sigma, double
   }
   SmoothArgs A{e->d_smper.as<SmoothPeriod>(), e->nperiod, e->d_xdeg.as<double>(),
                e->d_ydeg.as<double>(), e->d_smnyw.as<int>(), e->d_adj.as<double>(),
-               e->d_ker.as<double>(), e->d_smtab.as<double>(), sigma, e->smplan.nodes};
+               e->d_ker.as<double>(), e->d_smtab.as<double>(), e->smplan.nodes};
   CK(cudaEventRecord(e->evs0, e->st));
   e->sm_launches = 1;
   if (sigma != e->sm_sigma) {  // the table depends on the grids and sigma only

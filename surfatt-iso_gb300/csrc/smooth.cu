@@ -31,14 +31,15 @@ bool uniform_axis(const double* x, int n, double step) {
 }  // namespace
 
 int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff,
-                const long long* xoff, const long long* yoff, const double* lons,
-                const double* lats, double sigma, SmoothPlan* plan) {
+                const long long* doff, const long long* xoff, const long long* yoff,
+                const double* lons, const double* lats, const double* sigma, SmoothPlan* plan) {
   SmoothPlan& P = *plan;
   P = SmoothPlan();
-  if (nperiod < 0 || !std::isfinite(sigma) || !(sigma > 0.0)) return ST_BAD_ARG;
-  const double sigma3 = sigma * 3;  // utils.f90:1205
+  if (nperiod < 0) return ST_BAD_ARG;
   P.per.resize(nperiod);
   for (int p = 0; p < nperiod; ++p) {
+    if (!std::isfinite(sigma[p]) || !(sigma[p] > 0.0)) return ST_BAD_ARG;
+    const double sigma3 = sigma[p] * 3;  // utils.f90:1205
     const int X = nx[p], Y = ny[p];
     if (X < 2 || Y < 2) return ST_BAD_ARG;  // dx, dy read the first two nodes
     const double* lo = lons + xoff[p];
@@ -52,7 +53,8 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
     // (the window is clamped to it anyway, :1216).
     const double vx = sigma3 / dx;
     const int nxw = vx >= (double)(X - 1) ? X - 1 : (int)vx;
-    if ((long long)P.nyw.size() < yoff[p] + Y) P.nyw.resize(yoff[p] + Y, 0);
+    const long long woff = (long long)P.nyw.size();
+    P.nyw.resize(woff + Y, 0);
     int wmax = 0;
     // columns summed over a row's nodes: sum_i (min(nxw, i) + min(nxw, X-1-i) + 1)
     const double side = nxw >= X - 1 ? 0.5 * (double)X * (X - 1)
@@ -61,7 +63,7 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
     for (int j = 0; j < Y; ++j) {
       const double vy = sigma3 / std::cos(la[j] * kCosdScale) / dy;  // :1213
       const int w = vy >= (double)(Y - 1) ? Y - 1 : (int)vy;
-      P.nyw[yoff[p] + j] = w;
+      P.nyw[woff + j] = w;
       wmax = w > wmax ? w : wmax;
       const int nr = (j + w < Y - 1 ? j + w : Y - 1) - (j - w > 0 ? j - w : 0) + 1;
       P.taps += (double)nr * cols;
@@ -73,9 +75,12 @@ int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff
     s.dmax = nxw;
     s.rows = 2 * wmax + 1 < Y ? 2 * wmax + 1 : Y;
     s.pad = 0;
+    s.sigma = sigma[p];
     s.goff = goff[p];
+    s.doff = doff ? doff[p] : goff[p];
     s.xoff = xoff[p];
     s.yoff = yoff[p];
+    s.woff = woff;
     s.toff = P.table_doubles;
     s.node0 = P.nodes;
     P.table_doubles += (long long)Y * smooth_row_doubles(s);
@@ -111,7 +116,7 @@ __global__ void __launch_bounds__(128) k_smooth_table(SmoothArgs A) {
   extern __shared__ double sh[];
   const double* lons = A.lons + P.xoff;
   const double* lats = A.lats + P.yoff;
-  const int nyw = A.nyw[P.yoff + j];
+  const int nyw = A.nyw[P.woff + j];
   const int n1 = max(0, j - nyw), n2 = min(P.ny - 1, j + nyw), nr = n2 - n1 + 1;
   const int W = P.dmax + 1;
   double* s1s = sh;       // [nr]
@@ -132,7 +137,7 @@ __global__ void __launch_bounds__(128) k_smooth_table(SmoothArgs A) {
   __syncthreads();
   double* wt = A.table + P.toff + (long long)j * smooth_row_doubles(P);
   double* pt = wt + (long long)P.rows * W;
-  const double two_sigma_sq = 2.0 * (A.sigma * A.sigma);
+  const double two_sigma_sq = 2.0 * (P.sigma * P.sigma);
   for (int e = threadIdx.x; e < nr * W; e += blockDim.x) {
     const int r = e / W, d = e - r * W;
     const double a = s1s[r] + s2s[d] * cc[r];
@@ -184,13 +189,13 @@ __global__ void __launch_bounds__(128) k_smooth_apply(SmoothArgs A) {
   const int rows = __ldg(&P.rows), ny = __ldg(&P.ny);
   const int k = (int)(n - __ldg(&P.node0));
   const int j = k / nx, i = k - j * nx;
-  const int nyw = __ldg(A.nyw + __ldg(&P.yoff) + j);
+  const int nyw = __ldg(A.nyw + __ldg(&P.woff) + j);
   const int n1 = max(0, j - nyw), n2 = min(ny - 1, j + nyw);
   const int kl = min(nxw, i), kr = min(nxw, nx - 1 - i);
   const double* wt = A.table + __ldg(&P.toff) + (long long)j * (2LL * (rows + 1) * W);
   const double* dl = wt + 2LL * rows * W;
   const double den = __ldg(dl + kl) + __ldg(dl + W + kr);
-  const double* col = A.data + __ldg(&P.goff) + i;
+  const double* col = A.data + __ldg(&P.doff) + i;
   double num = 0.0;
   for (int r = 0; r <= n2 - n1; ++r) {
     const double* w = wt + r * W;

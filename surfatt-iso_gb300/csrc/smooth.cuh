@@ -28,9 +28,12 @@ struct SmoothPeriod {
   int dmax;     // min(nxw, nx - 1): largest column offset in the table
   int rows;     // window rows of the table: 2 * max_j nyw(j) + 1, clamped to ny
   int pad;
-  long long goff;  // cell offset of the field (data and output)
+  double sigma;    // degrees
+  long long goff;  // cell offset of the period's output field
+  long long doff;  // cell offset of the period's input field
   long long xoff;  // offset of the period's longitudes
-  long long yoff;  // offset of the period's latitudes and of its per-row nyw
+  long long yoff;  // offset of the period's latitudes
+  long long woff;  // offset of the period's per-row nyw (it depends on sigma)
   long long toff;  // offset of the period's table (doubles)
   long long node0; // first node of the period in the apply kernel's flat numbering
 };
@@ -40,7 +43,7 @@ struct SmoothArgs {
   int nperiod;
   const double* lons;  // degrees
   const double* lats;  // degrees
-  const int* nyw;      // per row: int(3 sigma / cosd(lat_j) / dy), clamped to ny - 1
+  const int* nyw;      // per (period, row): int(3 sigma / cosd(lat_j) / dy), clamped to ny - 1
   const double* data;
   double* out;
   // per (period, row), W = dmax + 1: rows x W weights w[r][d], rows x W
@@ -48,7 +51,6 @@ struct SmoothArgs {
   // node clipped to kl columns on the left and kr on the right,
   // DL[kl] + DR[kr]: DL[k] = sum_r (P[r][k] - w[r][0]), DR[k] = sum_r P[r][k].
   double* table;
-  double sigma;     // degrees
   long long nodes;  // output nodes of all periods
 };
 
@@ -60,7 +62,7 @@ __host__ __device__ inline long long smooth_row_doubles(const SmoothPeriod& p) {
 // Host-side geometry of one smoothing call.
 struct SmoothPlan {
   std::vector<SmoothPeriod> per;
-  std::vector<int> nyw;        // indexed yoff + j
+  std::vector<int> nyw;        // indexed woff + j
   long long table_doubles = 0;
   long long nyw_count = 0;     // entries of nyw
   long long nodes = 0;         // output nodes of all periods
@@ -71,14 +73,15 @@ struct SmoothPlan {
 
 // Window geometry of a set of periods, computed on the host with the same
 // IEEE operations as the reference (so the integer truncations agree
-// exactly).  lons / lats: host copies, per-period offsets xoff / yoff.
-// Returns 0, or 2 (bad argument): fewer than 2 nodes on an axis,
-// non-increasing or non-uniform spacing (relative 1e-9 of the first step),
-// sigma <= 0 or not finite, |lat| >= 90, or a grid whose per-row factors
-// exceed the table kernel's shared memory.
+// exactly).  lons / lats: host copies, per-period offsets xoff / yoff;
+// goff / doff: output / input field offsets (doff NULL: the same as goff);
+// sigma: one value per period.  Returns 0, or 2 (bad argument): fewer than
+// 2 nodes on an axis, non-increasing or non-uniform spacing (relative 1e-9
+// of the first step), sigma <= 0 or not finite, |lat| >= 90, or a grid
+// whose per-row factors exceed the table kernel's shared memory.
 int smooth_plan(int nperiod, const int* nx, const int* ny, const long long* goff,
-                const long long* xoff, const long long* yoff, const double* lons,
-                const double* lats, double sigma, SmoothPlan* plan);
+                const long long* doff, const long long* xoff, const long long* yoff,
+                const double* lons, const double* lats, const double* sigma, SmoothPlan* plan);
 
 // Weight-table kernel (depends on the grid and sigma only) and apply kernel
 // (one launch each) on `st`.

@@ -50,6 +50,7 @@ EXPORTED = [
     "surfatt_srcrec_info", "surfatt_srcrec_periods", "surfatt_srcrec_stations",
     "surfatt_srcrec_station_name", "surfatt_srcrec_paths", "surfatt_srcrec_build_worklist",
     "surfatt_srcrec_worklist", "surfatt_srcrec_build_timing", "surfatt_srcrec_write_csv",
+    "surfatt_topo_metric", "surfatt_topo_sigma", "surfatt_topo_metric_timing",
     "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
     "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
     "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
@@ -373,6 +374,52 @@ def kernel_gradient_timing():
     st = L.surfatt_kernel_gradient_timing(ctypes.byref(ms), ctypes.byref(n))
     if st != OK:
         raise SurfattError(st, "kernel_gradient_timing")
+    return ms.value, n.value
+
+
+# ---------------------------------------------------------------------------
+# Surface metric from topography
+# ---------------------------------------------------------------------------
+def topo_metric(topo, lon, lat, sigma, angle=True):
+    """get_topo's per-period loop (src/grid.f90:117-145) on the GPU: topo
+    (nx, ny) km, one sigma (degrees) per period.  Returns (m11, m22, m12,
+    topo_angle), each (nperiod, nx, ny) Fortran order (angle None when not
+    asked for)."""
+    topo = _f2(topo)
+    nx, ny = topo.shape
+    sigma = _c64(np.atleast_1d(sigma))
+    P = len(sigma)
+    outs = [np.zeros((P, nx, ny), order="F") for _ in range(3)]
+    ang = np.zeros((P, nx, ny), order="F") if angle else None
+    L = lib()
+    L.surfatt_topo_metric.argtypes = [_dp, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                      _dp, _dp, _dp, _dp, _dp]
+    st = L.surfatt_topo_metric(_d(topo), nx, ny, _d(_c64(lon)), _d(_c64(lat)), P, _d(sigma),
+                               *[_d(o) for o in outs], _d(ang) if angle else None)
+    if st != OK:
+        raise SurfattError(st, "topo_metric")
+    return outs[0], outs[1], outs[2], ang
+
+
+def topo_sigma(phase_vel, periods, wavelen_factor):
+    """sigma per period of src/grid.f90:117."""
+    v, T = _c64(phase_vel), _c64(periods)
+    out = np.zeros(len(v))
+    L = lib()
+    L.surfatt_topo_sigma.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_double, _dp]
+    st = L.surfatt_topo_sigma(len(v), _d(v), _d(T), float(wavelen_factor), _d(out))
+    if st != OK:
+        raise SurfattError(st, "topo_sigma")
+    return out
+
+
+def topo_metric_timing():
+    L = lib()
+    L.surfatt_topo_metric_timing.argtypes = [_dp, _ip]
+    ms, n = ctypes.c_double(0), ctypes.c_int(0)
+    st = L.surfatt_topo_metric_timing(ctypes.byref(ms), ctypes.byref(n))
+    if st != OK:
+        raise SurfattError(st, "topo_metric_timing")
     return ms.value, n.value
 
 
