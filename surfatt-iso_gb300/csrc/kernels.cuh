@@ -100,9 +100,12 @@ inline void diag_q_arrays(float4* q, int nx, int ny, const float4** qa, const fl
   qd[0] = reinterpret_cast<const float2*>(q + 2 * D);
   qd[1] = qd[0] + D;
 }
-// Largest grid the diagonal-layout / warp-per-solve kernels take.
+// Largest grid the diagonal-layout kernel and the single-warp form of the
+// row kernel take; the row kernel's warp teams take up to kTeamMaxRows.
 constexpr int kWarpMaxRows = 128;
 constexpr int kWarpMaxCols = 4096;
+constexpr int kTeamMaxRows = 512;
+int fp32w_team(int max_ny);
 void launch_batch_fp64(const BatchArgs& a, int grid, int block, cudaStream_t st);
 void launch_batch_fp32(const BatchArgs& a, int grid, int block, cudaStream_t st);
 int batch_fp64_max_blocks_per_sm(int block);

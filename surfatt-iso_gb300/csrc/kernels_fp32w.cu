@@ -1,5 +1,6 @@
 // kernels_fp32w.cu -- FP32-factored batched solve, one warp per (period,
-// source) solve, for grids of at most 128 rows.
+// source) solve for grids of at most 128 rows, a team of up to four warps
+// (one block, 128 rows each) for grids of up to 512 rows.
 //
 // Wavefront without block barriers.  In each of the four sweeps, lane l owns
 // the logical rows v = l + 32*m (m < MB) and at step t visits the cell
@@ -25,6 +26,69 @@
 #include "warp_common.cuh"
 
 namespace sgb {
+
+// A solve's team: the NW warps of one block (NW = 1: the warp alone, one
+// warp per block).  tid runs over the team, wid is the warp's rank in it.
+template <int NW>
+struct Tm {
+  int tid, lane, wid;
+};
+
+template <int NW>
+__device__ __forceinline__ Tm<NW> this_team() {
+  Tm<NW> t;
+  t.lane = (int)(threadIdx.x & 31);
+  t.tid = NW == 1 ? t.lane : (int)threadIdx.x;
+  t.wid = NW == 1 ? 0 : (int)(threadIdx.x >> 5);
+  return t;
+}
+
+template <int NW>
+__device__ __forceinline__ void tsync() {
+  if (NW == 1) __syncwarp();
+  else __syncthreads();
+}
+
+// Every thread of the team receives thread 0's value.
+template <int NW>
+__device__ __forceinline__ int tbcast(int v) {
+  if (NW == 1) return __shfl_sync(FULL, v, 0);
+  __shared__ int b;
+  __syncthreads();
+  if (threadIdx.x == 0) b = v;
+  __syncthreads();
+  return b;
+}
+
+// Sum (a) and maxima (b, c) over the team: within each warp by the xor
+// tree, then over the warps in order (deterministic).
+template <int NW>
+__device__ __forceinline__ void tsum_max2(double& a, double& b, double& c) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(FULL, a, o);
+    b = fmax(b, __shfl_xor_sync(FULL, b, o));
+    c = fmax(c, __shfl_xor_sync(FULL, c, o));
+  }
+  if (NW == 1) return;
+  __shared__ double r[3][NW > 1 ? NW : 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    r[0][wid] = a;
+    r[1][wid] = b;
+    r[2][wid] = c;
+  }
+  __syncthreads();
+  a = 0.0;
+  b = 0.0;
+  c = 0.0;
+  for (int w = 0; w < NW; ++w) {
+    a += r[0][w];
+    b = fmax(b, r[1][w]);
+    c = fmax(c, r[2][w]);
+  }
+}
 
 
 // Workspace per warp slot: S (float4: T0, T0x, T0y, -), W (float4 adjoint
@@ -60,17 +124,18 @@ __device__ inline WSlot wcarve(double* base, size_t N) {
 
 
 // T0, T0x, T0y of every cell into S; tau initialised (1 in the frozen box).
+template <int NW>
 __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSolve& w,
-                            const WSlot& V, int lane) {
-  const int nx = P.nx, ny = P.ny;
+                            const WSlot& V, const Tm<NW>& T) {
+  const int nx = P.nx, ny = P.ny, lane = T.lane;
   const T0Src src = t0_source(w, x0, y0);
-  for (int i = lane; i < nx; i += 32) {
+  for (int i = T.tid; i < nx; i += 32 * NW) {
     const float hx = (float)((P.xs[i] - x0) * 0.5);
     V.col[i] = sinf(hx);
     V.col[nx + i] = cosf(hx);
   }
-  __syncwarp();
-  for (int j = 0; j < ny; ++j) {
+  tsync<NW>();
+  for (int j = T.wid; j < ny; j += NW) {  // rows by warp, columns by lane
     const T0Row row = t0_row(P, src, j);
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
@@ -78,7 +143,7 @@ __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSol
       V.tau[k] = w.box.has(i, j) ? 1.0f : 10.0f;
     }
   }
-  __syncwarp();
+  tsync<NW>();
 }
 
 
@@ -126,12 +191,24 @@ __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, i
 // Iterations it0 .. it1 (1-based; the reference runs 1 .. MaxIter): status
 // ST_OK and the iteration count when one of them converges, otherwise
 // ST_NOT_CONVERGED and it1.
-template <int MB, int PF>
-__device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w, int lane,
-                                    int it0, int it1, int* status_out, int* iters_out) {
-  const int nx = P.nx, ny = P.ny;
+template <int MB, int PF, int NW>
+__device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w,
+                                    const Tm<NW>& T, int it0, int it1, int* status_out,
+                                    int* iters_out) {
+  const int nx = P.nx, ny = P.ny, lane = T.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const int nsteps = nx + ny - 1;
+  // Teams: warp w owns the rows vb .. vb + 32 MB - 1.  The south neighbour
+  // of its first row is the last row of warp w-1, visited a step earlier:
+  // it comes through a shared slot (double-buffered by step parity, one
+  // team barrier per step).  The north neighbour of its last row is the
+  // first row of warp w+1, visited a step later: its old value is read from
+  // memory a step ahead (that cell is rewritten two steps later).
+  const int vb = 32 * MB * T.wid;
+  const int vtop = vb + 32 * MB - 1;
+  const bool top = NW > 1 && lane == 31 && T.wid < NW - 1;
+  const bool bot = NW > 1 && lane == 0 && T.wid > 0;
+  __shared__ float xs_val[2][NW > 1 ? NW : 1], xs_t0[2][NW > 1 ? NW : 1];
   int iter, status = ST_NOT_CONVERGED;
   for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f;
@@ -139,19 +216,35 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
       const bool last = s == 3;
+      // old tau and T0 of the cell north of the top row at step tau
+      auto north_of_top = [&](int tau, float& own, float& t0) {
+        const int u = tau - vtop;
+        own = 0.f;
+        t0 = 0.f;
+        if (u >= 0 && u < nx && vtop + 1 < ny) {
+          const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? vtop + 1 : ny - 2 - vtop);
+          own = V.tau[k];
+          t0 = reinterpret_cast<const float*>(V.S)[4 * k];
+        }
+      };
       float res[MB], t0prev[MB];
       WFwd cur[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
         t0prev[m] = 0.f;
-        wf_load<PF == 1>(cur[m], 0, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+        wf_load<PF == 1>(cur[m], 0, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
       }
+      float pn_own = 0.f, pn_t0 = 0.f;
+      if (top) north_of_top(0, pn_own, pn_t0);
       for (int t = 0; t < nsteps; ++t) {
         WFwd nxt[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m)
-          wf_load<PF == 1>(nxt[m], t + 1, lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+          wf_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box,
+                           last);
+        float qn_own = 0.f, qn_t0 = 0.f;
+        if (top) north_of_top(t + 1, qn_own, qn_t0);
         // Bands in descending order: band m's south neighbours include lane 31
         // of band m-1, whose value must still be the previous step's.  Each
         // band exchanges its values right before its visit, which keeps the
@@ -160,11 +253,21 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
 #pragma unroll
         for (int mm = 0; mm < MB; ++mm) {
           const int m = MB - 1 - mm;
-          const float south = w_below<MB>(res, m, lane), t0s = w_below<MB>(t0prev, m, lane);
-          const float north = w_above_own<MB>(nxt, m, lane), t0n = w_above_t0<MB>(nxt, m, lane);
+          float south = w_below<MB>(res, m, lane), t0s = w_below<MB>(t0prev, m, lane);
+          float north = w_above_own<MB>(nxt, m, lane), t0n = w_above_t0<MB>(nxt, m, lane);
+          if (NW > 1) {
+            if (m == 0 && bot) {
+              south = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
+              t0s = xs_t0[(t + 1) & 1][T.wid - 1];
+            }
+            if (m == MB - 1 && top) {
+              north = pn_own;
+              t0n = pn_t0;
+            }
+          }
           dds[m] = 0.f;
           if (cur[m].on) {
-            const int v = lane + 32 * m, u = t - v;
+            const int v = vb + lane + 32 * m, u = t - v;
             const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? v : ny - 1 - v);
             float nv;
             if (cur[m].frz) {
@@ -184,6 +287,10 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
             t0prev[m] = cur[m].t0;
           }
           cur[m] = nxt[m];
+          if (NW > 1 && m == MB - 1 && top) {
+            xs_val[t & 1][T.wid] = res[m];
+            xs_t0[t & 1][T.wid] = t0prev[m];
+          }
         }
         if (last) {
           // in band order (the order of the row-major visit of a lane)
@@ -193,16 +300,14 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
             lmax = fmaxf(lmax, dds[m]);
           }
         }
-        __syncwarp();
+        pn_own = qn_own;
+        pn_t0 = qn_t0;
+        tsync<NW>();
       }
     }
     // FP64 decision over the lanes' partial sums (:1091-1115)
-    double sl1 = (double)l1, smax = (double)lmax;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      sl1 += __shfl_xor_sync(FULL, sl1, o);
-      smax = fmax(smax, __shfl_xor_sync(FULL, smax, o));
-    }
+    double sl1 = (double)l1, smax = (double)lmax, unused = 0.0;
+    tsum_max2<NW>(sl1, smax, unused);
     sl1 = sl1 / (double)nx / (double)ny;
     if (fabs(sl1) < TOL_UW && smax < TOL_UW) {
       status = ST_OK;
@@ -218,14 +323,15 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
 // ---------------------------------------------------------------------------
 // Weights of Ta = src + ww*Ta_W + we*Ta_E + ws*Ta_S + wn*Ta_N (face fluxes of
 // :1348-1370 with T = tau*T0 in FP32) and 1/d per interior cell.
-__device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, int lane) {
-  const int nx = P.nx, ny = P.ny;
+template <int NW>
+__device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, const Tm<NW>& TM) {
+  const int nx = P.nx, ny = P.ny, lane = TM.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const float* T0 = reinterpret_cast<const float*>(V.S);
   const float4* PA = P.p4a;
   // T = tau*T0 rounded on its own (no contraction with the differences below)
   auto T = [&](size_t k) { return __fmul_rn(V.tau[k], T0[4 * k]); };
-  for (int j = 0; j < ny; ++j) {
+  for (int j = TM.wid; j < ny; j += NW) {  // rows by warp, columns by lane
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
       if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1) {
@@ -244,7 +350,7 @@ __device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, int lane)
       V.id[k] = id;
     }
   }
-  __syncwarp();
+  tsync<NW>();
 }
 
 struct WAdj {
@@ -278,18 +384,26 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
 // Sweeps one adjoint field (held in V.tau) to convergence: the reference's
 // absolute rule (:1429) or no change beyond the FP32 resolution of the field.
 // Neighbours outside the interior are the boundary's zeros.
-template <int MB, int PF>
-__device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src, int lane,
-                                    int* status_out, int* iters_out) {
-  const int nx = P.nx, ny = P.ny;
+template <int MB, int PF, int NW>
+__device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src,
+                                    const Tm<NW>& T, int* status_out, int* iters_out) {
+  const int nx = P.nx, ny = P.ny, lane = T.lane;
   const int nu = nx - 2, nv = ny - 2;
   const int nsteps = nu + nv - 1;
-  for (int j = 0; j < ny; ++j)
+  for (int j = T.wid; j < ny; j += NW)
     for (int i = lane; i < nx; i += 32) {
       const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
       V.tau[i + (size_t)nx * j] = in ? 100.f : 0.f;
     }
-  __syncwarp();
+  tsync<NW>();
+  // Teams: as in the forward sweeps, the first row's south value comes
+  // through a shared slot from the warp below, the last row's north value
+  // from memory a step ahead.
+  const int vb = 32 * MB * T.wid;
+  const int vtop = vb + 32 * MB - 1;
+  const bool top = NW > 1 && lane == 31 && T.wid < NW - 1;
+  const bool bot = NW > 1 && lane == 0 && T.wid > 0;
+  __shared__ float xs_val[2][NW > 1 ? NW : 1];
   int iter, status = ST_NOT_CONVERGED;
   for (iter = 1; iter <= MAXITER_JSE; ++iter) {
     float l1 = 0.f, lmax = 0.f, vmax = 0.f;
@@ -297,27 +411,39 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
       const bool last = s == 3;
+      auto north_of_top = [&](int tau) {
+        const int u = tau - vtop;
+        if (u < 0 || u >= nu || vtop + 1 >= nv) return 0.f;
+        return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
+      };
       float res[MB];
       WAdj cur[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
-        wa_load<PF == 1>(cur[m], 0, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+        wa_load<PF == 1>(cur[m], 0, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
       }
+      float pn = top ? north_of_top(0) : 0.f;
       for (int t = 0; t < nsteps; ++t) {
         WAdj nxt[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m)
-          wa_load<PF == 1>(nxt[m], t + 1, lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+          wa_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
+                           last);
+        const float qn = top ? north_of_top(t + 1) : 0.f;
         float south[MB], north[MB], nown[MB];
 #pragma unroll
         for (int m = 0; m < MB; ++m) nown[m] = nxt[m].own;
         w_from_below<MB>(res, south, lane);
         w_from_above<MB>(nown, north, lane);
+        if (NW > 1) {
+          if (bot) south[0] = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
+          if (top) north[MB - 1] = pn;
+        }
 #pragma unroll
         for (int m = 0; m < MB; ++m) {
           if (cur[m].on) {
-            const int v = lane + 32 * m, u = t - v;
+            const int v = vb + lane + 32 * m, u = t - v;
             const int k = (xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 1 + v : nv - v);
             const float west = u > 0 ? res[m] : 0.f;
             const float east = u < nu - 1 ? nown[m] : 0.f;
@@ -343,16 +469,13 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
           }
           cur[m] = nxt[m];
         }
-        __syncwarp();
+        if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
+        pn = qn;
+        tsync<NW>();
       }
     }
     double sl1 = (double)l1, smax = (double)lmax, svmax = (double)vmax;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      sl1 += __shfl_xor_sync(FULL, sl1, o);
-      smax = fmax(smax, __shfl_xor_sync(FULL, smax, o));
-      svmax = fmax(svmax, __shfl_xor_sync(FULL, svmax, o));
-    }
+    tsum_max2<NW>(sl1, smax, svmax);
     sl1 = sl1 / (double)(nx * ny);
     if ((fabs(sl1) < TOL_JSE && smax < TOL_JSE) || smax <= svmax * 0x1p-21) {
       status = ST_OK;
@@ -406,18 +529,20 @@ __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, d
 // ---------------------------------------------------------------------------
 // Receiver times, misfit, outlier weights (src/measadj.f90:71-72, 82-84);
 // returns the status (ST_BAD_ARG for a receiver outside the grid).
+template <int NW>
 __device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const WSlot& V, int s,
-                                  int r0, int nr, int lane, int st) {
+                                  int r0, int nr, const Tm<NW>& T, int st) {
   int bad = 0;
-  for (int r = lane; r < nr; r += 32) {
+  for (int r = T.tid; r < nr; r += 32 * NW) {
     double v = 0.0;
     if (!w_interp(P, V, A.recx[r0 + r], A.recy[r0 + r], &v)) bad = 1;
     A.tekio[r0 + r] = v;
     A.tt_fwd[A.path[r0 + r]] = v;
   }
-  bad = __any_sync(FULL, bad);
-  __syncwarp();
-  if (lane == 0) {
+  if (NW == 1) bad = __any_sync(FULL, bad);
+  else bad = __syncthreads_or(bad);
+  tsync<NW>();
+  if (T.tid == 0) {
     double ssum = 0;
     for (int r = 0; r < nr; ++r) {
       const double d = A.tekio[r0 + r] - A.tt[r0 + r];
@@ -430,22 +555,23 @@ __device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const 
       A.wgt_eff[r0 + r] = wt;
     }
   }
-  __syncwarp();
+  tsync<NW>();
   return (bad && st == ST_OK) ? ST_BAD_ARG : st;
 }
 
 // Adjoint coefficients and the scaled sources of nf fields: weight*(tekio-tt)
 // (src/measadj.f90:88) and -weight (:102), splat bilinearly over the cell
 // area (src/eikon_solver_2d.f90:1328-1336) and scaled by 1/d.
+template <int NW>
 __device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, const WSlot& V,
-                                    int r0, int nr, int nf, int lane, int st) {
+                                    int r0, int nr, int nf, const Tm<NW>& T, int st) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
-  w_adj_setup(P, V, lane);
+  w_adj_setup<NW>(P, V, T);
   for (int f = 0; f < nf; ++f)
-    for (size_t k = lane; k < N; k += 32) V.src[f][k] = 0.f;
-  __syncwarp();
-  if (lane == 0) {
+    for (size_t k = T.tid; k < N; k += 32 * NW) V.src[f][k] = 0.f;
+  tsync<NW>();
+  if (T.tid == 0) {
     for (int f = 0; f < nf && st != ST_BAD_ARG; ++f)
       for (int r = 0; r < nr; ++r) {
         const double wt = A.wgt_eff[r0 + r];
@@ -470,21 +596,22 @@ __device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, cons
           sf[k + nx + 1] += (float)(sv * (double)r1 * (double)r2 / den) * V.id[k + nx + 1];
       }
   }
-  st = __shfl_sync(FULL, st, 0);
-  __syncwarp();
+  st = tbcast<NW>(st);
+  tsync<NW>();
   return st;
 }
 
 // Mask (src/eikon_solver_2d.f90:1449-1467) and the kernel slot adj/svel**k
 // (src/acqui.f90:314-315) of adjoint field f, FP32 here, summed per period
 // in FP64.
+template <int NW>
 __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlot& V,
-                              const WSolve& w, int s, int f, int lane) {
-  const int nx = P.nx, ny = P.ny;
+                              const WSolve& w, int s, int f, const Tm<NW>& T) {
+  const int nx = P.nx, ny = P.ny, lane = T.lane;
   float* out = reinterpret_cast<float*>(f == 0 ? A.kcontrib : A.kcontrib_den) + A.kslot[s];
   // groups of G cells: loads first, then stores (as in w_adj_setup)
   constexpr int G = 4;
-  for (int j = 0; j < ny; ++j)
+  for (int j = T.wid; j < ny; j += NW)  // rows by warp
     for (int i0 = lane; i0 < nx; i0 += 32 * G) {
       float isv[G], ta[G];
 #pragma unroll
@@ -505,7 +632,7 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlo
         if (i < nx) out[i + (size_t)nx * j] = w.mbox.has(i, j) ? 0.f : ta[g] * isv[g];
       }
     }
-  __syncwarp();
+  tsync<NW>();
 }
 
 // ---------------------------------------------------------------------------
@@ -547,17 +674,18 @@ __host__ __device__ inline int w_items_for_mode(int mode) {
   return kFwdItems + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
 }
 
-template <int MB, int PF, int MINW>
-__global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
-  const int lane = threadIdx.x & 31;
+template <int MB, int PF, int MINW, int NW>
+__global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A) {
+  const Tm<NW> T = this_team<NW>();
+  const int lane = T.lane;
   const bool cut = A.items > 1;
   const int nitem = cut ? A.items : 1;
   float* kf = reinterpret_cast<float*>(A.kcontrib);
   float* kdf = reinterpret_cast<float*>(A.kcontrib_den);
   for (;;) {
     int q = 0;
-    if (lane == 0) q = atomicAdd(A.queue, 1);
-    q = __shfl_sync(FULL, q, 0);
+    if (T.tid == 0) q = atomicAdd(A.queue, 1);
+    q = tbcast<NW>(q);
     if (q >= A.nsolve * nitem) break;
     const int item = q / A.nsolve;
     const int s = A.order[q % A.nsolve];
@@ -570,13 +698,19 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
         d = ld_acquire(ss + SS_DONE);
         ++it;
       }
-      if (d < 0) continue;  // the solve failed in an earlier item
-      if (d < item) {       // wait limit: report and drop the solve
-        if (lane == 0) {
+      // every thread acquired the state itself; the team takes one decision
+      bool failed = d < 0, late = d >= 0 && d < item;
+      if (NW > 1) {
+        failed = __syncthreads_or(failed);
+        late = !failed && __syncthreads_or(late);
+      }
+      if (failed) continue;  // the solve failed in an earlier item
+      if (late) {            // wait limit: report and drop the solve
+        if (T.tid == 0) {
           A.status[s] = ST_TIMEOUT;
           st_release(ss + SS_DONE, -1);
         }
-        __syncwarp();
+        tsync<NW>();
         continue;
       }
     }
@@ -593,7 +727,7 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
     auto mark = [&](int ph) {
       if (pc) {
         const long long c1 = clock64();
-        if (lane == 0) atomicAdd(pc + ph, (unsigned long long)(c1 - c0));
+        if (T.tid == 0) atomicAdd(pc + ph, (unsigned long long)(c1 - c0));
         c0 = c1;
       }
     };
@@ -601,10 +735,10 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
     auto finish_item = [&](int done) {
       if (cut) {
         __threadfence();
-        __syncwarp();
-        if (lane == 0) st_release(ss + SS_DONE, done);
+        tsync<NW>();
+        if (T.tid == 0) st_release(ss + SS_DONE, done);
       }
-      __syncwarp();
+      tsync<NW>();
     };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
     const int nf = A.mode == 3 ? 2 : 1;
@@ -614,29 +748,29 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
     int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0;
     if (cut && first > 0) {
       int v0 = 0, v1 = 0, v2 = 0, v3 = 0;
-      if (lane == 0) {
+      if (T.tid == 0) {
         v0 = ss[SS_FIT];
         v1 = ss[SS_FST];
         v2 = ss[SS_ST];
         v3 = ss[SS_ITS0];
       }
-      fit = __shfl_sync(FULL, v0, 0);
-      fst = __shfl_sync(FULL, v1, 0);
-      st = __shfl_sync(FULL, v2, 0);
-      its0 = __shfl_sync(FULL, v3, 0);
+      fit = tbcast<NW>(v0);
+      fst = tbcast<NW>(v1);
+      st = tbcast<NW>(v2);
+      its0 = tbcast<NW>(v3);
     }
     if (first == 0 && w.status != ST_OK) {
-      for (int r = lane; r < nr; r += 32) {
+      for (int r = T.tid; r < nr; r += 32 * NW) {
         A.tekio[r0 + r] = 0.0;
         A.wgt_eff[r0 + r] = 0.0;
         A.tt_fwd[A.path[r0 + r]] = 0.0;
       }
       if (A.mode >= 2)
-        for (size_t kk = lane; kk < N; kk += 32) {
+        for (size_t kk = T.tid; kk < N; kk += 32 * NW) {
           kf[A.kslot[s] + kk] = 0.f;
           if (A.mode == 3) kdf[A.kslot[s] + kk] = 0.f;
         }
-      if (lane == 0) {
+      if (T.tid == 0) {
         A.chi[s] = 0.0;
         A.status[s] = w.status;
         A.fwd_iters[s] = 0;
@@ -650,19 +784,19 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
     // (k+1)*kSplitIter, the last one (a whole solve: all) up to MaxIter,
     // unless an earlier item converged
     if (first == 0) {
-      w_t0(P, x0, y0, w, V, lane);
+      w_t0<NW>(P, x0, y0, w, V, T);
       mark(PH_SETUP);
     }
     if (first < kFwdItems && (first == 0 || (fst != ST_OK && fit < MAXITER_UW))) {
       const int it0 = first == 0 ? 1 : fit + 1;
       const int it1 = (cut && first < kFwdItems - 1) ? (first + 1) * kSplitIter : MAXITER_UW;
       int n = 0;
-      w_fwd_sweeps<MB, PF>(P, V, w, lane, it0, it1, &fst, &n);
+      w_fwd_sweeps<MB, PF, NW>(P, V, w, T, it0, it1, &fst, &n);
       fit = n;
       mark(PH_FWD);
     }
     if (cut && first < kFwdItems - 1) {
-      if (lane == 0) {
+      if (T.tid == 0) {
         ss[SS_FIT] = fit;
         ss[SS_FST] = fst;
       }
@@ -670,18 +804,18 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
       continue;
     }
     if (first <= kFwdItems - 1) {
-      if (A.fwd_updates && lane == 0) {
+      if (A.fwd_updates && T.tid == 0) {
         const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
         A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
       }
-      st = w_receivers(A, P, V, s, r0, nr, lane, fst);
+      st = w_receivers<NW>(A, P, V, s, r0, nr, T, fst);
       mark(PH_RECV);
       if (A.mode >= 2) {
-        st = w_adj_sources(A, P, V, r0, nr, nf, lane, st);
+        st = w_adj_sources<NW>(A, P, V, r0, nr, nf, T, st);
         mark(PH_ADJ_SETUP);
       }
       if (cut && A.mode >= 2) {
-        if (lane == 0) {
+        if (T.tid == 0) {
           ss[SS_FIT] = fit;
           ss[SS_ST] = st;
         }
@@ -694,15 +828,15 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
     const int f1 = A.mode >= 2 ? (cut ? lastit - kFwdItems : nf - 1) : -1;
     for (int f = f0; f <= f1; ++f) {
       int ast = ST_OK, n = 0;
-      w_adj_sweeps<MB, PF>(P, V, f ? V.src[1] : V.src[0], lane, &ast, &n);
+      w_adj_sweeps<MB, PF, NW>(P, V, f ? V.src[1] : V.src[0], T, &ast, &n);
       mark(PH_ADJ);
       if (f == 0) its0 = n; else its1 = n;
       if (ast != ST_OK && st == ST_OK) st = ast;
-      w_slot(A, P, V, w, s, f, lane);
+      w_slot<NW>(A, P, V, w, s, f, T);
       mark(PH_SLOT);
     }
     if (cut && lastit < nitems_mode - 1) {
-      if (lane == 0) {
+      if (T.tid == 0) {
         ss[SS_ST] = st;
         ss[SS_ITS0] = its0;
       }
@@ -710,7 +844,7 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32w(BatchArgs A) {
       continue;
     }
     // the solve's last item: its outputs
-    if (lane == 0) {
+    if (T.tid == 0) {
       A.status[s] = st;
       A.fwd_iters[s] = fit;
       A.adj_iters[s] = its0 > its1 ? its0 : its1;
@@ -734,53 +868,68 @@ int fp32w_variant_count() { return kFp32wVariants; }
 bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2; }
 int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
 
-template <int MB, int PF, int MINW>
+template <int MB, int PF, int MINW, int NW>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
-  k_batch_fp32w<MB, PF, MINW><<<grid, 32, 0, st>>>(a);
+  k_batch_fp32w<MB, PF, MINW, NW><<<grid, 32 * NW, 0, st>>>(a);
 }
 
-template <int MB, int PF, int MINW>
+template <int MB, int PF, int MINW, int NW>
 static int occupancy_w() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF, MINW>, 32, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF, MINW, NW>, 32 * NW, 0);
   return n;
 }
 
-template <int MB>
+template <int MB, int NW>
 static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st) {
   switch (variant) {
     case 0:
-    case 1: launch_w<MB, 1, 8>(a, grid, st); break;
-    case 2: launch_w<MB, 0, 12>(a, grid, st); break;
-    default: launch_w<MB, 0, 8>(a, grid, st); break;
+    case 1: launch_w<MB, 1, 8, NW>(a, grid, st); break;
+    case 2: launch_w<MB, 0, 12, NW>(a, grid, st); break;
+    default: launch_w<MB, 0, 8, NW>(a, grid, st); break;
   }
 }
 
-template <int MB>
+template <int MB, int NW>
 static int occupancy_mb(int variant) {
   switch (variant) {
     case 0:
-    case 1: return occupancy_w<MB, 1, 8>();
-    case 2: return occupancy_w<MB, 0, 12>();
-    default: return occupancy_w<MB, 0, 8>();
+    case 1: return occupancy_w<MB, 1, 8, NW>();
+    case 2: return occupancy_w<MB, 0, 12, NW>();
+    default: return occupancy_w<MB, 0, 8, NW>();
   }
 }
 
+// Grids of more than 128 rows: teams of fp32w_team(ny) warps of four bands.
+int fp32w_team(int max_ny) { return max_ny <= 32 * 4 ? 1 : (max_ny + 127) / 128; }
+
 void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st) {
   switch (bands) {
-    case 1: launch_mb<1>(a, grid, variant, st); break;
-    case 2: launch_mb<2>(a, grid, variant, st); break;
-    case 3: launch_mb<3>(a, grid, variant, st); break;
-    default: launch_mb<4>(a, grid, variant, st); break;
+    case 1: launch_mb<1, 1>(a, grid, variant, st); break;
+    case 2: launch_mb<2, 1>(a, grid, variant, st); break;
+    case 3: launch_mb<3, 1>(a, grid, variant, st); break;
+    case 4: launch_mb<4, 1>(a, grid, variant, st); break;
+    default:
+      switch (fp32w_team(32 * bands)) {
+        case 2: launch_mb<4, 2>(a, grid, variant, st); break;
+        case 3: launch_mb<4, 3>(a, grid, variant, st); break;
+        default: launch_mb<4, 4>(a, grid, variant, st); break;
+      }
   }
 }
 
 int batch_fp32w_max_blocks_per_sm(int bands, int variant) {
   switch (bands) {
-    case 1: return occupancy_mb<1>(variant);
-    case 2: return occupancy_mb<2>(variant);
-    case 3: return occupancy_mb<3>(variant);
-    default: return occupancy_mb<4>(variant);
+    case 1: return occupancy_mb<1, 1>(variant);
+    case 2: return occupancy_mb<2, 1>(variant);
+    case 3: return occupancy_mb<3, 1>(variant);
+    case 4: return occupancy_mb<4, 1>(variant);
+    default:
+      switch (fp32w_team(32 * bands)) {
+        case 2: return occupancy_mb<4, 2>(variant);
+        case 3: return occupancy_mb<4, 3>(variant);
+        default: return occupancy_mb<4, 4>(variant);
+      }
   }
 }
 

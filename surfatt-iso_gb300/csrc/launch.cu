@@ -32,10 +32,9 @@ std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
     return c;
   }
   if (sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)
-  {
     for (int v = 0; v < fp32d_variant_count(); ++v) c.push_back({KK_FP32_DIAG, v});
+  if (sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols)
     for (int v = 0; v < fp32w_variant_count(); ++v) c.push_back({KK_FP32_WARP, v});
-  }
   if (sh.max_diag <= kFp32MaxThreads) c.push_back({KK_FP32_BLOCK, 0});
   return c;
 }
@@ -51,15 +50,18 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.block = 128;
     p.per_sm = batch_fp64_max_blocks_per_sm(p.block);
     p.ws_doubles = batch_fp64_ws_doubles(sh.max_cells);
-  } else if ((force.kind == KK_FP32_WARP || force.kind == KK_FP32_DIAG) &&
-             !(sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)) {
-    return ST_BAD_ARG;  // the warp kernels hold at most 128 rows
-  } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= kWarpMaxRows &&
-             sh.max_nx <= kWarpMaxCols) {
-    // one warp per solve, lanes own the rows
+  } else if ((force.kind == KK_FP32_DIAG &&
+              !(sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)) ||
+             (force.kind == KK_FP32_WARP &&
+              !(sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols))) {
+    return ST_BAD_ARG;  // the diagonal kernel holds 128 rows, the row kernel 512
+  } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= kTeamMaxRows &&
+             sh.max_nx <= kWarpMaxCols &&
+             (force.kind != KK_FP32_DIAG || sh.max_ny <= kWarpMaxRows)) {
+    // one warp (a team of warps above 128 rows) per solve, lanes own the rows
     // automatic: the row-per-lane kernel (the faster on the measured shapes)
     p.kind = force.kind == KK_FP32_DIAG ? KK_FP32_DIAG : KK_FP32_WARP;
-    p.block = 32;
+    p.block = p.kind == KK_FP32_WARP ? 32 * fp32w_team(sh.max_ny) : 32;
     p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
     const int nvar = p.kind == KK_FP32_WARP ? fp32w_variant_count() : fp32d_variant_count();

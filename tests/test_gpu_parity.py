@@ -221,10 +221,51 @@ def test_engine_fp32_mode2_odd_grid(sg, oracle):
     _engine_vs_oracle(sg, oracle, pb, 2, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
 
 
-def test_engine_fp32_block_kernel_tall_grids(sg, oracle):
-    """Grids taller than 128 rows use the one-block-per-solve FP32 kernel."""
+def test_engine_fp32_tall_grids(sg, oracle):
+    """Grids taller than 128 rows: warp teams (automatic) and the
+    one-block-per-solve kernel (forced) both match the oracle."""
     pb = W.config4(nsrc=4, nperiod=3, nmax=168, nmin=48, span_deg=2.0)
     _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
+    ref = oracle.gradient_eval(pb, mode=3, nthreads=8)
+    st, kv, out = _run_kernel(sg, pb, 3, 1, -1)
+    assert st == sg.OK and kv["kind"] == 1
+    assert rel_pointwise(out["tt_fwd"], ref["tt_fwd"]) <= TT_TOL_F32
+    assert rel_max(out["adj_s"], ref["adj_s"]) <= KER_TOL_F32
+
+
+@pytest.mark.parametrize("nx,ny", [(60, 200), (150, 257), (96, 384), (40, 512)])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_fp32_warp_teams(sg, oracle, nx, ny, variant):
+    """Warp teams (2 to 4 warps of 128 rows): every variant gives the same
+    bits and matches the oracle within the FP32 tolerances."""
+    pb = W.flat_case(nx=nx, ny=ny, d=0.02, nsta=4, nperiod=1, mode=3, seed=40 + ny)
+    st0, kv0, base = _run_kernel(sg, pb, 3, 2, 0)
+    st, kv, o = _run_kernel(sg, pb, 3, 2, variant)
+    assert st0 == st == sg.OK and kv == dict(kind=2, variant=variant)
+    assert np.array_equal(o["tt_fwd"], base["tt_fwd"])
+    assert np.array_equal(o["adj_s"], base["adj_s"])
+    assert np.array_equal(o["adj_density"], base["adj_density"])
+    if variant == 0:
+        ref = oracle.gradient_eval(pb, mode=3, nthreads=8)
+        assert np.all(o["status"] == ref["status"])
+        assert rel_pointwise(o["tt_fwd"], ref["tt_fwd"]) <= TT_TOL_F32
+        assert rel_max(o["adj_s"], ref["adj_s"]) <= KER_TOL_F32
+        assert rel_max(o["adj_density"], ref["adj_density"]) <= KER_TOL_F32
+
+
+def test_fp32_team_batch_small_grids_unchanged(sg):
+    """In a batch that needs warp teams (one tall grid), the solves on small
+    grids give the bits they give alone (single warps)."""
+    pb = W.config4(nsrc=5, nperiod=3, nmax=200, nmin=48, span_deg=2.0, seed=41)
+    assert int(np.max(pb.ny)) > 128 and int(np.min(pb.ny)) <= 128
+    eng = sg.Engine(0)
+    full = eng.evaluate(pb, mode=3, precision=sg.PREC_FP32)
+    small = [s for s in range(pb.nsolve) if pb.ny[pb.pidx[s]] <= 128][:3]
+    for s in small:
+        one = eng.evaluate(pb.subset([s]), mode=3, precision=sg.PREC_FP32)
+        r0, nr = int(pb.rec_off[s]), int(pb.nrec[s])
+        assert np.array_equal(one["tt_fwd"], full["tt_fwd"][pb.path[r0:r0 + nr]])
+    eng.close()
 
 
 def test_engine_uneven_grids(sg, oracle):
@@ -287,11 +328,22 @@ def test_fp32_warp_variants(sg, oracle, variant):
     eng.close()
 
 
-def test_forced_warp_kernel_rejects_tall_grid(sg):
-    pb = W.flat_case(nx=40, ny=140, nsta=3, nperiod=1, mode=2, seed=32)
+def test_forced_kernels_reject_too_tall_grids(sg):
+    """The row kernel takes 512 rows (teams), the diagonal kernel 128."""
+    pb = W.flat_case(nx=20, ny=520, d=0.01, nsta=3, nperiod=1, mode=2, seed=32)
     eng = sg.Engine(0)
     eng.load(pb)
     eng.set_kernel(sg.PREC_FP32, kind=2)
+    with pytest.raises(sg.SurfattError):
+        eng.run(2, sg.PREC_FP32)
+    eng.set_kernel(sg.PREC_FP32)
+    eng.run(2, sg.PREC_FP32)
+    assert eng.sync() == sg.OK
+    eng.close()
+    pb = W.flat_case(nx=40, ny=140, nsta=3, nperiod=1, mode=2, seed=32)
+    eng = sg.Engine(0)
+    eng.load(pb)
+    eng.set_kernel(sg.PREC_FP32, kind=3)
     with pytest.raises(sg.SurfattError):
         eng.run(2, sg.PREC_FP32)
     eng.set_kernel(sg.PREC_FP32)
