@@ -518,6 +518,7 @@ struct surfatt_engine {
   bool smoothed = false;
   int sm_launches = 0;         // kernel launches of the last smoothing
   cudaEvent_t evs0 = nullptr, evs1 = nullptr;
+  ClassStreams cs;  // side streams of the FP32 row kernel's team classes
   int grid = 0, block = 128, per_sm = 0, last_block = 0, last_kind = 0, last_pf = 0;
   size_t last_smem = 0;
   KernelChoice tuned[2];  // per precision; -1 fields: automatic
@@ -610,7 +611,9 @@ surfatt_status_t surfatt_engine_create(surfatt_engine_t** out, int device, size_
   if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess ||
       cudaEventCreate(&e->evk0) != cudaSuccess || cudaEventCreate(&e->evk1) != cudaSuccess ||
-      cudaEventCreate(&e->evs0) != cudaSuccess || cudaEventCreate(&e->evs1) != cudaSuccess) {
+      cudaEventCreate(&e->evs0) != cudaSuccess || cudaEventCreate(&e->evs1) != cudaSuccess ||
+      e->cs.create() != ST_OK) {
+    e->cs.destroy();
     delete e;
     return SURFATT_CUDA_ERROR;
   }
@@ -630,6 +633,7 @@ void surfatt_engine_destroy(surfatt_engine_t* e) {
   cudaEventDestroy(e->evk1);
   cudaEventDestroy(e->evs0);
   cudaEventDestroy(e->evs1);
+  e->cs.destroy();
   cudaStreamDestroy(e->st);
   delete e;
 }
@@ -670,10 +674,14 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   for (int r = 0; r < nrec_total; ++r)
     if (pb->path[r] < 0 || pb->path[r] >= pb->npath) return SURFATT_BAD_ARG;
   e->nrec_total = nrec_total;
-  // processing order: largest grids first (longest-processing-time first)
+  // processing order: by team class of the FP32 row kernel (the class of
+  // the tallest grids first, each class contiguous), then largest grids
+  // first (longest-processing-time first)
   e->order.resize(ns);
   std::iota(e->order.begin(), e->order.end(), 0);
   std::stable_sort(e->order.begin(), e->order.end(), [&](int a, int b) {
+    const int ka = team_class_key(e->ny[e->pidx[a]]), kb = team_class_key(e->ny[e->pidx[b]]);
+    if (ka != kb) return ka > kb;
     return (long long)e->nx[e->pidx[a]] * e->ny[e->pidx[a]] >
            (long long)e->nx[e->pidx[b]] * e->ny[e->pidx[b]];
   });
@@ -741,7 +749,7 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
        up(e, e->d_adjd, (double*)nullptr, NC) | up(e, e->d_status, (int*)nullptr, ns) |
        up(e, e->d_fit, (int*)nullptr, ns) | up(e, e->d_ait, (int*)nullptr, ns) |
        up(e, e->d_fupd, (double*)nullptr, ns) | up(e, e->d_aupd, (double*)nullptr, ns) |
-       up(e, e->d_queue, (int*)nullptr, 1);
+       up(e, e->d_queue, (int*)nullptr, kTeamClasses);
   if (r & SURFATT_CUDA_ERROR) return SURFATT_CUDA_ERROR;
   if (r) return SURFATT_OOM;
   // per-period descriptors
@@ -820,7 +828,8 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, const KernelChoice& fo
                    bool graph = false) {
   CK(cudaSetDevice(e->device));
   EvalShape sh;
-  sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
+  sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath,
+                e->pidx.data());
   LaunchPlan plan;
   int r = plan_evaluation(sh, prec, e->device, 0, &plan, force);
   if (r) return (surfatt_status_t)r;
@@ -882,7 +891,7 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, const KernelChoice& fo
       cudaGraph_t gr = nullptr;
       CK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeRelaxed));
       const int n = enqueue_evaluation(sh, dev, plan, mode, prec, e->d_ws.as<double>(),
-                                       e->d_queue.as<int>(), e->st, e->evk0, e->evk1);
+                                       e->d_queue.as<int>(), e->st, e->evk0, e->evk1, &e->cs);
       const cudaError_t ce = cudaStreamEndCapture(e->st, &gr);
       if (n < 0 || ce != cudaSuccess) {
         if (gr) cudaGraphDestroy(gr);
@@ -909,7 +918,7 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, const KernelChoice& fo
   } else {
     CK(cudaEventRecord(e->ev0, e->st));
     const int n = enqueue_evaluation(sh, dev, plan, mode, prec, e->d_ws.as<double>(),
-                                     e->d_queue.as<int>(), e->st, e->evk0, e->evk1);
+                                     e->d_queue.as<int>(), e->st, e->evk0, e->evk1, &e->cs);
     if (n < 0) return -n;
     CK(cudaEventRecord(e->ev1, e->st));
     e->launches = n;
@@ -980,7 +989,8 @@ surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* e, surfatt_mode_t mod
   if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
   const int p = prec == SURFATT_PREC_FP64 ? 0 : 1;
   EvalShape sh;
-  sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath);
+  sh.from_grids(e->nx.data(), e->ny.data(), e->goff.data(), e->nperiod, e->nsolve, e->npath,
+                e->pidx.data());
   double best = 1e300;
   KernelChoice bc;
   // one warm-up and one timed evaluation of a candidate

@@ -6,8 +6,10 @@
 
 namespace sgb {
 
+int team_class_key(int ny) { return std::min(fp32w_team(ny), kTeamClasses + 1); }
+
 void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goffs, int np, int ns,
-                           int npth) {
+                           int npth, const int* pidx) {
   nperiod = np;
   nsolve = ns;
   npath = npth;
@@ -23,6 +25,14 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
     max_pitched = std::max(max_pitched, (long long)batch_fp32_pitch(nxs[p]) * nys[p]);
     max_dcells = std::max(max_dcells, diag_cells(nxs[p], nys[p]));
   }
+  for (int c = 0; c < kTeamClasses; ++c) team_count[c] = team_max_ny[c] = 0;
+  if (pidx)
+    for (int s = 0; s < ns; ++s) {
+      const int y = nys[pidx[s]], c = team_class_key(y) - 1;
+      if (c >= kTeamClasses) continue;  // taller than any team
+      ++team_count[c];
+      team_max_ny[c] = std::max(team_max_ny[c], y);
+    }
 }
 
 std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
@@ -85,25 +95,78 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.ws_doubles = batch_fp32_ws_doubles(sh.max_cells);
   }
   if (p.per_sm < 1) p.per_sm = 1;
-  p.grid = nsm * p.per_sm;
-  if (max_grid > 0) p.grid = std::min(p.grid, max_grid);
-  const int units = std::max(1, sh.nsolve) * (p.cut ? fp32w_items_for_mode(3) : 1);
-  const int need = (units + p.slots_per_block - 1) / p.slots_per_block;
-  p.grid = std::max(1, std::min(p.grid, need));
+  const int units_per_solve = p.cut ? fp32w_items_for_mode(3) : 1;
+  auto grid_for = [&](int per_sm, int nsolve) {
+    int g = nsm * std::max(1, per_sm);
+    if (max_grid > 0) g = std::min(g, max_grid);
+    const int need = (std::max(1, nsolve) * units_per_solve + p.slots_per_block - 1) /
+                     p.slots_per_block;
+    return std::max(1, std::min(g, need));
+  };
+  p.grid = grid_for(p.per_sm, sh.nsolve);
+  // several team classes: one launch per class (the processing order holds
+  // the classes contiguously, the largest team first)
+  int nonempty = 0, counted = 0;
+  for (int c = 0; c < kTeamClasses; ++c) {
+    nonempty += sh.team_count[c] > 0;
+    counted += sh.team_count[c];
+  }
+  if (p.kind == KK_FP32_WARP && nonempty > 1 && counted == sh.nsolve) {
+    p.classes = 0;
+    p.grid = 0;
+    int off = 0;
+    for (int c = kTeamClasses - 1; c >= 0; --c) {
+      if (sh.team_count[c] == 0) continue;
+      const int k = p.classes++;
+      p.class_solves[k] = sh.team_count[c];
+      p.class_off[k] = off;
+      p.class_bands[k] = fp32w_bands(sh.team_max_ny[c]);
+      p.class_grid[k] =
+          grid_for(batch_fp32w_max_blocks_per_sm(p.class_bands[k], p.pf), sh.team_count[c]);
+      p.grid += p.class_grid[k];
+      off += sh.team_count[c];
+    }
+  }
   *plan = p;
   return ST_OK;
 }
 
 long long plan_ws_doubles(const LaunchPlan& plan, int nsolve) {
   const long long n = std::max(1, nsolve);
+  // (a split plan's grid is the sum of its class grids: disjoint slots)
   const long long slots = plan.cut ? n : (long long)plan.grid * plan.slots_per_block;
   const long long state = plan.cut ? (n * kSolveStateInts + 1) / 2 : 0;
   return slots * plan.ws_doubles + state;
 }
 
+int ClassStreams::create() {
+  for (int i = 0; i < kTeamClasses - 1; ++i)
+    if (cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return ST_CUDA_ERROR;
+    }
+  if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return ST_CUDA_ERROR;
+  }
+  return ST_OK;
+}
+
+void ClassStreams::destroy() {
+  for (int i = 0; i < kTeamClasses - 1; ++i) {
+    if (side[i]) cudaStreamDestroy(side[i]);
+    if (join[i]) cudaEventDestroy(join[i]);
+    side[i] = nullptr;
+    join[i] = nullptr;
+  }
+  if (fork) cudaEventDestroy(fork);
+  fork = nullptr;
+}
+
 int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan& plan, int mode,
                        int prec, double* ws, int* queue, cudaStream_t st, cudaEvent_t ev_k0,
-                       cudaEvent_t ev_k1) {
+                       cudaEvent_t ev_k1, const ClassStreams* cs) {
   BatchArgs A = dev.args;
   A.mode = mode;
   A.ws = ws;
@@ -123,7 +186,8 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
       return -ST_CUDA_ERROR;
   }
   int launches = 0;
-  if (cudaMemsetAsync(queue, 0, sizeof(int), st) != cudaSuccess) return -ST_CUDA_ERROR;
+  if (cudaMemsetAsync(queue, 0, std::max(1, plan.classes) * sizeof(int), st) != cudaSuccess)
+    return -ST_CUDA_ERROR;
   if (A.phase_cycles &&
       cudaMemsetAsync(A.phase_cycles, 0, PH_COUNT * sizeof(unsigned long long), st) != cudaSuccess)
     return -ST_CUDA_ERROR;
@@ -141,7 +205,30 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
       cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
   if (ev_k0) cudaEventRecordWithFlags(ev_k0, st, ev_flags);
   (void)prec;
-  if (sh.nsolve > 0) {
+  if (sh.nsolve > 0 && plan.classes > 1) {
+    // class k > 0 on side stream k - 1 (forked after the resets above), the
+    // largest team's class on `st`, launched first
+    if (cs && cudaEventRecord(cs->fork, st) != cudaSuccess) return -ST_CUDA_ERROR;
+    long long slot0 = 0;
+    for (int k = 0; k < plan.classes; ++k) {
+      BatchArgs C = A;
+      C.order = A.order + plan.class_off[k];
+      C.nsolve = plan.class_solves[k];
+      C.queue = queue + k;
+      if (!plan.cut) C.ws = ws + slot0 * plan.ws_doubles;  // disjoint block slots
+      slot0 += plan.class_grid[k];
+      cudaStream_t sk = st;
+      if (cs && k > 0) {
+        sk = cs->side[k - 1];
+        if (cudaStreamWaitEvent(sk, cs->fork, 0) != cudaSuccess) return -ST_CUDA_ERROR;
+      }
+      launch_batch_fp32w(C, plan.class_grid[k], plan.class_bands[k], plan.pf, sk);
+      ++launches;
+      if (cs && k > 0 && (cudaEventRecord(cs->join[k - 1], sk) != cudaSuccess ||
+                          cudaStreamWaitEvent(st, cs->join[k - 1], 0) != cudaSuccess))
+        return -ST_CUDA_ERROR;
+    }
+  } else if (sh.nsolve > 0) {
     if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_BLOCK) launch_batch_fp32(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_WARP) launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);

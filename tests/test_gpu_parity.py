@@ -268,6 +268,39 @@ def test_fp32_team_batch_small_grids_unchanged(sg):
     eng.close()
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_fp32_team_classes(sg, oracle, variant):
+    """A batch of three team classes (grids of 48 to 304 rows) runs as one
+    concurrent launch per class; every solve gives the bits it gives as
+    the only solve of its evaluation, in every variant, and the batch meets
+    the FP32 tolerances against the oracle."""
+    pb = W.config4(nsrc=4, nperiod=5, nmax=300, nmin=48, span_deg=2.0, seed=42)
+    teams = {1 if n <= 128 else (int(n) + 127) // 128 for n in pb.ny}
+    assert teams == {1, 2, 3}
+    eng = sg.Engine(0)
+    eng.load(pb)
+    eng.set_kernel(sg.PREC_FP32, kind=2, variant=variant)
+    eng.run(3, sg.PREC_FP32)
+    assert eng.sync() == sg.OK
+    assert eng.timing()[2] == 3 + 3   # three class launches, two kernel sums, misfit
+    full = eng.results()
+    eng.close()
+    assert np.all(full["status"] == sg.OK)
+    for p in range(pb.nperiod):
+        s = int(np.flatnonzero(pb.pidx == p)[0])
+        st, _, one = _run_kernel(sg, pb.subset([s]), 3, 2, variant)
+        r0, nr = int(pb.rec_off[s]), int(pb.nrec[s])
+        assert st == sg.OK
+        assert np.array_equal(one["tt_fwd"], full["tt_fwd"][pb.path[r0:r0 + nr]])
+        assert one["fwd_iters"][0] == full["fwd_iters"][s]
+        assert one["adj_iters"][0] == full["adj_iters"][s]
+    if variant == 0:
+        ref = oracle.gradient_eval(pb, mode=3, nthreads=8)
+        assert rel_pointwise(full["tt_fwd"], ref["tt_fwd"]) <= TT_TOL_F32
+        assert rel_max(full["adj_s"], ref["adj_s"]) <= KER_TOL_F32
+        assert rel_max(full["adj_density"], ref["adj_density"]) <= KER_TOL_F32
+
+
 def test_engine_uneven_grids(sg, oracle):
     pb = W.config4(nsrc=5, nperiod=3, nmax=72, nmin=40, span_deg=2.0)
     _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
