@@ -436,11 +436,11 @@ surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* engine, int* gri
                                               int* blocks_per_sm, size_t* smem_bytes);
 
 /* Time every solve-kernel variant that applies to the loaded problem (plain
- * FP64: one; FP32: the warp-per-solve kernel's variants -- 0 / 3: cell
- * constants loaded at the visit, 12 / 8 resident warps per SM; 1 / 2: every
- * operand loaded a step ahead, 8 / 12 resident warps per SM -- and the
- * block-per-solve kernel; the warp kernels on row-major arrays and on the
- * diagonal layouts) with one warm-up and one timed evaluation each,
+ * FP64: one; FP32: the row-per-lane kernel's variants -- 0 / 1: every
+ * operand loaded a step ahead, 8 resident warps per SM, solves cut into work
+ * items / whole; 2 / 3: cell constants loaded at the visit, 12 / 8 warps,
+ * items / whole -- the diagonal-layout kernel's variants and the
+ * block-per-solve kernel) with one warm-up and one timed evaluation each,
  * and use the fastest for later runs of this precision until the next load.
  * Returns the chosen kernel (0 FP64, 1 FP32 block, 2 / 3 FP32 warp), its variant
  * and its solve-kernel time. */
