@@ -821,36 +821,10 @@ __global__ void __launch_bounds__(32, MINW) k_batch_fp32d(BatchArgs A) {
         for (long long k = lane; k < D; k += 32) sf[k] = 0.f;
       }
       __syncwarp();
-      if (lane == 0) {
-        // adjoint sources weight*(tekio-tt) (src/measadj.f90:88) and -weight
-        // (:102), bilinear splat over the cell area (:1328-1336), scaled by 1/d
-        for (int f = 0; f < nf && st != ST_BAD_ARG; ++f)
-          for (int r = 0; r < nr; ++r) {
-            const double wt = A.wgt_eff[r0 + r];
-            const double sv = f == 0 ? wt * (A.tekio[r0 + r] - A.tt[r0 + r]) : -1.0 * wt;
-            const double xr = A.recx[r0 + r] / 180.0 * PI_S, yr = A.recy[r0 + r] / 180.0 * PI_S;
-            float r1 = 0.f, r2 = 0.f;
-            const int i0 = locate_cell(P.xs, nx, P.dx, xr, &r1);
-            const int j0 = locate_cell(P.ys, ny, P.dy, yr, &r2);
-            if (i0 < 0 || j0 < 0) { st = ST_BAD_ARG; break; }
-            const double den = P.dx * R_EARTH * cos(yr) * P.dy * R_EARTH;
-            float* sf = f ? V.src[1][0] : V.src[0][0];
-            const int k00 = dix(g, 0, i0, j0);
-            sf[k00] += (float)(sv * (double)(1 - r1) * (double)(1 - r2) / den) * V.id[k00];
-            if (j0 + 1 < ny) {
-              const int k01 = dix(g, 0, i0, j0 + 1);
-              sf[k01] += (float)(sv * (double)(1 - r1) * (double)r2 / den) * V.id[k01];
-            }
-            if (i0 + 1 < nx) {
-              const int k10 = dix(g, 0, i0 + 1, j0);
-              sf[k10] += (float)(sv * (double)r1 * (double)(1 - r2) / den) * V.id[k10];
-            }
-            if (i0 + 1 < nx && j0 + 1 < ny) {
-              const int k11 = dix(g, 0, i0 + 1, j0 + 1);
-              sf[k11] += (float)(sv * (double)r1 * (double)r2 / den) * V.id[k11];
-            }
-          }
-      }
+      // adjoint sources weight*(tekio-tt) (src/measadj.f90:88) and -weight
+      // (:102), bilinear splat over the cell area (:1328-1336), scaled by 1/d
+      st = adj_sources_warp(A, P, r0, nr, nf, V.src[0][0], V.src[nf - 1][0], V.id,
+                            [&g](int i, int j) { return dix(g, 0, i, j); }, lane, st);
       st = __shfl_sync(FULL, st, 0);
       __syncwarp();
       for (int f = 0; f < nf; ++f)

@@ -571,31 +571,9 @@ __device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, cons
   for (int f = 0; f < nf; ++f)
     for (size_t k = T.tid; k < N; k += 32 * NW) V.src[f][k] = 0.f;
   tsync<NW>();
-  if (T.tid == 0) {
-    for (int f = 0; f < nf && st != ST_BAD_ARG; ++f)
-      for (int r = 0; r < nr; ++r) {
-        const double wt = A.wgt_eff[r0 + r];
-        const double sv = f == 0 ? wt * (A.tekio[r0 + r] - A.tt[r0 + r]) : -1.0 * wt;
-        const double xr = A.recx[r0 + r] / 180.0 * PI_S, yr = A.recy[r0 + r] / 180.0 * PI_S;
-        float r1 = 0.f, r2 = 0.f;
-        const int i0 = locate_cell(P.xs, nx, P.dx, xr, &r1);
-        const int j0 = locate_cell(P.ys, ny, P.dy, yr, &r2);
-        if (i0 < 0 || j0 < 0) {
-          st = ST_BAD_ARG;
-          break;
-        }
-        const double den = P.dx * R_EARTH * cos(yr) * P.dy * R_EARTH;
-        const size_t k = i0 + (size_t)nx * j0;
-        float* sf = V.src[f];
-        sf[k] += (float)(sv * (double)(1 - r1) * (double)(1 - r2) / den) * V.id[k];
-        if (j0 + 1 < ny)
-          sf[k + nx] += (float)(sv * (double)(1 - r1) * (double)r2 / den) * V.id[k + nx];
-        if (i0 + 1 < nx)
-          sf[k + 1] += (float)(sv * (double)r1 * (double)(1 - r2) / den) * V.id[k + 1];
-        if (i0 + 1 < nx && j0 + 1 < ny)
-          sf[k + nx + 1] += (float)(sv * (double)r1 * (double)r2 / den) * V.id[k + nx + 1];
-      }
-  }
+  if (T.wid == 0)
+    st = adj_sources_warp(A, P, r0, nr, nf, V.src[0], V.src[nf - 1], V.id,
+                          [nx](int i, int j) { return i + nx * j; }, T.lane, st);
   st = tbcast<NW>(st);
   tsync<NW>();
   return st;

@@ -46,34 +46,31 @@ __device__ inline WSolve w_locate(const PeriodDev& P, double x0, double y0, doub
       w.si = i0;
       w.sj = j0;
     }
-    int a0 = nx, a1 = -1, b0 = ny, b1 = -1, c0 = nx, c1 = -1, e0 = ny, e1 = -1;
-    const double ddx = P.xdeg[1] - P.xdeg[0], ddy = P.ydeg[1] - P.ydeg[0];
-    for (int i = 0; i < nx; ++i) {
-      if (fabs((P.xs[i] - x0) / P.dx) <= 1.0) { a0 = min(a0, i); a1 = max(a1, i); }
-      if (fabs(P.xdeg[i] - xd0) < 1.5 * ddx) { c0 = min(c0, i); c1 = max(c1, i); }
-    }
-    for (int j = 0; j < ny; ++j) {
-      if (fabs((P.ys[j] - y0) / P.dy) <= 1.0) { b0 = min(b0, j); b1 = max(b1, j); }
-      if (fabs(P.ydeg[j] - yd0) < 1.5 * ddy) { e0 = min(e0, j); e1 = max(e1, j); }
-    }
-    w.box = Box{a0, a1, b0, b1};
-    w.mbox = Box{c0, c1, e0, e1};
-    if (w.status == ST_OK && a0 <= a1 && b0 <= b1 &&
-        (a0 == 0 || a1 == nx - 1 || b0 == 0 || b1 == ny - 1))
-      w.status = ST_SOURCE_ON_BOUNDARY;
   }
   w.status = __shfl_sync(FULL, w.status, 0);
   w.fun0 = shfl_d(w.fun0, 0);
   w.si = __shfl_sync(FULL, w.si, 0);
   w.sj = __shfl_sync(FULL, w.sj, 0);
-  w.box.i0 = __shfl_sync(FULL, w.box.i0, 0);
-  w.box.i1 = __shfl_sync(FULL, w.box.i1, 0);
-  w.box.j0 = __shfl_sync(FULL, w.box.j0, 0);
-  w.box.j1 = __shfl_sync(FULL, w.box.j1, 0);
-  w.mbox.i0 = __shfl_sync(FULL, w.mbox.i0, 0);
-  w.mbox.i1 = __shfl_sync(FULL, w.mbox.i1, 0);
-  w.mbox.j0 = __shfl_sync(FULL, w.mbox.j0, 0);
-  w.mbox.j1 = __shfl_sync(FULL, w.mbox.j1, 0);
+  // frozen box (|x-x0| <= dx, |y-y0| <= dy) and mask box (|x-x0| < 1.5 dx in
+  // degrees): the nodes' tests spread over the lanes, then min / max
+  int a0 = nx, a1 = -1, b0 = ny, b1 = -1, c0 = nx, c1 = -1, e0 = ny, e1 = -1;
+  const double ddx = P.xdeg[1] - P.xdeg[0], ddy = P.ydeg[1] - P.ydeg[0];
+  for (int i = lane; i < nx; i += 32) {
+    if (fabs((P.xs[i] - x0) / P.dx) <= 1.0) { a0 = min(a0, i); a1 = max(a1, i); }
+    if (fabs(P.xdeg[i] - xd0) < 1.5 * ddx) { c0 = min(c0, i); c1 = max(c1, i); }
+  }
+  for (int j = lane; j < ny; j += 32) {
+    if (fabs((P.ys[j] - y0) / P.dy) <= 1.0) { b0 = min(b0, j); b1 = max(b1, j); }
+    if (fabs(P.ydeg[j] - yd0) < 1.5 * ddy) { e0 = min(e0, j); e1 = max(e1, j); }
+  }
+  w.box = Box{__reduce_min_sync(FULL, a0), __reduce_max_sync(FULL, a1),
+              __reduce_min_sync(FULL, b0), __reduce_max_sync(FULL, b1)};
+  w.mbox = Box{__reduce_min_sync(FULL, c0), __reduce_max_sync(FULL, c1),
+               __reduce_min_sync(FULL, e0), __reduce_max_sync(FULL, e1)};
+  const Box& b = w.box;
+  if (w.status == ST_OK && b.i0 <= b.i1 && b.j0 <= b.j1 &&
+      (b.i0 == 0 || b.i1 == nx - 1 || b.j0 == 0 || b.j1 == ny - 1))
+    w.status = ST_SOURCE_ON_BOUNDARY;
   return w;
 }
 
@@ -346,6 +343,93 @@ __device__ inline float adj_weights(float Tk, float Tw, float Te, float Ts, floa
                      __fmul_rn(b1p * idy, id), __fmul_rn(-(b2m * idy), id));
   }
   return id;
+}
+
+// Adjoint sources of one solve: weight*(tekio-tt) for field 0
+// (src/measadj.f90:88) and -weight for field 1 (:102), each splat
+// bilinearly over the receiver's cell divided by the cell area
+// (src/eikon_solver_2d.f90:1328-1336) and scaled by the cell's 1/d.  Called
+// by all 32 lanes of one warp.  The lanes evaluate 32 receivers at a time
+// (cell search, cos, the FP64 quotients: the costly part, which a single
+// lane would run at 1/32 of the FP64 pipe); lane 0 then adds the
+// contributions in receiver order, so every cell's sum is the sequential
+// one.  A receiver outside the grid stops field 0 there, skips field 1 and
+// returns ST_BAD_ARG, as the sequential loop over fields and receivers
+// does.  `ix(i, j)` maps a node to its index in `sf0`, `sf1` and `id`.
+template <class Ix>
+__device__ inline int adj_sources_warp(const BatchArgs& A, const PeriodDev& P, int r0, int nr,
+                                       int nf, float* sf0, float* sf1, const float* id, Ix ix,
+                                       int lane, int st) {
+  if (st == ST_BAD_ARG) return st;
+  const int nx = P.nx, ny = P.ny;
+  auto cell = [&](int r, int* i0, int* j0, float* r1, float* r2, double* yr) {
+    const double xr = A.recx[r0 + r] / 180.0 * PI_S;
+    *yr = A.recy[r0 + r] / 180.0 * PI_S;
+    *i0 = locate_cell(P.xs, nx, P.dx, xr, r1);
+    *j0 = locate_cell(P.ys, ny, P.dy, *yr, r2);
+  };
+  // the first receiver outside the grid (nr: none)
+  int n0 = nr;
+  for (int rb = 0; rb < nr; rb += 32) {
+    bool out = false;
+    if (rb + lane < nr) {
+      int i0, j0;
+      float r1, r2;
+      double yr;
+      cell(rb + lane, &i0, &j0, &r1, &r2, &yr);
+      out = i0 < 0 || j0 < 0;
+    }
+    const unsigned m = __ballot_sync(FULL, out);
+    if (m) {
+      n0 = rb + __ffs(m) - 1;
+      break;
+    }
+  }
+  const bool two = nf == 2 && n0 == nr;
+  for (int rb = 0; rb < n0; rb += 32) {
+    int i0 = 0, j0 = 0;
+    float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+    if (rb + lane < n0) {
+      const int r = rb + lane;
+      float r1 = 0.f, r2 = 0.f;
+      double yr;
+      cell(r, &i0, &j0, &r1, &r2, &yr);
+      const double wt = A.wgt_eff[r0 + r];
+      const double sv0 = wt * (A.tekio[r0 + r] - A.tt[r0 + r]), sv1 = -1.0 * wt;
+      const double den = P.dx * R_EARTH * cos(yr) * P.dy * R_EARTH;
+      // corner c = (i0 + c/2, j0 + c%2): sv * wx * wy / den, left to right
+      const double wx[2] = {(double)(1 - r1), (double)r1}, wy[2] = {(double)(1 - r2), (double)r2};
+      const bool has[4] = {true, j0 + 1 < ny, i0 + 1 < nx, i0 + 1 < nx && j0 + 1 < ny};
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (has[c]) {
+          const float d = id[ix(i0 + (c >> 1), j0 + (c & 1))];
+          c0[c] = __fmul_rn((float)(sv0 * wx[c >> 1] * wy[c & 1] / den), d);
+          if (two) c1[c] = __fmul_rn((float)(sv1 * wx[c >> 1] * wy[c & 1] / den), d);
+        }
+    }
+    const int cnt = min(32, n0 - rb);
+    for (int l = 0; l < cnt; ++l) {
+      const int i = __shfl_sync(FULL, i0, l), j = __shfl_sync(FULL, j0, l);
+      float a0[4], a1[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        a0[c] = __shfl_sync(FULL, c0[c], l);
+        a1[c] = two ? __shfl_sync(FULL, c1[c], l) : 0.f;
+      }
+      if (lane == 0) {
+        const bool has[4] = {true, j + 1 < ny, i + 1 < nx, i + 1 < nx && j + 1 < ny};
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (has[c]) {
+            const int k = ix(i + (c >> 1), j + (c & 1));
+            sf0[k] = __fadd_rn(sf0[k], a0[c]);
+            if (two) sf1[k] = __fadd_rn(sf1[k], a1[c]);
+          }
+      }
+    }
+  }
+  return n0 < nr ? ST_BAD_ARG : st;
 }
 
 }  // namespace sgb
