@@ -175,6 +175,7 @@ struct WorkList {
   int *pidx, *rec_off, *nrec, *path, *order, *plist_off, *plist;
   double *srcx, *srcy, *recx, *recy, *tt, *weight;
   long long* kslot;
+  std::vector<int> pidx_h;  // host copy: team classes of the launch plan
 };
 
 enum ReqState { RQ_PENDING = 0, RQ_RUNNING = 1, RQ_DONE = 2 };
@@ -188,6 +189,7 @@ struct Request {
   std::chrono::steady_clock::time_point t_submit, t_start, t_done;
   size_t off = 0, bytes = 0;
   cudaStream_t st = nullptr;
+  ClassStreams cs;  // side streams of the row kernel's team classes
   cudaEvent_t done = nullptr;
   // device buffers (in the request's chunk)
   PeriodArrays d{};
@@ -293,7 +295,8 @@ int start_request(surfatt_server* S, Request& r) {
   WorkList& L = *S->lists[r.wl];
   Model& M = *S->models[L.model];
   const bool own_vel = !r.svel.empty();
-  r.shape.from_grids(M.nx.data(), M.ny.data(), M.goff.data(), M.nperiod, L.nsolve, L.npath);
+  r.shape.from_grids(M.nx.data(), M.ny.data(), M.goff.data(), M.nperiod, L.nsolve, L.npath,
+                     L.pidx_h.data());
   // Whole solves per warp: requests run side by side and share the SMs, so
   // the short last round that cut solves buy a single evaluation is not
   // what limits a request here.
@@ -318,7 +321,7 @@ int start_request(surfatt_server* S, Request& r) {
     r.status_d = cv.take<int>(ns);
     r.fit = cv.take<int>(ns);
     r.ait = cv.take<int>(ns);
-    r.queue = cv.take<int>(1);
+    r.queue = cv.take<int>(kTeamClasses);
     r.ws = cv.take<double>((size_t)plan_ws_doubles(r.plan, L.nsolve));
   };
   Carver sizer;
@@ -333,6 +336,7 @@ int start_request(surfatt_server* S, Request& r) {
   if (cudaStreamCreateWithFlags(&r.st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming) != cudaSuccess)
     return ST_CUDA_ERROR;
+  if (r.plan.classes > 1 && r.cs.create() != ST_OK) return ST_CUDA_ERROR;
   const PeriodDev* periods = M.d.periods;
   if (own_vel) {
     // the request's velocity with the model's axes and metric
@@ -387,7 +391,7 @@ int start_request(surfatt_server* S, Request& r) {
   dev.adj_s = r.adj;
   dev.adj_density = r.adjd;
   const int n = enqueue_evaluation(r.shape, dev, r.plan, r.mode, r.prec, r.ws, r.queue, r.st,
-                                   nullptr, nullptr);
+                                   nullptr, nullptr, &r.cs);
   if (n < 0) return -n;
   if (cudaEventRecord(r.done, r.st) != cudaSuccess) return ST_CUDA_ERROR;
   return ST_OK;
@@ -422,6 +426,7 @@ void finish_request(surfatt_server* S, Request& r) {
   }
   if (r.st) cudaStreamDestroy(r.st);
   if (r.done) cudaEventDestroy(r.done);
+  r.cs.destroy();
   r.st = nullptr;
   r.done = nullptr;
   if (r.bytes) S->arena.release(r.off, r.bytes);
@@ -629,7 +634,13 @@ surfatt_status_t surfatt_server_add_worklist(surfatt_server_t* S, int model_id,
   std::vector<long long> kslot(ns);
   std::iota(order.begin(), order.end(), 0);
   auto cells = [&](int s) { return (long long)M.nx[pb->pidx[s]] * M.ny[pb->pidx[s]]; };
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cells(a) > cells(b); });
+  // team classes of the FP32 row kernel contiguous (largest team first),
+  // then largest grids first
+  auto cls = [&](int s) { return team_class_key(M.ny[pb->pidx[s]]); };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return cls(a) != cls(b) ? cls(a) > cls(b) : cells(a) > cells(b);
+  });
+  L->pidx_h.assign(pb->pidx, pb->pidx + ns);
   for (int s = 0; s < ns; ++s) plist_off[pb->pidx[s] + 1]++;
   for (int p = 0; p < M.nperiod; ++p) plist_off[p + 1] += plist_off[p];
   {
