@@ -39,10 +39,12 @@ FWD_FLOPS_PER_VISIT = 351.8
 ADJ_FLOPS_PER_VISIT = 16.0
 KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w", 3: "k_batch_fp32d"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# FP32 solve kernel, from one ncu capture of the 320-solve case (1.955 GB),
-# scaled by the solves for the 1280-solve workload (the per-solve workspace
-# and operands are the same for every solve): profiles/k_batch_fp32w_config2s.md.
-DRAM_BYTES_PER_LAUNCH = {"config2": 7.82e9, "config2s": 1.955e9}
+# FP32 row kernel (k_batch_fp32w), from one ncu capture of the 320-solve case
+# (1.603 GB read + 0.629 GB written), scaled by the solves for the 1280-solve
+# workload (the per-solve workspace and operands are the same for every
+# solve): profiles/k_batch_fp32w_config2s.md.  Reported only when the
+# autotuner picked that kernel.
+DRAM_BYTES_PER_LAUNCH = {"config2": 8.929e9, "config2s": 2.232e9}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
 
 
@@ -336,7 +338,7 @@ def run_ours(args):
     k64_ms = statistics.mean(k64)
     ach32 = flops32 / (k32_ms * 1e-3) / 1e12
     ach64 = flops64 / (k64_ms * 1e-3) / 1e12
-    traffic = DRAM_BYTES_PER_LAUNCH.get(args.workload)
+    traffic = DRAM_BYTES_PER_LAUNCH.get(args.workload) if launch32.get("kind") == 2 else None
 
     # where the solve kernel's time goes: one more evaluation with the
     # per-phase SM cycle counters on (outside the timed region)
