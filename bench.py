@@ -72,7 +72,7 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
                     choices=["config1", "config2", "config2s", "config4", "serving", "smooth",
-                             "kernel3d", "worklist", "topo"])
+                             "kernel3d", "worklist", "topo", "dropin"])
     ap.add_argument("--requests", type=int, default=40,
                     help="serving: requests in the Poisson stream")
     ap.add_argument("--load", type=float, default=0.7,
@@ -424,6 +424,8 @@ def run_reference(args):
         return _run_reference_worklist(args, O, dist)
     if args.workload == "topo":
         return _run_reference_topo(args, O, dist)
+    if args.workload == "dropin":
+        return _run_reference_dropin(args, O, dist)
     pb, desc = _workload(args.workload)
     nthr = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -695,6 +697,257 @@ def run_smooth(args):
     eng.close()
     if dist is not None:
         dist.barrier()
+        dist.destroy_process_group()
+
+
+def _dropin_case():
+    """Config 1 as the unchanged tomo2d drives the solver drop-ins: per
+    source the forward solve, the adjoint solve with the residual sources
+    and the mask (src/measadj.f90:62-90, called from src/tomo2d.f90:177-189),
+    every call with host arrays.  The adjoint sources come from one FP64
+    evaluation of the same model (outside the timed region)."""
+    from surfatt_gb300 import workloads as W
+    obs = W.read_src_rec_tt(os.path.join(ROOT, "tests", "golden", "config1_src_rec.csv"))
+    pb = W.config1(observed_tt=obs)
+    F = lambda a: np.asfortranarray(a, dtype=np.float64)
+    xx, yy = (np.ascontiguousarray(v, dtype=np.float64) for v in pb.grid(0))
+    a, b, c = F(pb.field("m11", 0)), F(pb.field("m22", 0)), F(-pb.field("m12", 0))
+    fun = F(1.0 / pb.field("svel", 0))
+    srcs = []
+    for s in range(pb.nsolve):
+        r0, nr = int(pb.rec_off[s]), int(pb.nrec[s])
+        sl = slice(r0, r0 + nr)
+        srcs.append(dict(x0=float(pb.srcx[s]), y0=float(pb.srcy[s]),
+                         xr=np.ascontiguousarray(pb.recx[sl]), yr=np.ascontiguousarray(pb.recy[sl]),
+                         tt=np.asarray(pb.tt[sl]), w=np.asarray(pb.weight[sl]),
+                         path=np.asarray(pb.path[sl])))
+    return pb, xx, yy, a, b, c, fun, srcs
+
+
+def _dropin_sadj(srcs, tt_fwd):
+    """sourceAdj = weight*(tekio-tt) after the outlier zeroing (src/measadj.f90:82-88)."""
+    for d in srcs:
+        tek = tt_fwd[d["path"]]
+        w = np.where(np.abs(tek - d["tt"]) / d["tt"] > 0.5, 0.0, d["w"])
+        d["sadj"] = np.ascontiguousarray(w * (tek - d["tt"]))
+
+
+def _dropin_blocks(n, parts):
+    """Contiguous split of n sources over `parts` callers, the first ones one
+    larger (src/shared/parallel.f90 scatter_all_i)."""
+    q, r = divmod(n, parts)
+    out, lo = [], 0
+    for k in range(parts):
+        hi = lo + q + (1 if k < r else 0)
+        out.append(range(lo, hi))
+        lo = hi
+    return out
+
+
+def _oracle_dropin_block(job):
+    """One caller's sources through the oracle's forward, adjoint and mask."""
+    import oracle as O
+    xx, yy, a, b, c, fun, block = job
+    for d in block:
+        T, _, _ = O.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, d["x0"], d["y0"])
+        Ta, _, _ = O.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, T, d["xr"], d["yr"], d["sadj"])
+        O.mask(xx, yy, Ta, d["x0"], d["y0"])
+    return len(block)
+
+
+def run_dropin(args):
+    """The gfortran-mangled drop-ins (fsm_uw_ps_lonlat_2d_, fsm_o1_jse_lonlat_2d_,
+    mask_) on config 1, called per source exactly as the unchanged Fortran
+    calls them, from 1 host thread and from one thread per host core (the
+    reference runs one MPI rank per core, each calling the solver for its
+    block of sources).  Each call copies its host arrays in and its result
+    out: `value` and `e2e` are the same measurement."""
+    import ctypes
+    import multiprocessing as mp
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    import torch
+    import surfatt_gb300 as sg
+    dist, rank, world, local = _dist()
+    ncores = os.cpu_count() or 1
+    pool = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        pool = mp.get_context("spawn").Pool(1)
+    sg.build()
+    torch.cuda.set_device(local)
+    pb, xx, yy, a, b, c, fun, srcs = _dropin_case()
+    eng = sg.Engine(local)
+    _dropin_sadj(srcs, eng.evaluate(pb, mode=2)["tt_fwd"])
+    eng.close()
+    fp64_peak, _ = sg.measure_peaks(local)
+    nx, ny = len(xx), len(yy)
+    N = nx * ny
+    L = sg.lib()
+    dp = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    ci = lambda v: ctypes.byref(ctypes.c_int(v))
+    cd = lambda v: ctypes.byref(ctypes.c_double(v))
+    common = (dp(xx), dp(yy), ci(nx), ci(ny), dp(a), dp(b), dp(c))
+    tl = threading.local()
+
+    def run_block(block):
+        if not hasattr(tl, "T"):
+            tl.T = np.zeros((nx, ny), order="F")
+            tl.Ta = np.zeros((nx, ny), order="F")
+            tl.u = np.zeros((nx, ny), order="F")
+        its = [0, 0]
+        for k in block:
+            d = srcs[k]
+            L.fsm_uw_ps_lonlat_2d_(*common, dp(tl.T), dp(fun), cd(d["x0"]), cd(d["y0"]),
+                                   dp(tl.u))
+            if sg.last_status() != sg.OK:
+                raise RuntimeError(f"forward drop-in status {sg.last_status()}")
+            its[0] += sg.last_iterations()
+            L.fsm_o1_jse_lonlat_2d_(*common, dp(tl.T), dp(tl.Ta), dp(d["xr"]), dp(d["yr"]),
+                                    dp(d["sadj"]), ci(len(d["xr"])))
+            if sg.last_status() != sg.OK:
+                raise RuntimeError(f"adjoint drop-in status {sg.last_status()}")
+            its[1] += sg.last_iterations()
+            L.mask_(dp(xx), dp(yy), ci(nx), ci(ny), dp(tl.Ta), cd(d["x0"]), cd(d["y0"]))
+        return its
+
+    def timed(nthreads):
+        blocks = _dropin_blocks(len(srcs), nthreads)
+        ts, its = [], [0, 0]
+        with ThreadPoolExecutor(max_workers=nthreads) as ex:
+            for i in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                res = list(ex.map(run_block, blocks))
+                t1 = time.perf_counter()
+                if i >= args.warmup:
+                    ts.append(t1 - t0)
+                    its = [its[0] + sum(r[0] for r in res), its[1] + sum(r[1] for r in res)]
+        return statistics.mean(ts), its
+
+    clocks = Clocks(local)
+    _barrier(dist, local)
+    clocks.start()
+    s_many, its = timed(ncores)
+    _barrier(dist, local)
+    ck = clocks.stop()
+    s_one, _ = timed(1)
+    s_many = _max_over_ranks(dist, s_many, local)
+    value = len(srcs) * world / s_many
+    # FP64 work of the timed calls (reference formulation), over wall time
+    fwd_visits = its[0] / args.steps * 4 * N
+    adj_visits = its[1] / args.steps * 4 * (nx - 2) * (ny - 2)
+    flops = fwd_visits * FWD_FLOPS_PER_VISIT + adj_visits * ADJ_FLOPS_PER_VISIT
+    ach = flops / s_many / 1e12
+    nr_tot = sum(len(d["xr"]) for d in srcs)
+    h2d = len(srcs) * ((4 * N + nx + ny) + (4 * N + nx + ny) + (N + nx + ny)) * 8 + nr_tot * 3 * 8
+    d2h = len(srcs) * 3 * N * 8
+
+    # parity of the drop-ins on two sources against the oracle (outside timing)
+    parity, cpu = {}, None
+    if pool is not None:
+        worst_t = worst_a = 0.0
+        for k in (0, len(srcs) - 1):
+            d = srcs[k]
+            T, _, _ = sg.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, d["x0"], d["y0"])
+            Ta, _, _ = sg.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, T, d["xr"], d["yr"], d["sadj"])
+            Ta = sg.mask(xx, yy, Ta, d["x0"], d["y0"])
+            Tr, _, _ = O.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, d["x0"], d["y0"])
+            Tar, _, _ = O.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, Tr, d["xr"], d["yr"], d["sadj"])
+            Tar = O.mask(xx, yy, Tar, d["x0"], d["y0"])
+            worst_t = max(worst_t, float(np.max(np.abs(T - Tr) / np.abs(Tr).clip(1e-30))))
+            worst_a = max(worst_a, float(np.linalg.norm(Ta - Tar) / np.linalg.norm(Tar)))
+        parity = {"tt_rel_max_vs_oracle": worst_t, "adjoint_rel_norm_vs_oracle": worst_a}
+        # the oracle's same calls on one core, a sample of 8 sources
+        sample = list(range(8))
+        t0 = time.perf_counter()
+        pool.map(_oracle_dropin_block, [(xx, yy, a, b, c, fun, [srcs[k] for k in sample])])
+        t1 = time.perf_counter()
+        pool.close()
+        pool.join()
+        cpu = {"value": len(sample) / (t1 - t0), "unit": "sources/s", "cores": 1,
+               "kind": "port", "seconds": t1 - t0,
+               "sample": "8 of the 25 sources, forward + adjoint + mask each, one process"}
+
+    if rank == 0:
+        line = {
+            "metric": "drop-in solves/s (forward + adjoint + mask per source through the "
+                      "gfortran-mangled symbols, host arrays)",
+            "value": value, "unit": "sources/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": s_many * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "config1 through the drop-ins: 81x81, 25 sources x 24 "
+                                   "receivers, 2-D mode (one adjoint per source)",
+                       "callers": ncores, "caller_kind": "host threads (one per core, as "
+                       "the reference's MPI ranks), contiguous source blocks",
+                       "single_caller": {"value": len(srcs) / s_one, "unit": "sources/s",
+                                         "ms_per_step": s_one * 1e3},
+                       "note": "every call copies its host arrays to the device and its "
+                               "result back (the callee keeps no state): value and e2e are "
+                               "the same measurement",
+                       "l2": "inputs re-copied from the host every call"},
+            "clocks": ck,
+            "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": s_many * 1e3,
+                    "host_buffers": "pageable (the caller's arrays)"},
+            "gpu_launches": 5 * len(srcs) * args.steps,
+            "roofline": {"bound": "fp64", "bound_note": "one 256-thread block per call (one "
+                         "SM); achieved = reference-formulation FP64 flops of the timed calls "
+                         "over wall time, copies included",
+                         "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": ach / fp64_peak, "traffic": None,
+                         "peak_source": "surfatt_measure_peaks (FP64 FMA chains), this run",
+                         "kernel": "k_uw_single + k_jse_single"},
+            "iterations": {"fwd_per_source": its[0] / args.steps / len(srcs),
+                           "adj_per_source": its[1] / args.steps / len(srcs)},
+            "cpu_baseline": cpu, "parity": parity,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _run_reference_dropin(args, O, dist):
+    """Reference arm of the drop-in workload: the oracle's forward, adjoint
+    and mask per source, sources split over one process per core (the
+    reference's MPI ranks)."""
+    import multiprocessing as mp
+    from surfatt_gb300 import workloads as W
+    nthr = os.cpu_count() or 1
+    pb, xx, yy, a, b, c, fun, srcs = _dropin_case()
+    _dropin_sadj(srcs, O.gradient_eval(pb, mode=2, nthreads=nthr)["tt_fwd"])
+    pool = mp.get_context("spawn").Pool(nthr)
+    jobs = [(xx, yy, a, b, c, fun, [srcs[k] for k in blk])
+            for blk in _dropin_blocks(len(srcs), nthr)]
+    ts = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        pool.map(_oracle_dropin_block, jobs)
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    pool.close()
+    pool.join()
+    s = statistics.mean(ts)
+    v = len(srcs) / s
+    line = {"impl": "reference",
+            "metric": "drop-in solves/s (forward + adjoint + mask per source through the "
+                      "gfortran-mangled symbols, host arrays)",
+            "value": v, "unit": "sources/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "config1 through the solver routines: 81x81, 25 sources x "
+                                   "24 receivers, 2-D mode", "callers": nthr},
+            "cpu_baseline": {"value": v, "unit": "sources/s", "cores": nthr, "kind": "port",
+                             "sample": "all 25 sources per step, contiguous blocks over one "
+                                       "process per core"},
+            "e2e": {"value": v, "unit": "sources/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
+                    "is timed through the C restatement in oracle/"}
+    print(json.dumps(line))
+    if dist is not None:
         dist.destroy_process_group()
 
 
@@ -1116,5 +1369,7 @@ if __name__ == "__main__":
         run_worklist(a)
     elif a.workload == "topo":
         run_topo(a)
+    elif a.workload == "dropin":
+        run_dropin(a)
     else:
         run_ours(a)
