@@ -47,6 +47,36 @@ def test_alone_equals_in_the_mix(sg):
     srv.close()
 
 
+def test_team_classes_alone_equals_in_the_mix(sg):
+    """A request whose grids need warp teams of three sizes (48 to 304 rows:
+    one launch per team class on the request's side streams) gives the same
+    bits alone, in the mix with other requests, and through the engine."""
+    c = W.config4(nsrc=4, nperiod=5, nmax=300, nmin=48, span_deg=2.0, seed=43)
+    assert {1 if n <= 128 else (int(n) + 127) // 128 for n in c.ny} == {1, 2, 3}
+    a, _ = _model_and_lists()
+    srv = sg.Server(0, hbm_budget_bytes=4 << 30, max_inflight=4)
+    wc = srv.add_worklist(srv.add_model(c), c)
+    wa = srv.add_worklist(srv.add_model(a), a)
+    reqs = [(wc, None, 3, sg.PREC_FP32), (wa, None, 3, sg.PREC_FP32),
+            (wc, c.svel * 1.01, 2, sg.PREC_FP32), (wc, None, 3, sg.PREC_FP64)]
+    alone = []
+    for wl, v, mode, prec in reqs:
+        st, res, _ = srv.wait(srv.submit(wl, v, mode, prec))
+        assert st == sg.OK
+        alone.append(res)
+    tickets = [srv.submit(wl, v, mode, prec) for wl, v, mode, prec in reqs]
+    for t, ref in zip(tickets, alone):
+        st, res, _ = srv.wait(t)
+        assert st == sg.OK
+        assert _same(res, ref)
+    srv.close()
+    eng = sg.Engine(0)
+    ref = eng.evaluate(c, mode=3, precision=sg.PREC_FP32)
+    eng.close()
+    assert np.array_equal(alone[0]["adj_s"], ref["adj_s"])
+    assert np.array_equal(alone[0]["tt_fwd"], ref["tt_fwd"])
+
+
 def test_server_matches_engine(sg):
     a, _ = _model_and_lists()
     srv = sg.Server(0, hbm_budget_bytes=1 << 30, max_inflight=2)
