@@ -416,20 +416,37 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
         if (u < 0 || u >= nu || vtop + 1 >= nv) return 0.f;
         return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
       };
+      // Teams with register prefetch load the operands of step t+2 at step t
+      // (a visit is four FMAs, and a team step also waits at the barrier: one
+      // step does not cover the loads' latency).  A cell is written only at
+      // its own visit and the weights, sources and iteration-start values are
+      // fixed within a sweep, so the early loads see the values a load at the
+      // visit would.  (A single warp keeps one step: the extra registers
+      // spill in its loop.)
+      constexpr bool AHEAD2 = PF == 1 && NW > 1;
       float res[MB];
-      WAdj cur[MB];
+      WAdj cur[MB], ahead[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
         wa_load<PF == 1>(cur[m], 0, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+        if (AHEAD2)
+          wa_load<true>(ahead[m], 1, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
       }
       float pn = top ? north_of_top(0) : 0.f;
       for (int t = 0; t < nsteps; ++t) {
         WAdj nxt[MB];
 #pragma unroll
-        for (int m = 0; m < MB; ++m)
-          wa_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
-                           last);
+        for (int m = 0; m < MB; ++m) {
+          if (AHEAD2) {
+            nxt[m] = ahead[m];
+            wa_load<true>(ahead[m], t + 2, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
+                          last);
+          } else {
+            wa_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
+                             last);
+          }
+        }
         const float qn = top ? north_of_top(t + 1) : 0.f;
         float south[MB], north[MB], nown[MB];
 #pragma unroll
