@@ -301,6 +301,65 @@ def test_fp32_team_classes(sg, oracle, variant):
         assert rel_max(full["adj_density"], ref["adj_density"]) <= KER_TOL_F32
 
 
+def _drop_receivers(pb, solves):
+    """The problem with the receiver lists of `solves` emptied (the other
+    solves keep theirs and their path indices)."""
+    import dataclasses
+    offs, nrec, keep = [], [], []
+    for s in range(pb.nsolve):
+        r0, n = int(pb.rec_off[s]), 0 if s in solves else int(pb.nrec[s])
+        offs.append(len(keep))
+        nrec.append(n)
+        keep.extend(range(r0, r0 + n))
+    ridx = np.asarray(keep, np.int64)
+    return dataclasses.replace(
+        pb, rec_off=np.asarray(offs, np.int32), nrec=np.asarray(nrec, np.int32),
+        recx=pb.recx[ridx].copy(), recy=pb.recy[ridx].copy(), tt=pb.tt[ridx].copy(),
+        weight=pb.weight[ridx].copy(), path=pb.path[ridx].copy(), n_paths=pb.npath)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_engine_solves_without_receivers(sg, oracle, prec):
+    """Solves with empty receiver lists (zero misfit, zero adjoint sources),
+    among solves with receivers, on a one-warp grid and on a team grid."""
+    P = sg.PREC_FP64 if prec == "fp64" else sg.PREC_FP32
+    tols = (TT_TOL, KER_TOL) if prec == "fp64" else (TT_TOL_F32, KER_TOL_F32)
+    pb = _drop_receivers(W.flat_case(nx=40, ny=36, nsta=5, nperiod=2, mode=3, seed=13), {0, 3})
+    assert pb.nrec[0] == 0 and pb.nrec[3] == 0 and pb.nrec[1] > 0
+    _engine_vs_oracle(sg, oracle, pb, 3, P, *tols)
+    pb = _drop_receivers(W.flat_case(nx=30, ny=150, d=0.02, nsta=4, nperiod=1, mode=3,
+                                     seed=14), {1})
+    _engine_vs_oracle(sg, oracle, pb, 3, P, *tols)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_engine_empty_work_list(sg, prec):
+    """No solves: zero kernels and misfit, every launch still well formed."""
+    P = sg.PREC_FP64 if prec == "fp64" else sg.PREC_FP32
+    pb = W.flat_case(nx=30, ny=28, nsta=4, nperiod=2, mode=3, seed=15).subset([])
+    assert pb.nsolve == 0
+    eng = sg.Engine(0)
+    got = eng.evaluate(pb, mode=3, precision=P)
+    eng.close()
+    assert got["chi"] == 0.0
+    assert not np.any(got["adj_s"]) and not np.any(got["adj_density"])
+
+
+def test_engine_fp32_team_source_on_boundary(sg, oracle):
+    """A source on the grid boundary of a team grid (200 rows): that solve
+    reports it and contributes nothing; the others match the oracle."""
+    pb = W.flat_case(nx=40, ny=200, d=0.02, nsta=4, nperiod=1, mode=2, seed=16)
+    xx, _ = pb.grid(0)
+    pb.srcx[2] = xx[-1] - 0.001
+    eng = sg.Engine(0)
+    got = eng.evaluate(pb, mode=2, precision=sg.PREC_FP32)
+    eng.close()
+    ref = oracle.gradient_eval(pb, mode=2, nthreads=4)
+    assert got["status"][2] == sg.SOURCE_ON_BOUNDARY == ref["status"][2]
+    assert np.all(got["status"] == ref["status"])
+    assert rel_max(got["adj_s"], ref["adj_s"]) <= KER_TOL_F32
+
+
 def test_engine_uneven_grids(sg, oracle):
     pb = W.config4(nsrc=5, nperiod=3, nmax=72, nmin=40, span_deg=2.0)
     _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
