@@ -78,6 +78,32 @@ def test_adjoint_no_receivers(sg, oracle):
     assert np.array_equal(Ta, Tar)
 
 
+def test_dropins_from_concurrent_threads(sg):
+    """Callers on several host threads (the reference's MPI ranks sharing a
+    GPU): each thread's forward, adjoint and mask on its own grid give the
+    bits the same calls give alone, and each thread reads its own status."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def job(k):
+        nx, ny = 24 + 5 * k, 20 + 3 * k
+        xx, yy, a, b, c, fun = _flat(nx, ny)
+        src = (xx[nx // 3] + 0.013, yy[ny // 2] + 0.021)
+        T, st, it = sg.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, *src)
+        xr, yr = xx[[2, nx - 3, nx // 2]], yy[[ny - 3, 2, ny // 2 + 1]]
+        Ta, sta, ita = sg.fsm_o1_jse_lonlat_2d(xx, yy, a, b, c, T, xr, yr,
+                                               np.array([0.5, -1.0, 0.25]))
+        Ta = sg.mask(xx, yy, Ta, *src)
+        return T, Ta, (st, it, sta, ita)
+
+    alone = [job(k) for k in range(8)]
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        for _ in range(2):
+            mixed = list(ex.map(job, range(8)))
+            for (T, Ta, s), (T0, Ta0, s0) in zip(mixed, alone):
+                assert s == s0 and s[0] == sg.OK and s[2] == sg.OK
+                assert np.array_equal(T, T0) and np.array_equal(Ta, Ta0)
+
+
 def test_mask_dropin(sg, oracle):
     xx, yy = W.arange_grid(100, 30, 0.05), W.arange_grid(22, 25, 0.05)
     t = np.random.default_rng(1).normal(size=(30, 25))
