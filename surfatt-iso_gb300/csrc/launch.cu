@@ -111,6 +111,17 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     nonempty += sh.team_count[c] > 0;
     counted += sh.team_count[c];
   }
+  if (p.kind == KK_FP32_WARP && nonempty == 1 && counted == sh.nsolve) {
+    // one class: the team of its tallest grid (periods without solves, e.g.
+    // a work list over some of a model's periods, do not widen it)
+    for (int c = 0; c < kTeamClasses; ++c)
+      if (sh.team_count[c] > 0) {
+        p.bands = fp32w_bands(sh.team_max_ny[c]);
+        p.block = 32 * fp32w_team(sh.team_max_ny[c]);
+        p.per_sm = std::max(1, batch_fp32w_max_blocks_per_sm(p.bands, p.pf));
+        p.grid = grid_for(p.per_sm, sh.nsolve);
+      }
+  }
   if (p.kind == KK_FP32_WARP && nonempty > 1 && counted == sh.nsolve) {
     p.classes = 0;
     p.grid = 0;

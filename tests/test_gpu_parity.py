@@ -327,6 +327,29 @@ def test_fp32_team_classes(sg, oracle, variant):
         assert rel_max(full["adj_density"], ref["adj_density"]) <= KER_TOL_F32
 
 
+def test_fp32_single_class_ignores_periods_without_solves(sg):
+    """Solves of one team class in a problem that also holds taller grids
+    without solves run on their own class's team (two warps for 192 rows,
+    not the three a 304-row grid would need) and give the bits they give in
+    the full multi-class batch."""
+    pb = W.config4(nsrc=4, nperiod=5, nmax=300, nmin=48, span_deg=2.0, seed=42)
+    sel = [s for s in range(pb.nsolve) if 128 < pb.ny[pb.pidx[s]] <= 256]
+    assert sel and int(np.max(pb.ny)) > 256
+    eng = sg.Engine(0)
+    full = eng.evaluate(pb, mode=3, precision=sg.PREC_FP32)
+    sub = pb.subset(sel)
+    eng.load(sub)
+    eng.run(3, sg.PREC_FP32)
+    assert eng.sync() == sg.OK
+    assert eng.launch_config()["block"] == 64
+    one = eng.results()
+    eng.close()
+    for q, s in enumerate(sel):
+        r0, nr = int(pb.rec_off[s]), int(pb.nrec[s])
+        q0 = int(sub.rec_off[q])
+        assert np.array_equal(one["tt_fwd"][q0:q0 + nr], full["tt_fwd"][pb.path[r0:r0 + nr]])
+
+
 def _drop_receivers(pb, solves):
     """The problem with the receiver lists of `solves` emptied (the other
     solves keep theirs and their path indices)."""
