@@ -139,9 +139,11 @@ def _max_over_ranks(dist, v, local):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling (every 50 ms) around the timed region: start()
+    returns once the sampler has written its first sample, and stop() keeps
+    the samples stamped between the two calls."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -149,18 +151,27 @@ class Clocks:
         self.index = index
         self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
         self.p = None
+        self.t0 = self.t1 = 0.0
 
     def start(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+        deadline = time.time() + 2.0
+        while self.p is not None and time.time() < deadline:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.01)
+        self.t0 = time.time()
 
     def stop(self):
+        self.t1 = time.time()
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.06)  # the sample that closes the window
         self.p.terminate()
         try:
             self.p.wait(timeout=5)
@@ -168,26 +179,29 @@ class Clocks:
             self.p.kill()
         self.f.flush()
         self.f.seek(0)
-        sm, smax, reasons, power = [], [], set(), []
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        import datetime
+        rows = []
         for line in self.f.read().strip().splitlines():
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-                power.append(float(parts[3]))
+                t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((t, float(parts[2]), float(parts[3]), float(parts[4]), parts[6:10]))
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
         os.unlink(self.f.name)
-        return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(smax) if smax else None,
-                "power_w_max": max(power) if power else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+        inside = [r for r in rows if self.t0 - 0.06 <= r[0] <= self.t1 + 0.06]
+        window = "timed region"
+        if not inside:
+            inside, window = rows, "whole sampling (no sample inside the timed region)"
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = {n for r in inside for n, v in zip(names, r[4]) if v.lower() == "active"}
+        return {"sm_mhz": statistics.median(r[1] for r in inside) if inside else None,
+                "sm_max_mhz": max(r[2] for r in inside) if inside else None,
+                "power_w_max": max(r[3] for r in inside) if inside else None,
+                "samples": len(inside), "window": window,
+                "region_s": round(self.t1 - self.t0, 3), "reasons": sorted(reasons)}
 
 
 def _flush_l2(buf):
