@@ -327,6 +327,20 @@ def test_fp32_team_classes(sg, oracle, variant):
         assert rel_max(full["adj_density"], ref["adj_density"]) <= KER_TOL_F32
 
 
+def test_engine_fp32_wide_grid_block_kernel(sg, oracle):
+    """A grid wider than the row kernel's column limit (4096) runs on the
+    block-per-solve kernel, automatically, within the FP32 tolerances."""
+    pb = W.flat_case(nx=4104, ny=10, d=0.001, nsta=3, nperiod=1, mode=2, seed=17)
+    eng = sg.Engine(0)
+    got = eng.evaluate(pb, mode=2, precision=sg.PREC_FP32)
+    assert eng.kernel_variant()["kind"] == 1
+    eng.close()
+    ref = oracle.gradient_eval(pb, mode=2, nthreads=4)
+    assert np.all(got["status"] == ref["status"])
+    assert rel_pointwise(got["tt_fwd"], ref["tt_fwd"]) <= TT_TOL_F32
+    assert rel_max(got["adj_s"], ref["adj_s"]) <= KER_TOL_F32
+
+
 def test_fp32_single_class_ignores_periods_without_solves(sg):
     """Solves of one team class in a problem that also holds taller grids
     without solves run on their own class's team (two warps for 192 rows,
