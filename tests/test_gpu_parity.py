@@ -327,6 +327,13 @@ def test_fp32_team_classes(sg, oracle, variant):
         assert rel_max(full["adj_density"], ref["adj_density"]) <= KER_TOL_F32
 
 
+def test_engine_fp64_large_grid(sg, oracle):
+    """The plain FP64 path on a 220 x 300 grid: anti-diagonals longer than its
+    128-thread block, within the plain tolerances."""
+    pb = W.flat_case(nx=220, ny=300, d=0.01, nsta=3, nperiod=1, mode=3, seed=18)
+    _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
+
+
 def test_engine_fp32_wide_grid_block_kernel(sg, oracle):
     """A grid wider than the row kernel's column limit (4096) runs on the
     block-per-solve kernel, automatically, within the FP32 tolerances."""
