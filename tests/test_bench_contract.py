@@ -6,6 +6,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -43,3 +45,22 @@ def test_workload_choices():
     for w in ("config1", "config2", "config4", "serving", "dropin", "smooth", "kernel3d",
               "worklist", "topo"):
         assert w in out.stdout, w
+
+
+@pytest.mark.gpu
+def test_our_arm_line():
+    d = _run(["--workload", "config1", "--steps", "3", "--warmup", "3", "--no-cpu-baseline"],
+             timeout=900)
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "e2e",
+              "gpu_launches", "roofline", "clocks"):
+        assert k in d, k
+    assert d["value"] > 0 and d["n_gpus"] == 1 and d["gpu_launches"] > 0
+    r = d["roofline"]
+    for k in ("bound", "achieved", "peak", "unit", "frac"):
+        assert k in r, k
+    assert 0 < r["frac"] < 2
+    e = d["e2e"]
+    assert e["value"] > 0 and e["h2d_bytes_per_step"] > 0 and e["d2h_bytes_per_step"] > 0
+    c = d["clocks"]
+    assert "sm_mhz" in c and "reasons" in c
