@@ -397,7 +397,13 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* engine, const surfatt_pro
  * trial model or the next inversion iterate); same layout as pb->svel. */
 surfatt_status_t surfatt_engine_update_velocity(surfatt_engine_t* engine, const double* svel);
 
-/* Launch one gradient evaluation on the engine's stream (asynchronous). */
+/* Launch one gradient evaluation on the engine's stream (asynchronous).
+ * SURFATT_PREC_FP32 runs, unless surfatt_engine_set_kernel or the autotuner
+ * chose otherwise, the row-per-lane kernel: one warp per solve on grids of
+ * at most 128 rows, a team of 2 - 4 warps per solve up to 512 rows (taller
+ * or wider than 4096 columns: one block per solve).  A batch that mixes
+ * grid heights runs as one launch per team class, concurrently on the
+ * engine's side streams; each solve's results are the same as alone. */
 surfatt_status_t surfatt_engine_run(surfatt_engine_t* engine, surfatt_mode_t mode,
                                     surfatt_precision_t precision);
 
