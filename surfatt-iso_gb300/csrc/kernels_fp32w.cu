@@ -286,12 +286,16 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
             res[m] = nv;
             t0prev[m] = cur[m].t0;
           }
-          cur[m] = nxt[m];
           if (NW > 1 && m == MB - 1 && top) {
             xs_val[t & 1][T.wid] = res[m];
             xs_t0[t & 1][T.wid] = t0prev[m];
           }
         }
+        // the next step's operands, after every band's visit (the latest
+        // point: the loads issued at the start of this step have the whole
+        // step to arrive)
+#pragma unroll
+        for (int m = 0; m < MB; ++m) cur[m] = nxt[m];
         if (last) {
           // in band order (the order of the row-major visit of a lane)
 #pragma unroll
@@ -484,8 +488,11 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
             }
             res[m] = val;
           }
-          cur[m] = nxt[m];
         }
+        // the next step's operands after every band's visit (as in the
+        // forward sweeps)
+#pragma unroll
+        for (int m = 0; m < MB; ++m) cur[m] = nxt[m];
         if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
         pn = qn;
         tsync<NW>();
