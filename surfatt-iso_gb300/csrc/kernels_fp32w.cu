@@ -160,7 +160,9 @@ __device__ __forceinline__ void wf_load_heavy(WFwd& o, int k, const PeriodDev& P
 
 // HEAVY: also load the constants now (a step ahead of their use) rather
 // than at the visit.
-template <bool HEAVY>
+// EXCH: also the values the lanes exchange (own, t0); else the caller
+// supplies them.
+template <bool HEAVY, bool EXCH = true>
 __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, int xdir, int ydir,
                                         const PeriodDev& P, const WSlot& V, const Box& box,
                                         bool last) {
@@ -175,14 +177,29 @@ __device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, i
   const int j = ydir > 0 ? v : ny - 1 - v;
   const int k = i + nx * j;
   o.frz = box.has(i, j);
-  o.own = V.tau[k];
-  o.t0 = reinterpret_cast<const float*>(V.S)[4 * k];
+  if (EXCH) {
+    o.own = V.tau[k];
+    o.t0 = reinterpret_cast<const float*>(V.S)[4 * k];
+  }
   if (HEAVY) {
     wf_load_heavy(o, k, P, V);
     if (last) o.old = V.old[k];
   }
 }
 
+
+// The value and T0 of row v's cell at step t (0 off the grid).
+__device__ __forceinline__ void wf_exch(float& own, float& t0, int t, int v, int nx, int ny,
+                                        int xdir, int ydir, const WSlot& V) {
+  const int u = t - v;
+  own = 0.f;
+  t0 = 0.f;
+  if (v < ny && u >= 0 && u < nx) {
+    const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? v : ny - 1 - v);
+    own = V.tau[k];
+    t0 = reinterpret_cast<const float*>(V.S)[4 * k];
+  }
+}
 
 // PF = 1: every operand of the next step is loaded a step ahead; PF = 0:
 // only the values exchanged between lanes are, the cell's constants are
@@ -227,22 +244,37 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
           t0 = reinterpret_cast<const float*>(V.S)[4 * k];
         }
       };
-      float res[MB], t0prev[MB];
+      // With register prefetch a single warp loads the values the lanes
+      // exchange within a step (the next cell's tau and T0) two steps ahead,
+      // the other operands one (a cell is written only at its own visit).
+      // (Teams keep one step: the extra registers spill in their loop.)
+      constexpr bool EX2 = PF == 1 && NW == 1;
+      float res[MB], t0prev[MB], own2[MB], t02[MB];
       WFwd cur[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
         t0prev[m] = 0.f;
         wf_load<PF == 1>(cur[m], 0, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
+        if (EX2) wf_exch(own2[m], t02[m], 1, vb + lane + 32 * m, nx, ny, xdir, ydir, V);
       }
       float pn_own = 0.f, pn_t0 = 0.f;
       if (top) north_of_top(0, pn_own, pn_t0);
       for (int t = 0; t < nsteps; ++t) {
         WFwd nxt[MB];
 #pragma unroll
-        for (int m = 0; m < MB; ++m)
-          wf_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box,
-                           last);
+        for (int m = 0; m < MB; ++m) {
+          if (EX2) {
+            wf_load<true, false>(nxt[m], t + 1, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V,
+                                 w.box, last);
+            nxt[m].own = own2[m];
+            nxt[m].t0 = t02[m];
+            wf_exch(own2[m], t02[m], t + 2, vb + lane + 32 * m, nx, ny, xdir, ydir, V);
+          } else {
+            wf_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box,
+                             last);
+          }
+        }
         float qn_own = 0.f, qn_t0 = 0.f;
         if (top) north_of_top(t + 1, qn_own, qn_t0);
         // Bands in descending order: band m's south neighbours include lane 31
