@@ -40,11 +40,11 @@ ADJ_FLOPS_PER_VISIT = 16.0
 KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w", 3: "k_batch_fp32d"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # FP32 row kernel (k_batch_fp32w), from one ncu capture of the 320-solve case
-# (1.603 GB read + 0.629 GB written), scaled by the solves for the 1280-solve
+# (1.670 GB read + 0.641 GB written), scaled by the solves for the 1280-solve
 # workload (the per-solve workspace and operands are the same for every
 # solve): profiles/k_batch_fp32w_config2s.md.  Reported only when the
 # autotuner picked that kernel.
-DRAM_BYTES_PER_LAUNCH = {"config2": 8.929e9, "config2s": 2.232e9}
+DRAM_BYTES_PER_LAUNCH = {"config2": 9.245e9, "config2s": 2.311e9}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
 
 
