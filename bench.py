@@ -230,7 +230,6 @@ def _time_steps(eng, pb, prec, steps, warmup, flush):
 
 
 def _errors(a, b, pb):
-    from surfatt_gb300 import workloads as W  # noqa: F401
     out = {}
     m = b["tt_fwd"] != 0
     out["tt_rel_max"] = float(np.max(np.abs(a["tt_fwd"][m] - b["tt_fwd"][m]) / np.abs(b["tt_fwd"][m])))
@@ -928,7 +927,6 @@ def _run_reference_dropin(args, O, dist):
     and mask per source, sources split over one process per core (the
     reference's MPI ranks)."""
     import multiprocessing as mp
-    from surfatt_gb300 import workloads as W
     nthr = os.cpu_count() or 1
     pb, xx, yy, a, b, c, fun, srcs = _dropin_case()
     _dropin_sadj(srcs, O.gradient_eval(pb, mode=2, nthreads=nthr)["tt_fwd"])
@@ -1299,7 +1297,6 @@ def run_topo(args):
     e2e_s = _max_over_ranks(dist, statistics.mean(walls), dev)
     cpu, parity = None, {}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        import multiprocessing as mp
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
         O.build()
