@@ -81,6 +81,8 @@ def _args():
                     help="smooth: smoothing length in degrees (the example's sigma_2d)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the config 4 and serving side runs")
     return ap.parse_args()
 
 
@@ -211,16 +213,37 @@ def _flush_l2(buf):
     torch.cuda.synchronize()
 
 
-def _time_steps(eng, pb, prec, steps, warmup, flush):
+def _reduce_step(eng, dist):
+    """The evaluation's exchange step on N ranks: one NCCL all-reduce of this
+    rank's adj_s, adj_density, tt_fwd and chi (device memory, no host copy);
+    returns its device time in ms (CUDA events on torch's current stream)."""
+    import torch
+    from surfatt_gb300 import parallel as par
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    out = par.reduce_device(eng.device_results(), dist)
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b), out
+
+
+def _time_steps(eng, pb, prec, steps, warmup, flush, dist=None):
+    """Per step: the evaluation's device time (CUDA events on the engine's
+    stream) plus, on N > 1 ranks, the all-reduce's (events on the stream it
+    runs on)."""
     for _ in range(warmup):
         eng.run(pb.mode, prec)
         eng.sync()
+        if dist is not None:
+            _reduce_step(eng, dist)
     totals, kernels, launches = [], [], 0
     for _ in range(steps):
         _flush_l2(flush)
         eng.run(pb.mode, prec)
         st = eng.sync()
         t, k, n = eng.timing()
+        if dist is not None:
+            t += _reduce_step(eng, dist)[0]
         totals.append(t)
         kernels.append(k)
         launches += n
@@ -243,6 +266,50 @@ def _errors(a, b, pb):
                 worst = max(worst, float(np.max(np.abs(a[key][g0:g0 + n] - b[key][g0:g0 + n])) / den))
         out[key + "_rel_max_per_period"] = worst
     return out
+
+
+def _errors_per_period(a, b, pb):
+    """Per period: travel times at the receivers (max pointwise relative
+    error), the period's misfit (0.5 sum w (t - tt)^2 over its paths, from
+    each side's synthetic times), and adj_s / adj_density (max norm-wise
+    relative error).  a: result under test, b: reference result."""
+    rows = []
+    pid = np.asarray(pb.pidx)
+    for p in range(pb.nperiod):
+        sol = np.flatnonzero(pid == p)
+        if len(sol) == 0:
+            continue
+        ridx = np.concatenate([np.arange(pb.rec_off[s], pb.rec_off[s] + pb.nrec[s]) for s in sol])
+        paths = np.asarray(pb.path)[ridx]
+        ta, tb = a["tt_fwd"][paths], b["tt_fwd"][paths]
+        m = tb != 0
+        w, tt = np.asarray(pb.weight)[ridx], np.asarray(pb.tt)[ridx]
+        ca = 0.5 * np.sum(w * (ta - tt) ** 2)
+        cb = 0.5 * np.sum(w * (tb - tt) ** 2)
+        g0, n = int(pb.goff[p]), int(pb.nx[p] * pb.ny[p])
+        row = {"period": p, "grid": f"{int(pb.nx[p])}x{int(pb.ny[p])}", "solves": int(len(sol)),
+               "tt_rel_max": float(np.max(np.abs(ta[m] - tb[m]) / np.abs(tb[m]))) if m.any() else 0.0,
+               "chi_rel": float(abs(ca - cb) / abs(cb)) if cb else 0.0}
+        for key in ("adj_s", "adj_density"):
+            den = np.max(np.abs(b[key][g0:g0 + n]))
+            row[key + "_rel"] = float(np.max(np.abs(a[key][g0:g0 + n] - b[key][g0:g0 + n])) / den) \
+                if den > 0 else 0.0
+        rows.append(row)
+    return rows
+
+
+def _config(pb, desc, world):
+    """The `config` object of both arms' JSON lines (same keys, same values)."""
+    grids = sorted({f"{int(x)}x{int(y)}" for x, y in zip(pb.nx, pb.ny)})
+    return {"workload": desc, "solves_per_step": int(pb.nsolve),
+            "grid": grids[0] if len(grids) == 1 else grids,
+            "periods": int(pb.nperiod), "receivers": int(len(pb.tt)),
+            "mode": {3: "3-D (adj and density /svel^3)", 2: "2-D (adj /svel^2)",
+                     0: "forward only"}[int(pb.mode)],
+            "l2": "flushed (256 MB write) between timed steps",
+            "parallelism": (f"{world} GPU(s): the work list split by predicted cost (cells x "
+                            f"iterations), one NCCL all-reduce of adj_s, adj_density, tt_fwd and "
+                            f"chi per step" if world > 1 else "1 GPU")}
 
 
 def _pinned_problem(pb):
@@ -273,9 +340,13 @@ def _pinned_problem(pb):
 def run_ours(args):
     import torch
     import surfatt_gb300 as sg
+    from surfatt_gb300 import parallel as par
     dist, rank, world, local = _dist()
     sg.build()
-    pb, desc = _workload(args.workload)
+    pb_full, desc = _workload(args.workload)
+    # N ranks: one gradient evaluation split by predicted cost, each rank its
+    # shard (same periods and path table), results summed every step
+    pb = par.shard(pb_full, world, rank) if world > 1 else pb_full
     dev = local
     torch.cuda.set_device(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=f"cuda:{dev}")
@@ -303,13 +374,13 @@ def run_ours(args):
     _barrier(dist, dev)
     clocks.start()
     t0 = time.perf_counter()
-    t32, k32, launches = _time_steps(eng, pb, sg.PREC_FP32, args.steps, args.warmup, flush)
+    t32, k32, launches = _time_steps(eng, pb, sg.PREC_FP32, args.steps, args.warmup, flush, dist)
     wall = time.perf_counter() - t0
     _barrier(dist, dev)
     ck = clocks.stop()
     ms_step = statistics.mean(t32)
     ms_step_max = _max_over_ranks(dist, ms_step, dev)
-    value = pb.nsolve * world / (ms_step_max / 1e3)
+    value = pb_full.nsolve / (ms_step_max / 1e3)
 
     e2e = None
     if not args.no_e2e:
@@ -335,12 +406,20 @@ def run_ours(args):
             eng.load(ppb)
             eng.run(pb.mode, sg.PREC_FP32)
             eng.sync()
-            eng.results(into=into)
+            if dist is not None:
+                # this rank's per-solve results, then the sums over the ranks
+                eng.results(adj=False, density=False, tt=False, into=into)
+                red = _reduce_step(eng, dist)[1]
+                for k in ("adj_s", "adj_density", "tt_fwd", "chi"):
+                    if red[k] is not None:
+                        torch.from_numpy(into[k][:red[k].numel()]).copy_(red[k])
+            else:
+                eng.results(into=into)
             b = time.perf_counter()
             if i >= args.warmup:
                 e2e_t.append(b - a)
         e2e_s = _max_over_ranks(dist, statistics.mean(e2e_t), dev)
-        e2e = {"value": pb.nsolve * world / e2e_s, "unit": "solves/s",
+        e2e = {"value": pb_full.nsolve / e2e_s, "unit": "solves/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned"}
 
@@ -369,28 +448,36 @@ def run_ours(args):
         import oracle as O
         O.build()
         nthr = os.cpu_count() or 1
-        a = time.perf_counter()
+        # parity against the -ffp-contract=off build (untimed), the CPU
+        # baseline timed on the -O3 build of the same sources
         ref = O.gradient_eval(pb, mode=pb.mode, nthreads=nthr)
+        a = time.perf_counter()
+        O.gradient_eval(pb, mode=pb.mode, nthreads=nthr, timed=True)
         b = time.perf_counter()
         cpu = {"value": pb.nsolve / (b - a), "unit": "solves/s", "cores": nthr, "kind": "port",
                "sample": f"the full workload ({pb.nsolve} solves), one evaluation, "
                          f"{nthr} threads, contiguous work-list blocks",
-               "seconds": b - a}
-        parity = {"fp64_vs_oracle": _errors(r64, ref, pb), "fp32_vs_oracle": _errors(r32, ref, pb)}
+               "build": O.FAST_FLAGS, "seconds": b - a}
+        parity = {"fp64_vs_oracle": _errors(r64, ref, pb), "fp32_vs_oracle": _errors(r32, ref, pb),
+                  "oracle_build": O.STRICT_FLAGS,
+                  "fp32_vs_oracle_per_period": _errors_per_period(r32, ref, pb),
+                  "fp64_vs_oracle_per_period": _errors_per_period(r64, ref, pb)}
+
+    side = {}
+    if rank == 0 and world == 1 and not args.no_extras and args.workload == "config2":
+        side["config4"] = _side_config4(sg, flush, dev)
+        side["serving"] = _side_serving(sg, dev)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step_max,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
             "dtype": "f32 sweep / f64 T0, misfit, kernels", "data": "synthetic",
-            "config": {"workload": desc, "solves_per_step": pb.nsolve, "grid": "120x120",
-                       "periods": int(pb.nperiod), "receivers": int(len(pb.tt)),
-                       "mode": "3-D (adj and density /svel^3)", "l2": "flushed (256 MB write) between timed steps",
-                       "parallelism": f"{world} GPU(s), one engine per GPU, independent evaluations"},
+            "config": _config(pb_full, desc, world),
             "p50_ms": statistics.median(t32), "p99_ms": float(np.percentile(t32, 99)),
             "cell_updates_per_s": (fwd32 + adj32) * world / (ms_step_max / 1e3),
-            "plain_fp64": {"value": pb.nsolve * world / (statistics.mean(t64) / 1e3),
+            "plain_fp64": {"value": pb_full.nsolve / (statistics.mean(t64) / 1e3),
                            "unit": "solves/s", "ms_per_step": statistics.mean(t64),
                            "solve_kernel_ms": k64_ms, "achieved_tflops": ach64,
                            "peak_tflops_fp64": fp64_peak, "frac": ach64 / fp64_peak},
@@ -413,6 +500,7 @@ def run_ours(args):
                            "adj_mean": float(np.mean(r32["adj_iters"]))},
             "wall_s_timed_region": wall,
         }
+        line.update(side)
         print(json.dumps(line))
     eng.close()
     if dist is not None:
@@ -442,11 +530,11 @@ def run_reference(args):
     pb, desc = _workload(args.workload)
     nthr = os.cpu_count() or 1
     for _ in range(args.warmup):
-        O.gradient_eval(pb, mode=pb.mode, nthreads=nthr)
+        O.gradient_eval(pb, mode=pb.mode, nthreads=nthr, timed=True)
     ts = []
     for _ in range(args.steps):
         a = time.perf_counter()
-        r = O.gradient_eval(pb, mode=pb.mode, nthreads=nthr)
+        r = O.gradient_eval(pb, mode=pb.mode, nthreads=nthr, timed=True)
         ts.append(time.perf_counter() - a)
         if r["rc"] not in (0, 3):
             raise RuntimeError(f"oracle status {r['rc']}")
@@ -454,10 +542,11 @@ def run_reference(args):
     v = pb.nsolve / s
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": s * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": desc, "solves_per_step": pb.nsolve},
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": _config(pb, desc, world),
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": nthr, "kind": "port",
-                             "sample": f"the full workload ({pb.nsolve} solves) per step"},
+                             "sample": f"the full workload ({pb.nsolve} solves) per step",
+                             "build": O.FAST_FLAGS},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "note": "reference Fortran cannot be built (no Fortran compiler); its algorithm "
@@ -506,6 +595,99 @@ def _run_reference_smooth(args, O, dist):
         dist.destroy_process_group()
 
 
+def _latency_breakdown(reqs, lat):
+    """p50 / p99 request latency per grid side and per request kind, with
+    the requests' solve counts: whether a tail is queueing or the large
+    grids' own run time."""
+    out = {}
+    for key, groups in (("by_grid", sorted({r["n"] for r in reqs})),
+                        ("by_kind", ("gradient", "linesearch", "checkerboard"))):
+        tab = {}
+        for g in groups:
+            idx = [q for q, r in enumerate(reqs) if r["n" if key == "by_grid" else "kind"] == g]
+            if not idx:
+                continue
+            v = np.asarray([lat[q] for q in idx])
+            tab[f"{g}^2" if key == "by_grid" else g] = {
+                "requests": len(idx), "solves_mean": float(np.mean([reqs[q]["nsolve"] for q in idx])),
+                "p50_ms": float(np.percentile(v, 50)), "p99_ms": float(np.percentile(v, 99))}
+        out[key] = tab
+    return out
+
+
+def _serving_measure(sg, S, local, nreq, load, warmup, dist=None):
+    """Closed-loop capacity, then a Poisson stream at `load` of it."""
+    cat = S.Catalog()
+    reqs = S.make_requests(cat, nreq, seed=4)
+    srv = sg.Server(local, hbm_budget_bytes=16 << 30, max_inflight=8)
+    mids = {n: srv.add_model(cat.models[n]) for n in cat.models}
+    # warm-up: the first requests of the stream, run once and discarded
+    warm = S.run_poisson(srv, reqs[:max(3, warmup)], 1e6, sg.PREC_FP32, model_ids=mids)
+    closed = S.run_poisson(srv, reqs, 1e6, sg.PREC_FP32, model_ids=mids)
+    cap_rate = len(reqs) / closed["wall_s"]
+    rate = load * cap_rate
+    clocks = Clocks(local)
+    _barrier(dist, local)
+    clocks.start()
+    res = S.run_poisson(srv, reqs, rate, sg.PREC_FP32, seed=5, model_ids=mids)
+    _barrier(dist, local)
+    ck = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    return cat, reqs, warm, closed, res, cap_rate, rate, ck, st
+
+
+def _side_serving(sg, dev):
+    """The serving loop beside the headline (30 requests at 70 % of the
+    closed-loop capacity): solves/s, p50 / p99 and their breakdown."""
+    from surfatt_gb300 import serving as S
+    cat, reqs, warm, closed, res, cap, rate, ck, st = _serving_measure(sg, S, dev, 30, 0.7, 3)
+    lat = np.asarray(res["latency_ms"])
+    bad = [x for x in res["status"] + closed["status"] + warm["status"] if x not in (0, 3)]
+    return {"metric": "serving solves/s (Poisson request stream, FP32-factored)",
+            "value": res["solves"] / res["wall_s"], "unit": "solves/s",
+            "requests": len(reqs), "solves": res["solves"], "load": 0.7,
+            "offered_rate_per_s": rate, "closed_loop_rate_per_s": cap,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "closed_loop_solves_per_s": closed["solves"] / closed["wall_s"],
+            "breakdown": _latency_breakdown(reqs, lat), "failed_requests": len(bad),
+            "inflight_peak": st["inflight_peak"], "clocks": ck}
+
+
+def _side_config4(sg, flush, dev):
+    """Config 4 beside the headline: 120 sources x 25 periods = 3000 solves
+    on grids of 64^2 .. 384^2 (3-D mode), FP32-factored and plain FP64 on
+    the same engine, each timed with CUDA events on the engine's stream (L2
+    flushed between steps), the FP32 error against the FP64 results."""
+    from surfatt_gb300 import workloads as W
+    pb = W.config4()
+    eng = sg.Engine(dev)
+    eng.load(pb)
+    eng.run(pb.mode, sg.PREC_FP64)
+    eng.sync()
+    r64 = eng.results()
+    eng.run(pb.mode, sg.PREC_FP32)
+    eng.sync()
+    r32 = eng.results()
+    variant = eng.kernel_variant()
+    t64, k64, _ = _time_steps(eng, pb, sg.PREC_FP64, 2, 1, flush)
+    clocks = Clocks(dev)
+    clocks.start()
+    t32, k32, n32 = _time_steps(eng, pb, sg.PREC_FP32, 3, 2, flush)
+    ck = clocks.stop()
+    eng.close()
+    ms32, ms64 = statistics.mean(t32), statistics.mean(t64)
+    return {"workload": "config4: 120 sources x 25 periods = 3000 solves, grids 64^2..384^2, "
+                        "3-D mode", "solves_per_step": pb.nsolve,
+            "fp32": {"value": pb.nsolve / (ms32 / 1e3), "unit": "solves/s", "ms_per_step": ms32,
+                     "solve_kernel_ms": statistics.mean(k32), "steps": 3, "warmup": 2,
+                     "kernel": variant, "gpu_launches": n32},
+            "plain_fp64": {"value": pb.nsolve / (ms64 / 1e3), "unit": "solves/s",
+                           "ms_per_step": ms64, "solve_kernel_ms": statistics.mean(k64)},
+            "speedup_fp32_vs_fp64": ms64 / ms32,
+            "fp32_vs_fp64_error": _errors(r32, r64, pb), "clocks": ck}
+
+
 def run_serving(args):
     """Serving workload (curved surface, seed 4): a closed-loop pass (every
     request queued at once) measures the server's capacity; the Poisson
@@ -517,22 +699,8 @@ def run_serving(args):
     dist, rank, world, local = _dist()
     sg.build()
     torch.cuda.set_device(local)
-    cat = S.Catalog()
-    reqs = S.make_requests(cat, args.requests, seed=4)
-    srv = sg.Server(local, hbm_budget_bytes=16 << 30, max_inflight=8)
-    mids = {n: srv.add_model(cat.models[n]) for n in cat.models}
-    # warm-up: the first requests of the stream, run once and discarded
-    warm = S.run_poisson(srv, reqs[:max(3, args.warmup)], 1e6, sg.PREC_FP32, model_ids=mids)
-    closed = S.run_poisson(srv, reqs, 1e6, sg.PREC_FP32, model_ids=mids)
-    cap_rate = len(reqs) / closed["wall_s"]
-    rate = args.load * cap_rate
-    clocks = Clocks(local)
-    _barrier(dist, local)
-    clocks.start()
-    res = S.run_poisson(srv, reqs, rate, sg.PREC_FP32, seed=5, model_ids=mids)
-    _barrier(dist, local)
-    ck = clocks.stop()
-    st = srv.stats()
+    cat, reqs, warm, closed, res, cap_rate, rate, ck, st = _serving_measure(
+        sg, S, local, args.requests, args.load, args.warmup, dist)
     lat = np.asarray(res["latency_ms"])
     bad = [s for s in res["status"] + closed["status"] + warm["status"] if s not in (0, 3)]
     wall = _max_over_ranks(dist, res["wall_s"], local)
@@ -558,9 +726,9 @@ def run_serving(args):
                             "p50_ms": float(np.percentile(closed["latency_ms"], 50)),
                             "p99_ms": float(np.percentile(closed["latency_ms"], 99))},
             "server_stats": st, "failed_requests": len(bad), "clocks": ck,
+            "breakdown": _latency_breakdown(reqs, lat),
         }
         print(json.dumps(line))
-    srv.close()
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()

@@ -479,6 +479,40 @@ surfatt_status_t surfatt_engine_kernel_variant(surfatt_engine_t* engine, int* ki
  * grow, makes the next run capture again; a velocity update does not. */
 surfatt_status_t surfatt_engine_set_graphs(surfatt_engine_t* engine, int enable);
 
+/* Keep every solve's travel-time field T = tau*T0 of later runs (default
+ * off; forward grids of the solves one after another, solve s at the offset
+ * of its kernel slot: sum over the solves before it of nx*ny of their
+ * periods), and copy the last run's fields to `T` (host, that many doubles).
+ * The fields are what FSM_UW_PS_lonlat_2d returns per solve
+ * (src/eikon_solver_2d.f90:1124; src/measadj.f90:68-70), for checks of the
+ * whole field rather than its receiver values.  A solve that failed has a
+ * zero field. */
+surfatt_status_t surfatt_engine_set_keep_fields(surfatt_engine_t* engine, int enable);
+surfatt_status_t surfatt_engine_fields(surfatt_engine_t* engine, double* T);
+
+/* Test hook of the bounded device wait (no counterpart in the reference;
+ * default solve = -1: off).  With the FP32 row kernel cutting solves into
+ * work items, the first item of `solve` is skipped without being marked
+ * done, so the solve's next item waits for it until wait_polls polls (0:
+ * the production limit of 2^24) have run out; the solve then ends with
+ * SURFATT_TIMEOUT and contributes nothing, every other solve completes.
+ * The wait is the one a real stall of a previous item would meet; nothing
+ * on the device faults or hangs. */
+surfatt_status_t surfatt_engine_test_hold(surfatt_engine_t* engine, int solve, int wait_polls);
+
+/* Device addresses of the last run's results as they sit in the engine's
+ * memory: adj_s and adj_density (ncell doubles, the problem's per-period
+ * layout; NULL when the mode does not produce them), tt_fwd (npath doubles)
+ * and chi (one double), and the engine's stream (a cudaStream_t) that wrote
+ * them.  They stay valid until the next load.  For a caller that reduces the
+ * results of several ranks on the device (the MPI_Reduce of adj_s,
+ * adj_density, chi and the synthetic-time table, src/acqui.f90:152-160,
+ * 205-206) without copying them to the host; order the reduction after the
+ * run (surfatt_engine_sync, or an event on the stream). */
+surfatt_status_t surfatt_engine_device_results(surfatt_engine_t* engine, double** adj_s,
+                                               double** adj_density, double** tt_fwd,
+                                               double** chi, void** stream);
+
 /* Total sweep cell visits of the last run (forward, adjoint), for the
  * algorithmic roofline. */
 surfatt_status_t surfatt_engine_work(surfatt_engine_t* engine, double* fwd_cell_updates,
@@ -501,8 +535,11 @@ surfatt_status_t surfatt_measure_peaks(int device, double* fp64_tflops, double* 
  * library (about 4.8 MB per GPU, held until the process exits): grids above
  * 16384 cells or 2048 nodes per axis are rejected with SURFATT_BAD_ARG.  The
  * first call on a device looks up the scratch address and should come
- * before any stream capture.  Calls share the scratch: calls that overlap on
- * the GPU race and must be ordered (one stream, or events). */
+ * before any stream capture; the address is kept for the process, so the
+ * entry point must not be called after cudaDeviceReset on that device.
+ * Calls share the scratch: calls that overlap on the GPU race and must be
+ * ordered (one stream, or events).  The return value is this launch's own
+ * error only (an error pending from earlier work is left untouched). */
 surfatt_status_t surfatt_uw_lonlat_solve_noalloc(const double* xx_deg, const double* yy_deg,
                                                  int nx, int ny, const double* spha,
                                                  const double* sphb, const double* sphc,

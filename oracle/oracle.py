@@ -17,7 +17,13 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libsurfatt_oracle.so")
+# The same sources built -O3 with FP contraction on (the timed CPU baseline
+# only; parity checks use the -ffp-contract=off build above).
+_FAST_PATH = os.path.join(_HERE, "_build", "libsurfatt_oracle_fast.so")
+FAST_FLAGS = "gcc -O3 (FP contraction: gcc default, FMA on aarch64)"
+STRICT_FLAGS = "gcc -O2 -ffp-contract=off"
 _lib = None
+_fast = None
 
 OK, SOURCE_ON_BOUNDARY, BAD_ARG, NOT_CONVERGED = 0, 1, 2, 3
 
@@ -44,6 +50,17 @@ def lib():
             _dp, _dp, ctypes.c_double, _dp, _dp, _dp] + [ctypes.c_int] * 4 + [
             _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, _dp, _dp]
     return _lib
+
+
+def fast_lib():
+    """The -O3 build of the same sources, for timing only."""
+    global _fast
+    if _fast is None:
+        if not os.path.exists(_FAST_PATH):
+            build()
+        _fast = ctypes.CDLL(_FAST_PATH)
+        _fast.orc_gradient_eval_range.argtypes = lib().orc_gradient_eval_range.argtypes
+    return _fast
 
 
 def _d(a):
@@ -153,10 +170,12 @@ class _Problem(ctypes.Structure):
                 ("weight", _dp), ("path", _ip), ("npath", ctypes.c_int)]
 
 
-def gradient_eval(pb, mode=2, nthreads=1, s_begin=0, s_end=None):
+def gradient_eval(pb, mode=2, nthreads=1, s_begin=0, s_end=None, timed=False):
     """One gradient evaluation of a packed problem (see surfatt_gb300.workloads.Problem).
 
     mode 0: forward only; 2: tomo2d (adj/svel^2); 3: 3-D (adj and density /svel^3).
+    timed: run the -O3 build (the CPU baseline's timing) instead of the
+    parity build.
     Returns dict(adj_s, adj_density, chi, tt_fwd, status, fwd_iters, adj_iters, rc).
     """
     if s_end is None:
@@ -182,7 +201,8 @@ def gradient_eval(pb, mode=2, nthreads=1, s_begin=0, s_end=None):
     status = np.zeros(pb.nsolve, np.int32)
     fit = np.zeros(pb.nsolve, np.int32)
     ait = np.zeros(pb.nsolve, np.int32)
-    rc = lib().orc_gradient_eval_range(ctypes.byref(s), mode, nthreads, s_begin, s_end,
+    rc = (fast_lib() if timed else lib()).orc_gradient_eval_range(
+        ctypes.byref(s), mode, nthreads, s_begin, s_end,
                                        _d(adj_s), _d(adj_d), ctypes.byref(chi), _d(tt_fwd),
                                        _i(status), _i(fit), _i(ait))
     return dict(adj_s=adj_s, adj_density=adj_d, chi=chi.value, tt_fwd=tt_fwd[:pb.npath],

@@ -535,6 +535,9 @@ struct surfatt_engine {
   std::vector<long long> shape_sig;  // sizes of the loaded problem (see load)
   bool use_graphs = true;
   bool profile = false;  // per-phase cycle counters of the FP32 warp kernel
+  bool keep_fields = false;  // write every solve's travel-time field (d_T)
+  DBuf d_T;
+  int hold_solve = -1, item_wait_limit = 0;  // test hooks of the bounded item wait
   void drop_graphs() {
     for (auto& m : graphs)
       for (auto& g : m) {
@@ -548,7 +551,8 @@ struct surfatt_engine {
             &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
             &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
             &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
-            &d_aupd, &d_ws, &d_queue, &d_phase, &d_q, &d_ker, &d_smtab, &d_smnyw, &d_smper};
+            &d_aupd, &d_ws, &d_queue, &d_phase, &d_q, &d_ker, &d_smtab, &d_smnyw, &d_smper,
+            &d_T};
   }
 };
 
@@ -869,6 +873,13 @@ int engine_enqueue(surfatt_engine* e, int mode, int prec, const KernelChoice& fo
   A.fwd_updates = e->d_fupd.as<double>();
   A.adj_updates = e->d_aupd.as<double>();
   A.Tout = nullptr;
+  if (e->keep_fields) {
+    r = eng_ensure(e, e->d_T, (size_t)std::max(1LL, e->kslot_total) * sizeof(double));
+    if (r) return r;
+    A.Tout = e->d_T.as<double>();
+  }
+  A.hold_solve = e->hold_solve;
+  A.item_wait_limit = e->item_wait_limit;
   if (e->profile) {
     r = eng_ensure(e, e->d_phase, PH_COUNT * sizeof(unsigned long long));
     if (r) return r;
@@ -1142,6 +1153,42 @@ surfatt_status_t surfatt_engine_kernel_variant(surfatt_engine_t* e, int* kind, i
   if (!e || !e->ran) return SURFATT_BAD_ARG;
   if (kind) *kind = e->last_kind;
   if (pf) *pf = e->last_pf;
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_set_keep_fields(surfatt_engine_t* e, int enable) {
+  if (!e) return SURFATT_BAD_ARG;
+  e->keep_fields = enable != 0;
+  ++e->gen;  // the kernel arguments change
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_fields(surfatt_engine_t* e, double* T) {
+  if (!e || !e->ran || !e->keep_fields || !T || !e->d_T.p) return SURFATT_BAD_ARG;
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->st));
+  if (e->kslot_total > 0)
+    CK(cudaMemcpy(T, e->d_T.p, (size_t)e->kslot_total * sizeof(double), cudaMemcpyDeviceToHost));
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_test_hold(surfatt_engine_t* e, int solve, int wait_polls) {
+  if (!e || solve < -1 || wait_polls < 0) return SURFATT_BAD_ARG;
+  e->hold_solve = solve;
+  e->item_wait_limit = wait_polls;
+  ++e->gen;  // the kernel arguments change
+  return SURFATT_OK;
+}
+
+surfatt_status_t surfatt_engine_device_results(surfatt_engine_t* e, double** adj_s,
+                                               double** adj_density, double** tt_fwd,
+                                               double** chi, void** stream) {
+  if (!e || !e->ran) return SURFATT_BAD_ARG;
+  if (adj_s) *adj_s = e->last_mode >= 2 ? static_cast<double*>(e->d_adj.p) : nullptr;
+  if (adj_density) *adj_density = e->last_mode == 3 ? static_cast<double*>(e->d_adjd.p) : nullptr;
+  if (tt_fwd) *tt_fwd = e->npath ? static_cast<double*>(e->d_ttfwd.p) : nullptr;
+  if (chi) *chi = static_cast<double*>(e->d_chi.p);
+  if (stream) *stream = static_cast<void*>(e->st);
   return SURFATT_OK;
 }
 

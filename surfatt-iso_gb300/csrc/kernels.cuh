@@ -71,6 +71,12 @@ struct BatchArgs {
   unsigned long long* phase_cycles = nullptr;  // optional: SM cycles per solve phase, summed
   int items = 1;           // FP32 warp kernel: items per solve (1: whole solves)
   int* sstate = nullptr;   // FP32 warp kernel with items > 1: per-solve state records
+  // Test hooks of the bounded item wait (FP32 warp kernel with items; off by
+  // default): item_wait_limit > 0 replaces the wait's poll limit, and the
+  // first item of solve hold_solve (>= 0) is skipped without being marked
+  // done, so the solve's next item waits until the limit runs out.
+  int item_wait_limit = 0;
+  int hold_solve = -1;
 };
 
 // Solve phases timed when BatchArgs::phase_cycles is set (FP32 warp kernel).

@@ -597,6 +597,10 @@ __device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const 
   }
   if (NW == 1) bad = __any_sync(FULL, bad);
   else bad = __syncthreads_or(bad);
+  if (A.Tout) {
+    const size_t N = (size_t)P.nx * P.ny;
+    for (size_t k = T.tid; k < N; k += 32 * NW) A.Tout[A.kslot[s] + k] = w_T(V, k);
+  }
   tsync<NW>();
   if (T.tid == 0) {
     double ssum = 0;
@@ -724,10 +728,12 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     const int item = q / A.nsolve;
     const int s = A.order[q % A.nsolve];
     int* const ss = cut ? A.sstate + (size_t)kSolveStateInts * s : nullptr;
+    if (cut && item == 0 && s == A.hold_solve) continue;  // test hook: never done
     if (cut && item > 0) {
       // the previous item of this solve (taken earlier by a resident warp)
+      const int limit = A.item_wait_limit > 0 ? A.item_wait_limit : kItemWaitLimit;
       int d = ld_acquire(ss + SS_DONE), it = 0;
-      while (d >= 0 && d < item && it < kItemWaitLimit) {
+      while (d >= 0 && d < item && it < limit) {
         __nanosleep(128);
         d = ld_acquire(ss + SS_DONE);
         ++it;
@@ -740,8 +746,31 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
       }
       if (failed) continue;  // the solve failed in an earlier item
       if (late) {            // wait limit: report and drop the solve
+        // the solve contributes nothing (as a solve whose source is on the
+        // boundary): zero receiver times, misfit and kernel slots
+        const PeriodDev& Pz = A.periods[A.pidx[s]];
+        const size_t Nz = (size_t)Pz.nx * Pz.ny;
+        const int rz = A.rec_off[s], nz = A.nrec[s];
+        for (int r = T.tid; r < nz; r += 32 * NW) {
+          A.tekio[rz + r] = 0.0;
+          A.wgt_eff[rz + r] = 0.0;
+          A.tt_fwd[A.path[rz + r]] = 0.0;
+        }
+        if (A.mode >= 2)
+          for (size_t kk = T.tid; kk < Nz; kk += 32 * NW) {
+            kf[A.kslot[s] + kk] = 0.f;
+            if (A.mode == 3) kdf[A.kslot[s] + kk] = 0.f;
+          }
+        if (A.Tout)
+          for (size_t kk = T.tid; kk < Nz; kk += 32 * NW) A.Tout[A.kslot[s] + kk] = 0.0;
+        __threadfence();
+        tsync<NW>();
         if (T.tid == 0) {
+          A.chi[s] = 0.0;
           A.status[s] = ST_TIMEOUT;
+          A.fwd_iters[s] = 0;
+          A.adj_iters[s] = 0;
+          if (A.fwd_updates) A.fwd_updates[s] = 0;
           st_release(ss + SS_DONE, -1);
         }
         tsync<NW>();
@@ -804,6 +833,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
           kf[A.kslot[s] + kk] = 0.f;
           if (A.mode == 3) kdf[A.kslot[s] + kk] = 0.f;
         }
+      if (A.Tout)
+        for (size_t kk = T.tid; kk < N; kk += 32 * NW) A.Tout[A.kslot[s] + kk] = 0.0;
       if (T.tid == 0) {
         A.chi[s] = 0.0;
         A.status[s] = w.status;

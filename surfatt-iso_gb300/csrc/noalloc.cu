@@ -14,7 +14,10 @@
 // process exits.  Host code cannot use the array's name as a device address,
 // so the first call on each device looks the address up with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture.  All calls share the one array,
+// first call before any stream capture.  The cached address belongs to the
+// device's context: after cudaDeviceReset (which destroys that context and
+// the array with it) the entry point must not be called again in the same
+// process.  All calls share the one array,
 // which keeps whatever the last call left there; a call reads only scratch
 // words it has written itself earlier in the same call (nothing needs to
 // start at zero), so results do not depend on the previous call -- but two
@@ -159,8 +162,13 @@ extern "C" surfatt_status_t surfatt_uw_lonlat_solve_noalloc(
     }
     scratch = g_addr[dev];
   }
-  const double x0 = x0_deg / 180.0 * PI_S, y0 = y0_deg / 180.0 * PI_S;
-  k_uw_noalloc<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      xx_deg, yy_deg, nx, ny, spha, sphb, sphc, fun, x0, y0, scratch, T, status_iters);
-  return cudaGetLastError() == cudaSuccess ? SURFATT_OK : SURFATT_CUDA_ERROR;
+  double x0 = x0_deg / 180.0 * PI_S, y0 = y0_deg / 180.0 * PI_S;
+  // cudaLaunchKernel returns this launch's own error: an error that earlier,
+  // unrelated work left pending on the thread is neither reported as this
+  // call's failure nor cleared from under its owner.
+  void* args[] = {&xx_deg, &yy_deg, &nx, &ny, &spha, &sphb, &sphc, &fun,
+                  &x0, &y0, &scratch, &T, &status_iters};
+  const cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(&k_uw_noalloc), dim3(1),
+                                         dim3(256), args, 0, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? SURFATT_OK : SURFATT_CUDA_ERROR;
 }

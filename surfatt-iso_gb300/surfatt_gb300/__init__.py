@@ -51,7 +51,8 @@ EXPORTED = [
     "surfatt_srcrec_station_name", "surfatt_srcrec_paths", "surfatt_srcrec_build_worklist",
     "surfatt_srcrec_worklist", "surfatt_srcrec_build_timing", "surfatt_srcrec_write_csv",
     "surfatt_topo_metric", "surfatt_topo_sigma", "surfatt_topo_metric_timing",
-    "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc",
+    "surfatt_measure_peaks", "surfatt_uw_lonlat_solve_noalloc", "surfatt_engine_device_results",
+    "surfatt_engine_set_keep_fields", "surfatt_engine_fields", "surfatt_engine_test_hold",
     "surfatt_server_create", "surfatt_server_destroy", "surfatt_server_add_model",
     "surfatt_server_add_worklist", "surfatt_server_submit", "surfatt_server_wait",
     "surfatt_server_stats", "surfatt_server_reset_stats",
@@ -682,6 +683,16 @@ def pack_problem(pb, keep):
                      P(pb.path, "i"), pb.npath)
 
 
+class _DeviceArray:
+    """A float64 vector in device memory, exposed to torch through the CUDA
+    array interface (zero copy)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "<f8",
+                                         "data": (int(ptr), False), "version": 2,
+                                         "strides": None}
+
+
 class Engine:
     """Batched gradient evaluations on one GPU (device-resident problem)."""
 
@@ -864,6 +875,60 @@ class Engine:
         if st != OK:
             raise SurfattError(st, "engine_smooth_timing")
         return ms.value, taps.value, n.value
+
+    def set_keep_fields(self, enable):
+        """Keep every solve's travel-time field in later runs (default off)."""
+        L = lib()
+        L.surfatt_engine_set_keep_fields.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        st = L.surfatt_engine_set_keep_fields(self._h, 1 if enable else 0)
+        if st != OK:
+            raise SurfattError(st, "engine_set_keep_fields")
+
+    def fields(self):
+        """The last run's travel-time fields, one (nx, ny) array per solve."""
+        pb = self.pb
+        cells = (pb.nx[pb.pidx].astype(np.int64) * pb.ny[pb.pidx])
+        flat = np.zeros(max(int(cells.sum()), 1))
+        L = lib()
+        L.surfatt_engine_fields.argtypes = [ctypes.c_void_p, _dp]
+        st = L.surfatt_engine_fields(self._h, _d(flat))
+        if st != OK:
+            raise SurfattError(st, "engine_fields")
+        out, o = [], 0
+        for s in range(pb.nsolve):
+            p = int(pb.pidx[s])
+            n = int(cells[s])
+            out.append(flat[o:o + n].reshape((int(pb.nx[p]), int(pb.ny[p])), order="F"))
+            o += n
+        return out
+
+    def test_hold(self, solve=-1, wait_polls=0):
+        """Test hook of the bounded item wait (solve -1: off)."""
+        L = lib()
+        L.surfatt_engine_test_hold.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        st = L.surfatt_engine_test_hold(self._h, int(solve), int(wait_polls))
+        if st != OK:
+            raise SurfattError(st, "engine_test_hold")
+
+    def device_results(self):
+        """The last run's adj_s, adj_density, tt_fwd and chi as torch tensors
+        that view the engine's device memory (no copy; valid until the next
+        load; None where the mode produces no such field).  Call after
+        sync().  For the multi-rank sum of the results on the device."""
+        import torch
+        L = lib()
+        L.surfatt_engine_device_results.argtypes = [ctypes.c_void_p] + [
+            ctypes.POINTER(ctypes.c_void_p)] * 5
+        ptr = [ctypes.c_void_p() for _ in range(5)]
+        st = L.surfatt_engine_device_results(self._h, *[ctypes.byref(p) for p in ptr])
+        if st != OK:
+            raise SurfattError(st, "engine_device_results")
+        pb = self.pb
+        out = {}
+        for name, p, n in (("adj_s", ptr[0], pb.ncell), ("adj_density", ptr[1], pb.ncell),
+                           ("tt_fwd", ptr[2], pb.npath), ("chi", ptr[3], 1)):
+            out[name] = None if not p.value else torch.as_tensor(_DeviceArray(p.value, n))
+        return out
 
     def work(self):
         f, a = ctypes.c_double(0), ctypes.c_double(0)

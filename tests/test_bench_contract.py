@@ -28,8 +28,13 @@ def test_reference_arm_line(oracle):
         assert k in d, k
     assert d["impl"] == "reference"
     assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 1
-    assert d["higher_is_better"] is True and d["scaling"] == "weak"
-    assert "workload" in d["config"]
+    # one gradient evaluation split over the ranks: total work fixed
+    assert d["higher_is_better"] is True and d["scaling"] == "strong"
+    # the same config object as the GPU arm's line (bench._config)
+    for k in ("workload", "solves_per_step", "grid", "periods", "receivers", "mode", "l2",
+              "parallelism"):
+        assert k in d["config"], k
+    assert "-O3" in d["cpu_baseline"]["build"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
     assert cb["sample"]

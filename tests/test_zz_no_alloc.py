@@ -4,10 +4,13 @@ It exists for callers that must not allocate device memory when they call the
 solver -- e.g. a host framework whose memory pool owns the GPU's memory, or a
 loop that cannot afford the device-wide synchronisation of cudaMalloc and
 cudaFree.  It takes device arrays and uses a fixed scratch array compiled into
-the library.  This test calls it through the C ABI twice in a row (different
-sources, so stale scratch from the first call would show) and compares each
-result with the ordinary drop-in entry point, fsm_uw_ps_lonlat_2d_.  The file
-is collected last so that a run stopping at the first failure has already run
+the library.  This test calls it through the C ABI twice in a row, the second
+time on a smaller grid with another source (so the scratch regions sit at
+other offsets and hold other sizes: leftovers of the first call would show),
+and compares each result bit for bit with the ordinary drop-in entry point,
+fsm_uw_ps_lonlat_2d_ (the same FP64 solver code on the same inputs), and with
+the oracle within the plain path's travel-time tolerance.  The file is
+collected last so that a run stopping at the first failure has already run
 every other test.
 """
 import numpy as np
@@ -21,24 +24,29 @@ pytestmark = pytest.mark.gpu
 TT_TOL = 1e-6
 
 
-def test_noalloc_matches_dropin_two_calls(sg):
-    torch = pytest.importorskip("torch")
-    assert torch.cuda.is_available()
-    nx, ny = 120, 110
+def _case(nx, ny, m12):
     xx, yy = W.arange_grid(100.0, nx, 0.05), W.arange_grid(22.0, ny, 0.05)
     m11 = np.ones((nx, ny))
     m22 = np.ones((nx, ny))
-    m12 = np.full((nx, ny), 0.02)
+    m12 = np.full((nx, ny), m12)
     fun = 1.0 / (3.0 * W.checkerboard_2d(nx, ny, 2, 3, 0.06))
+    return xx, yy, m11, m22, m12, fun
+
+
+def test_noalloc_matches_dropin_two_calls(sg, oracle):
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
     dev = torch.device("cuda:0")
-    col = lambda a: torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).to(dev)
-    d_xx, d_yy = torch.from_numpy(xx).to(dev), torch.from_numpy(yy).to(dev)
-    d_a, d_b, d_c, d_f = col(m11), col(m22), col(-m12), col(fun)
-    d_T = torch.zeros(nx * ny, dtype=torch.float64, device=dev)
-    d_si = torch.zeros(2, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
-    for src in ((101.03, 23.01), (104.77, 26.02)):
-        d_T.fill_(-1.0)
+    col = lambda a: torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).to(dev)
+    # first call: 120 x 110 (13200 cells); second: 70 x 53 with another source
+    for (nx, ny, m12, src) in ((120, 110, 0.02, (101.03, 23.01)),
+                               (70, 53, -0.03, (102.61, 23.77))):
+        xx, yy, m11, m22, m12a, fun = _case(nx, ny, m12)
+        d_xx, d_yy = torch.from_numpy(xx).to(dev), torch.from_numpy(yy).to(dev)
+        d_a, d_b, d_c, d_f = col(m11), col(m22), col(-m12a), col(fun)
+        d_T = torch.full((nx * ny,), -1.0, dtype=torch.float64, device=dev)
+        d_si = torch.full((2,), -7, dtype=torch.int32, device=dev)
         st = sg.uw_lonlat_solve_noalloc(d_xx.data_ptr(), d_yy.data_ptr(), nx, ny, d_a.data_ptr(),
                                         d_b.data_ptr(), d_c.data_ptr(), d_f.data_ptr(), *src,
                                         d_T.data_ptr(), d_si.data_ptr(), stream)
@@ -46,9 +54,12 @@ def test_noalloc_matches_dropin_two_calls(sg):
         torch.cuda.synchronize(dev)
         T = d_T.cpu().numpy().reshape((nx, ny), order="F")
         status, iters = (int(v) for v in d_si.cpu().numpy())
-        Tr, sr, ir = sg.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12, fun, *src)
-        assert status == sr == sg.OK
-        assert iters == ir
+        Td, sd, idr = sg.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12a, fun, *src)
+        assert status == sd == sg.OK
+        assert iters == idr
+        assert np.array_equal(T, Td)
+        Tr, sr, ir = oracle.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12a, fun, *src)
+        assert sr == 0 and iters == ir
         assert rel_pointwise(T, Tr) <= TT_TOL
 
 
