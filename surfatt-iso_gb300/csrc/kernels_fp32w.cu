@@ -92,9 +92,11 @@ __device__ __forceinline__ void tsum_max2(double& a, double& b, double& c) {
 
 
 // Workspace per warp slot: S (float4: T0, T0x, T0y, -), W (float4 adjoint
-// weights), tau, old, 1/d, two scaled adjoint sources.
+// weights), tau, old, 1/d, two scaled adjoint sources, and a second
+// (Ta, old) pair for the density field when the adjoint kernel sweeps both
+// fields of a solve at once.
 long long batch_fp32w_ws_doubles(long long N) {
-  const long long floats = 8 * N + 5 * N + 2 * 4096;
+  const long long floats = 8 * N + 7 * N + 2 * 4096;
   long long d = (floats + 1) / 2 + 64;
   return (d + 31) / 32 * 32;  // keep every slot 256-byte aligned
 }
@@ -107,6 +109,8 @@ struct WSlot {
   float* id;
   float* src[2];
   float* col;  // per column sin and cos of half the longitude offset (2 * nx)
+  float* tau1;  // density field's Ta and iteration-start values (adjoint kernel)
+  float* old1;
 };
 
 __device__ inline WSlot wcarve(double* base, size_t N) {
@@ -119,6 +123,8 @@ __device__ inline WSlot wcarve(double* base, size_t N) {
   V.src[0] = V.id + N;
   V.src[1] = V.src[0] + N;
   V.col = V.src[1] + N;
+  V.tau1 = V.col + 2 * 4096;
+  V.old1 = V.tau1 + N;
   return V;
 }
 
@@ -420,7 +426,15 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
 // Sweeps one adjoint field (held in V.tau) to convergence: the reference's
 // absolute rule (:1429) or no change beyond the FP32 resolution of the field.
 // Neighbours outside the interior are the boundary's zeros.
-template <int MB, int PF, int NW>
+//
+// D is the depth of the operand ring: at step t the operands of step
+// t + D - 1 are loaded.  A visit is four FMAs, so a step is far shorter than
+// the latency of its operands (the weights are read once per sweep and do
+// not stay in L1); the step loop is unrolled by D so that every ring slot is
+// a fixed set of registers and no operand is ever copied.  The fused solve
+// kernel affords D = 2 (its forward sweeps hold the register file); the
+// adjoint kernel, with registers of its own, D = 4.
+template <int MB, int NW, int D>
 __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src,
                                     const Tm<NW>& T, int* status_out, int* iters_out) {
   const int nx = P.nx, ny = P.ny, lane = T.lane;
@@ -452,82 +466,68 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
         if (u < 0 || u >= nu || vtop + 1 >= nv) return 0.f;
         return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
       };
-      // Teams with register prefetch load the operands of step t+2 at step t
-      // (a visit is four FMAs, and a team step also waits at the barrier: one
-      // step does not cover the loads' latency).  A cell is written only at
-      // its own visit and the weights, sources and iteration-start values are
-      // fixed within a sweep, so the early loads see the values a load at the
-      // visit would.  (A single warp keeps one step: the extra registers
-      // spill in its loop.)
-      constexpr bool AHEAD2 = PF == 1 && NW > 1;
+      // A cell is written only at its own visit and the weights, sources and
+      // iteration-start values are fixed within a sweep, so operands loaded
+      // D - 1 steps early are the values a load at the visit would see.
       float res[MB];
-      WAdj cur[MB], ahead[MB];
+      WAdj ring[D][MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
-        wa_load<PF == 1>(cur[m], 0, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
-        if (AHEAD2)
-          wa_load<true>(ahead[m], 1, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          wa_load<true>(ring[d][m], d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
       }
       float pn = top ? north_of_top(0) : 0.f;
-      for (int t = 0; t < nsteps; ++t) {
-        WAdj nxt[MB];
+      for (int t0 = 0; t0 < nsteps; t0 += D) {
 #pragma unroll
-        for (int m = 0; m < MB; ++m) {
-          if (AHEAD2) {
-            nxt[m] = ahead[m];
-            wa_load<true>(ahead[m], t + 2, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
+        for (int d = 0; d < D; ++d) {
+          const int t = t0 + d;
+          if (t >= nsteps) break;  // the same for every thread of the team
+          WAdj(&cur)[MB] = ring[d];
+          const WAdj(&nxt)[MB] = ring[(d + 1) % D];
+          const float qn = top ? north_of_top(t + 1) : 0.f;
+          float south[MB], north[MB], nown[MB];
+#pragma unroll
+          for (int m = 0; m < MB; ++m) nown[m] = nxt[m].own;
+          w_from_below<MB>(res, south, lane);
+          w_from_above<MB>(nown, north, lane);
+          if (NW > 1) {
+            if (bot) south[0] = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
+            if (top) north[MB - 1] = pn;
+          }
+#pragma unroll
+          for (int m = 0; m < MB; ++m) {
+            if (cur[m].on) {
+              const int v = vb + lane + 32 * m, u = t - v;
+              const int k = (xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 1 + v : nv - v);
+              const float west = u > 0 ? res[m] : 0.f;
+              const float east = u < nu - 1 ? nown[m] : 0.f;
+              const float sth = v > 0 ? south[m] : 0.f;
+              const float nth = v < nv - 1 ? north[m] : 0.f;
+              const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
+              const float ts = ydir > 0 ? sth : nth, tn = ydir > 0 ? nth : sth;
+              const float val = adj_update(cur[m].src, cur[m].w, tw, te, ts, tn);
+              V.tau[k] = val;
+              if (s == 0) V.old[k] = cur[m].own;
+              if (last) {
+                const float dd = fabsf(val - cur[m].old);
+                l1 += dd;
+                lmax = fmaxf(lmax, dd);
+                vmax = fmaxf(vmax, fabsf(val));
+              }
+              res[m] = val;
+            }
+          }
+          // this slot now takes the operands of step t + D
+#pragma unroll
+          for (int m = 0; m < MB; ++m)
+            wa_load<true>(ring[d][m], t + D, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
                           last);
-          } else {
-            wa_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
-                             last);
-          }
+          if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
+          pn = qn;
+          tsync<NW>();
         }
-        const float qn = top ? north_of_top(t + 1) : 0.f;
-        float south[MB], north[MB], nown[MB];
-#pragma unroll
-        for (int m = 0; m < MB; ++m) nown[m] = nxt[m].own;
-        w_from_below<MB>(res, south, lane);
-        w_from_above<MB>(nown, north, lane);
-        if (NW > 1) {
-          if (bot) south[0] = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
-          if (top) north[MB - 1] = pn;
-        }
-#pragma unroll
-        for (int m = 0; m < MB; ++m) {
-          if (cur[m].on) {
-            const int v = vb + lane + 32 * m, u = t - v;
-            const int k = (xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 1 + v : nv - v);
-            const float west = u > 0 ? res[m] : 0.f;
-            const float east = u < nu - 1 ? nown[m] : 0.f;
-            const float sth = v > 0 ? south[m] : 0.f;
-            const float nth = v < nv - 1 ? north[m] : 0.f;
-            const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
-            const float ts = ydir > 0 ? sth : nth, tn = ydir > 0 ? nth : sth;
-            if (PF == 0) {
-              cur[m].w = V.W[k];
-              cur[m].src = src[k];
-              if (last) cur[m].old = V.old[k];
-            }
-            const float val = adj_update(cur[m].src, cur[m].w, tw, te, ts, tn);
-            V.tau[k] = val;
-            if (s == 0) V.old[k] = cur[m].own;
-            if (last) {
-              const float dd = fabsf(val - cur[m].old);
-              l1 += dd;
-              lmax = fmaxf(lmax, dd);
-              vmax = fmaxf(vmax, fabsf(val));
-            }
-            res[m] = val;
-          }
-        }
-        // the next step's operands after every band's visit (as in the
-        // forward sweeps)
-#pragma unroll
-        for (int m = 0; m < MB; ++m) cur[m] = nxt[m];
-        if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
-        pn = qn;
-        tsync<NW>();
       }
     }
     double sl1 = (double)l1, smax = (double)lmax, svmax = (double)vmax;
@@ -707,9 +707,12 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Items per solve for `mode` when solves are cut.
-__host__ __device__ inline int w_items_for_mode(int mode) {
-  return kFwdItems + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
+// Items per solve for `mode` when solves are cut.  With the adjoint fields
+// in their own kernel (BatchArgs::split_adj) a solve has only its forward
+// items, the last of which also computes receivers, misfit and the adjoint
+// coefficients and sources.
+__host__ __device__ inline int w_items_for_mode(int mode, int split_adj = 0) {
+  return kFwdItems + (split_adj ? 0 : (mode == 3 ? 2 : (mode == 2 ? 1 : 0)));
 }
 
 template <int MB, int PF, int MINW, int NW>
@@ -731,7 +734,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     if (cut && item == 0 && s == A.hold_solve) continue;  // test hook: never done
     if (cut && item > 0) {
       // the previous item of this solve (taken earlier by a resident warp)
-      const int limit = A.item_wait_limit > 0 ? A.item_wait_limit : kItemWaitLimit;
+      const int limit =
+          (s == A.hold_solve && A.item_wait_limit > 0) ? A.item_wait_limit : kItemWaitLimit;
       int d = ld_acquire(ss + SS_DONE), it = 0;
       while (d >= 0 && d < item && it < limit) {
         __nanosleep(128);
@@ -805,7 +809,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
     const int nf = A.mode == 3 ? 2 : 1;
-    const int nitems_mode = w_items_for_mode(A.mode);
+    const int nitems_mode = w_items_for_mode(A.mode, cut ? A.split_adj : 0);
     const int first = cut ? item : 0;                 // first item done here
     const int lastit = cut ? item : nitems_mode - 1;  // last item done here
     int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0;
@@ -879,7 +883,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
         st = w_adj_sources<NW>(A, P, V, r0, nr, nf, T, st);
         mark(PH_ADJ_SETUP);
       }
-      if (cut && A.mode >= 2) {
+      if (cut && A.mode >= 2 && !A.split_adj) {
         if (T.tid == 0) {
           ss[SS_FIT] = fit;
           ss[SS_ST] = st;
@@ -893,7 +897,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     const int f1 = A.mode >= 2 ? (cut ? lastit - kFwdItems : nf - 1) : -1;
     for (int f = f0; f <= f1; ++f) {
       int ast = ST_OK, n = 0;
-      w_adj_sweeps<MB, PF, NW>(P, V, f ? V.src[1] : V.src[0], T, &ast, &n);
+      w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2>(P, V, f ? V.src[1] : V.src[0], T, &ast,
+                                                        &n);
       mark(PH_ADJ);
       if (f == 0) its0 = n; else its1 = n;
       if (ast != ST_OK && st == ST_OK) st = ast;
@@ -920,19 +925,129 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
   }
 }
 
+// The adjoint fields of a batch whose forward items the solve kernel has
+// run with split_adj set (same work items, same order): unit q is field
+// q / nsolve of solve order[q % nsolve], so every solve's residual field is
+// handed out before any density field.  Each unit sweeps its field with the
+// solve's weights and sources (left in the solve's workspace slot by the
+// solve kernel; the density field in its own Ta / old arrays), applies the
+// mask and writes its kernel slot, exactly as the fused kernel would.  A
+// solve whose forward part failed (state -1: its outputs are already zero)
+// is skipped.  Iterations, visit counts and a non-converged status are
+// merged into the solve's outputs atomically (max, sum, first failure).
+template <int MB, int NW, int D, int MINW>
+__global__ void __launch_bounds__(32 * NW, MINW / NW) k_adj_fp32w(BatchArgs A) {
+  const Tm<NW> T = this_team<NW>();
+  const int lane = T.lane;
+  const int nf = A.mode == 3 ? 2 : 1;
+  for (;;) {
+    int q = 0;
+    if (T.tid == 0) q = atomicAdd(A.queue_adj, 1);
+    q = tbcast<NW>(q);
+    if (q >= A.nsolve * nf) break;
+    const int f = q / A.nsolve;
+    const int s = A.order[q % A.nsolve];
+    if (A.sstate[(size_t)kSolveStateInts * s + SS_DONE] < 0) continue;
+    const PeriodDev P = A.periods[A.pidx[s]];
+    const int nx = P.nx, ny = P.ny;
+    WSlot V = wcarve(A.ws + (long long)s * A.ws_doubles, (size_t)nx * ny);
+    if (f == 1) {
+      V.tau = V.tau1;
+      V.old = V.old1;
+    }
+    unsigned long long* const pc = A.phase_cycles;
+    long long c0 = pc ? clock64() : 0;
+    auto mark = [&](int ph) {
+      if (pc) {
+        const long long c1 = clock64();
+        if (T.tid == 0) atomicAdd(pc + ph, (unsigned long long)(c1 - c0));
+        c0 = c1;
+      }
+    };
+    int ast = ST_OK, n = 0;
+    w_adj_sweeps<MB, NW, D>(P, V, V.src[f], T, &ast, &n);
+    mark(PH_ADJ);
+    const double xd0 = A.srcx[s], yd0 = A.srcy[s];
+    const WSolve w = w_locate(P, xd0 / 180.0 * PI_S, yd0 / 180.0 * PI_S, xd0, yd0, lane);
+    w_slot<NW>(A, P, V, w, s, f, T);
+    mark(PH_SLOT);
+    if (T.tid == 0) {
+      atomicMax(A.adj_iters + s, n);
+      if (A.adj_updates) atomicAdd(A.adj_updates + s, (double)n * 4.0 * (nx - 2) * (ny - 2));
+      if (ast != ST_OK) atomicCAS(A.status + s, ST_OK, ast);
+    }
+    tsync<NW>();
+  }
+}
+
+// Ring depth and resident warps per SM of the adjoint kernel: operands three
+// steps ahead (four slots) in up to 255 registers, 8 warps per SM (at 12
+// warps per SM, 168 registers, the four-slot ring spills).
+constexpr int kAdjRing = 4;
+constexpr int kAdjWarps = 8;
+
+template <int MB, int NW>
+static void launch_adj(const BatchArgs& a, int grid, cudaStream_t st) {
+  k_adj_fp32w<MB, NW, (NW == 1 ? kAdjRing : 3), kAdjWarps><<<grid, 32 * NW, 0, st>>>(a);
+}
+
+template <int MB, int NW>
+static int occupancy_adj() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &n, k_adj_fp32w<MB, NW, (NW == 1 ? kAdjRing : 3), kAdjWarps>, 32 * NW, 0);
+  return n;
+}
+
+int fp32w_team(int max_ny);
+
+void launch_adj_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st) {
+  switch (bands) {
+    case 1: launch_adj<1, 1>(a, grid, st); break;
+    case 2: launch_adj<2, 1>(a, grid, st); break;
+    case 3: launch_adj<3, 1>(a, grid, st); break;
+    case 4: launch_adj<4, 1>(a, grid, st); break;
+    default:
+      switch (fp32w_team(32 * bands)) {
+        case 2: launch_adj<4, 2>(a, grid, st); break;
+        case 3: launch_adj<4, 3>(a, grid, st); break;
+        default: launch_adj<4, 4>(a, grid, st); break;
+      }
+  }
+}
+
+int adj_fp32w_max_blocks_per_sm(int bands) {
+  switch (bands) {
+    case 1: return occupancy_adj<1, 1>();
+    case 2: return occupancy_adj<2, 1>();
+    case 3: return occupancy_adj<3, 1>();
+    case 4: return occupancy_adj<4, 1>();
+    default:
+      switch (fp32w_team(32 * bands)) {
+        case 2: return occupancy_adj<4, 2>();
+        case 3: return occupancy_adj<4, 3>();
+        default: return occupancy_adj<4, 4>();
+      }
+  }
+}
+
 int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 
 // Variants of the warp kernel: operand loads, resident warps per SM, whole
-// solves or solves cut into items.
-//   0: every operand loaded a step ahead into registers, 8 warps per SM, items
-//   1: the same, whole solves
-//   2: cell constants loaded at the visit, 12 warps per SM, items
+// solves or solves cut into items, adjoint fields in the solve kernel or in
+// the adjoint kernel.
+//   0: every operand loaded a step ahead into registers, 8 warps per SM,
+//      items, adjoint fields in k_adj_fp32w (operands three steps ahead)
+//   1: register prefetch, 8 warps per SM, whole solves (fused)
+//   2: cell constants loaded at the visit, 12 warps per SM, items (fused)
 //   3: cell constants loaded at the visit, 8 warps per SM, whole solves
-constexpr int kFp32wVariants = 4;
+//   4: register prefetch, 8 warps per SM, items, adjoint fields in the solve
+//      kernel (one step ahead)
+constexpr int kFp32wVariants = 5;
 int fp32w_variant_count() { return kFp32wVariants; }
-bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2; }
-int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
-
+bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2 || variant == 4; }
+bool fp32w_variant_split(int variant) { return variant == 0; }
+int fp32w_items_for_mode(int mode, int split_adj) { return w_items_for_mode(mode, split_adj); }
 template <int MB, int PF, int MINW, int NW>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
   k_batch_fp32w<MB, PF, MINW, NW><<<grid, 32 * NW, 0, st>>>(a);
@@ -948,20 +1063,18 @@ static int occupancy_w() {
 template <int MB, int NW>
 static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st) {
   switch (variant) {
-    case 0:
-    case 1: launch_w<MB, 1, 8, NW>(a, grid, st); break;
     case 2: launch_w<MB, 0, 12, NW>(a, grid, st); break;
-    default: launch_w<MB, 0, 8, NW>(a, grid, st); break;
+    case 3: launch_w<MB, 0, 8, NW>(a, grid, st); break;
+    default: launch_w<MB, 1, 8, NW>(a, grid, st); break;
   }
 }
 
 template <int MB, int NW>
 static int occupancy_mb(int variant) {
   switch (variant) {
-    case 0:
-    case 1: return occupancy_w<MB, 1, 8, NW>();
     case 2: return occupancy_w<MB, 0, 12, NW>();
-    default: return occupancy_w<MB, 0, 8, NW>();
+    case 3: return occupancy_w<MB, 0, 8, NW>();
+    default: return occupancy_w<MB, 1, 8, NW>();
   }
 }
 

@@ -104,3 +104,66 @@ def test_projection_locate_failure_stops_like_the_reference(sg):
     assert "not reached" not in r.stdout
     vals = [float(v) for v in r.stdout.split("domain.")[1].split()]
     assert vals == [1.0, 1.0, 1.0]
+
+
+# C layout of the ISO_C_BINDING kinds the Fortran module uses (LP64)
+_F_KINDS = {"integer(c_int)": (4, 4), "type(c_ptr)": (8, 8), "real(c_double)": (8, 8),
+            "integer(c_size_t)": (8, 8), "integer(c_long_long)": (8, 8)}
+
+
+def _fortran_types():
+    """{type name: [(kind, field), ...]} of the bind(c) derived types of
+    include/surfatt_gpu.f90, in declaration order."""
+    src = open(os.path.join(ROOT, "include", "surfatt_gpu.f90")).read()
+    out = {}
+    for m in re.finditer(r"type\s*,\s*bind\(c\)\s*::\s*(\w+)(.*?)end\s+type", src, flags=re.S | re.I):
+        fields = []
+        for line in m.group(2).splitlines():
+            line = line.split("!")[0].strip()
+            if not line:
+                continue
+            kind, _, names = line.partition("::")
+            for name in names.split(","):
+                fields.append((kind.strip().lower().replace(" ", ""), name.strip()))
+        out[m.group(1)] = fields
+    return out
+
+
+def test_fortran_binding_matches_c_structs(tmp_path):
+    """The module's derived types have the C structs' fields in the same
+    order with the same sizes and offsets (what bind(c) relies on): a C
+    probe prints offsetof / sizeof of every field the module names, which
+    must equal the offsets the module's kinds give under C layout rules."""
+    import subprocess
+    types = _fortran_types()
+    assert set(types) == {"surfatt_problem_t", "surfatt_result_t"}
+    probe = ['#include <stdio.h>', '#include <stddef.h>', '#include "surfatt_gb300.h"',
+             "int main(void) {"]
+    expect = []
+    for t, fields in types.items():
+        off = 0
+        for kind, name in fields:
+            size, align = _F_KINDS[kind]
+            off = (off + align - 1) // align * align
+            expect.append(f"{t}.{name} {off} {size}")
+            probe.append(f'  printf("{t}.{name} %zu %zu\\n", offsetof({t}, {name}), '
+                         f'sizeof((({t}*)0)->{name}));')
+            off += size
+        total = (off + 7) // 8 * 8
+        expect.append(f"{t} {total}")
+        probe.append(f'  printf("{t} %zu\\n", sizeof({t}));')
+    probe.append("  return 0;\n}\n")
+    c = tmp_path / "probe.c"
+    c.write_text("\n".join(probe))
+    exe = tmp_path / "probe"
+    subprocess.check_call(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(c), "-o",
+                           str(exe)])
+    got = subprocess.check_output([str(exe)], text=True).split("\n")
+    assert [g for g in got if g] == expect
+
+
+def test_fortran_binding_names_exported_symbols():
+    """Every bind(c, name=...) of the module is a function the header declares."""
+    src = open(os.path.join(ROOT, "include", "surfatt_gpu.f90")).read()
+    names = set(re.findall(r'bind\(c,\s*name="(\w+)"\)', src))
+    assert names and names <= _declared()
