@@ -753,7 +753,7 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
        up(e, e->d_adjd, (double*)nullptr, NC) | up(e, e->d_status, (int*)nullptr, ns) |
        up(e, e->d_fit, (int*)nullptr, ns) | up(e, e->d_ait, (int*)nullptr, ns) |
        up(e, e->d_fupd, (double*)nullptr, ns) | up(e, e->d_aupd, (double*)nullptr, ns) |
-       up(e, e->d_queue, (int*)nullptr, 2 * kTeamClasses);
+       up(e, e->d_queue, (int*)nullptr, kTeamClasses);
   if (r & SURFATT_CUDA_ERROR) return SURFATT_CUDA_ERROR;
   if (r) return SURFATT_OOM;
   // per-period descriptors

@@ -78,11 +78,6 @@ struct BatchArgs {
   // solve keeps the production limit).
   int item_wait_limit = 0;
   int hold_solve = -1;
-  // FP32 warp kernel with items: 1 = the solve kernel stops after the
-  // adjoint coefficients and sources, and k_adj_fp32w sweeps the adjoint
-  // fields (queue_adj: its work counter, zeroed before launch)
-  int split_adj = 0;
-  int* queue_adj = nullptr;
 };
 
 // Solve phases timed when BatchArgs::phase_cycles is set (FP32 warp kernel).
@@ -150,13 +145,7 @@ int fp32w_variant_count();
 // Whether a variant cuts solves into work items (one workspace slot per
 // solve), and the items per solve of an evaluation mode.
 bool fp32w_variant_items(int variant);
-// variants whose adjoint fields run in k_adj_fp32w (after the solve kernel)
-bool fp32w_variant_split(int variant);
-int fp32w_items_for_mode(int mode, int split_adj = 0);
-// The adjoint kernel of a split evaluation (same bands / team as the solve
-// kernel's launch) and its resident blocks per SM.
-void launch_adj_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st);
-int adj_fp32w_max_blocks_per_sm(int bands);
+int fp32w_items_for_mode(int mode);
 constexpr int kSolveStateInts = 5;
 // The same solve on the diagonal layouts (PeriodDev::qa / qd prepared), its
 // operands staged in shared memory; `variant` < fp32d_variant_count().

@@ -92,11 +92,9 @@ __device__ __forceinline__ void tsum_max2(double& a, double& b, double& c) {
 
 
 // Workspace per warp slot: S (float4: T0, T0x, T0y, -), W (float4 adjoint
-// weights), tau, old, 1/d, two scaled adjoint sources, and a second
-// (Ta, old) pair for the density field when the adjoint kernel sweeps both
-// fields of a solve at once.
+// weights), tau, old, 1/d, two scaled adjoint sources.
 long long batch_fp32w_ws_doubles(long long N) {
-  const long long floats = 8 * N + 7 * N + 2 * 4096;
+  const long long floats = 8 * N + 5 * N + 2 * 4096;
   long long d = (floats + 1) / 2 + 64;
   return (d + 31) / 32 * 32;  // keep every slot 256-byte aligned
 }
@@ -109,8 +107,6 @@ struct WSlot {
   float* id;
   float* src[2];
   float* col;  // per column sin and cos of half the longitude offset (2 * nx)
-  float* tau1;  // density field's Ta and iteration-start values (adjoint kernel)
-  float* old1;
 };
 
 __device__ inline WSlot wcarve(double* base, size_t N) {
@@ -123,8 +119,6 @@ __device__ inline WSlot wcarve(double* base, size_t N) {
   V.src[0] = V.id + N;
   V.src[1] = V.src[0] + N;
   V.col = V.src[1] + N;
-  V.tau1 = V.col + 2 * 4096;
-  V.old1 = V.tau1 + N;
   return V;
 }
 
@@ -431,9 +425,9 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
 // t + D - 1 are loaded.  A visit is four FMAs, so a step is far shorter than
 // the latency of its operands (the weights are read once per sweep and do
 // not stay in L1); the step loop is unrolled by D so that every ring slot is
-// a fixed set of registers and no operand is ever copied.  The fused solve
-// kernel affords D = 2 (its forward sweeps hold the register file); the
-// adjoint kernel, with registers of its own, D = 4.
+// a fixed set of registers and no operand is ever copied.  The solve kernel
+// affords D = 2 for a single warp (its forward sweeps hold the register
+// file: deeper rings spill) and D = 3 for teams.
 template <int MB, int NW, int D>
 __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src,
                                     const Tm<NW>& T, int* status_out, int* iters_out) {
@@ -628,11 +622,15 @@ __device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, cons
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
   w_adj_setup<NW>(P, V, T);
-  for (int f = 0; f < nf; ++f)
-    for (size_t k = T.tid; k < N; k += 32 * NW) V.src[f][k] = 0.f;
+  // (the fields' arrays picked by selects: an indexed V.src[f] would put
+  // the whole slot descriptor in local memory)
+  for (int f = 0; f < nf; ++f) {
+    float* const sf = f ? V.src[1] : V.src[0];
+    for (size_t k = T.tid; k < N; k += 32 * NW) sf[k] = 0.f;
+  }
   tsync<NW>();
   if (T.wid == 0)
-    st = adj_sources_warp(A, P, r0, nr, nf, V.src[0], V.src[nf - 1], V.id,
+    st = adj_sources_warp(A, P, r0, nr, nf, V.src[0], nf == 2 ? V.src[1] : V.src[0], V.id,
                           [nx](int i, int j) { return i + nx * j; }, T.lane, st);
   st = tbcast<NW>(st);
   tsync<NW>();
@@ -707,12 +705,9 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Items per solve for `mode` when solves are cut.  With the adjoint fields
-// in their own kernel (BatchArgs::split_adj) a solve has only its forward
-// items, the last of which also computes receivers, misfit and the adjoint
-// coefficients and sources.
-__host__ __device__ inline int w_items_for_mode(int mode, int split_adj = 0) {
-  return kFwdItems + (split_adj ? 0 : (mode == 3 ? 2 : (mode == 2 ? 1 : 0)));
+// Items per solve for `mode` when solves are cut.
+__host__ __device__ inline int w_items_for_mode(int mode) {
+  return kFwdItems + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
 }
 
 template <int MB, int PF, int MINW, int NW>
@@ -809,7 +804,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
     const int nf = A.mode == 3 ? 2 : 1;
-    const int nitems_mode = w_items_for_mode(A.mode, cut ? A.split_adj : 0);
+    const int nitems_mode = w_items_for_mode(A.mode);
     const int first = cut ? item : 0;                 // first item done here
     const int lastit = cut ? item : nitems_mode - 1;  // last item done here
     int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0;
@@ -883,7 +878,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
         st = w_adj_sources<NW>(A, P, V, r0, nr, nf, T, st);
         mark(PH_ADJ_SETUP);
       }
-      if (cut && A.mode >= 2 && !A.split_adj) {
+      if (cut && A.mode >= 2) {
         if (T.tid == 0) {
           ss[SS_FIT] = fit;
           ss[SS_ST] = st;
@@ -925,129 +920,19 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
   }
 }
 
-// The adjoint fields of a batch whose forward items the solve kernel has
-// run with split_adj set (same work items, same order): unit q is field
-// q / nsolve of solve order[q % nsolve], so every solve's residual field is
-// handed out before any density field.  Each unit sweeps its field with the
-// solve's weights and sources (left in the solve's workspace slot by the
-// solve kernel; the density field in its own Ta / old arrays), applies the
-// mask and writes its kernel slot, exactly as the fused kernel would.  A
-// solve whose forward part failed (state -1: its outputs are already zero)
-// is skipped.  Iterations, visit counts and a non-converged status are
-// merged into the solve's outputs atomically (max, sum, first failure).
-template <int MB, int NW, int D, int MINW>
-__global__ void __launch_bounds__(32 * NW, MINW / NW) k_adj_fp32w(BatchArgs A) {
-  const Tm<NW> T = this_team<NW>();
-  const int lane = T.lane;
-  const int nf = A.mode == 3 ? 2 : 1;
-  for (;;) {
-    int q = 0;
-    if (T.tid == 0) q = atomicAdd(A.queue_adj, 1);
-    q = tbcast<NW>(q);
-    if (q >= A.nsolve * nf) break;
-    const int f = q / A.nsolve;
-    const int s = A.order[q % A.nsolve];
-    if (A.sstate[(size_t)kSolveStateInts * s + SS_DONE] < 0) continue;
-    const PeriodDev P = A.periods[A.pidx[s]];
-    const int nx = P.nx, ny = P.ny;
-    WSlot V = wcarve(A.ws + (long long)s * A.ws_doubles, (size_t)nx * ny);
-    if (f == 1) {
-      V.tau = V.tau1;
-      V.old = V.old1;
-    }
-    unsigned long long* const pc = A.phase_cycles;
-    long long c0 = pc ? clock64() : 0;
-    auto mark = [&](int ph) {
-      if (pc) {
-        const long long c1 = clock64();
-        if (T.tid == 0) atomicAdd(pc + ph, (unsigned long long)(c1 - c0));
-        c0 = c1;
-      }
-    };
-    int ast = ST_OK, n = 0;
-    w_adj_sweeps<MB, NW, D>(P, V, V.src[f], T, &ast, &n);
-    mark(PH_ADJ);
-    const double xd0 = A.srcx[s], yd0 = A.srcy[s];
-    const WSolve w = w_locate(P, xd0 / 180.0 * PI_S, yd0 / 180.0 * PI_S, xd0, yd0, lane);
-    w_slot<NW>(A, P, V, w, s, f, T);
-    mark(PH_SLOT);
-    if (T.tid == 0) {
-      atomicMax(A.adj_iters + s, n);
-      if (A.adj_updates) atomicAdd(A.adj_updates + s, (double)n * 4.0 * (nx - 2) * (ny - 2));
-      if (ast != ST_OK) atomicCAS(A.status + s, ST_OK, ast);
-    }
-    tsync<NW>();
-  }
-}
-
-// Ring depth and resident warps per SM of the adjoint kernel: operands three
-// steps ahead (four slots) in up to 255 registers, 8 warps per SM (at 12
-// warps per SM, 168 registers, the four-slot ring spills).
-constexpr int kAdjRing = 4;
-constexpr int kAdjWarps = 8;
-
-template <int MB, int NW>
-static void launch_adj(const BatchArgs& a, int grid, cudaStream_t st) {
-  k_adj_fp32w<MB, NW, (NW == 1 ? kAdjRing : 3), kAdjWarps><<<grid, 32 * NW, 0, st>>>(a);
-}
-
-template <int MB, int NW>
-static int occupancy_adj() {
-  int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &n, k_adj_fp32w<MB, NW, (NW == 1 ? kAdjRing : 3), kAdjWarps>, 32 * NW, 0);
-  return n;
-}
-
-int fp32w_team(int max_ny);
-
-void launch_adj_fp32w(const BatchArgs& a, int grid, int bands, cudaStream_t st) {
-  switch (bands) {
-    case 1: launch_adj<1, 1>(a, grid, st); break;
-    case 2: launch_adj<2, 1>(a, grid, st); break;
-    case 3: launch_adj<3, 1>(a, grid, st); break;
-    case 4: launch_adj<4, 1>(a, grid, st); break;
-    default:
-      switch (fp32w_team(32 * bands)) {
-        case 2: launch_adj<4, 2>(a, grid, st); break;
-        case 3: launch_adj<4, 3>(a, grid, st); break;
-        default: launch_adj<4, 4>(a, grid, st); break;
-      }
-  }
-}
-
-int adj_fp32w_max_blocks_per_sm(int bands) {
-  switch (bands) {
-    case 1: return occupancy_adj<1, 1>();
-    case 2: return occupancy_adj<2, 1>();
-    case 3: return occupancy_adj<3, 1>();
-    case 4: return occupancy_adj<4, 1>();
-    default:
-      switch (fp32w_team(32 * bands)) {
-        case 2: return occupancy_adj<4, 2>();
-        case 3: return occupancy_adj<4, 3>();
-        default: return occupancy_adj<4, 4>();
-      }
-  }
-}
-
 int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 
 // Variants of the warp kernel: operand loads, resident warps per SM, whole
-// solves or solves cut into items, adjoint fields in the solve kernel or in
-// the adjoint kernel.
-//   0: every operand loaded a step ahead into registers, 8 warps per SM,
-//      items, adjoint fields in k_adj_fp32w (operands three steps ahead)
-//   1: register prefetch, 8 warps per SM, whole solves (fused)
-//   2: cell constants loaded at the visit, 12 warps per SM, items (fused)
+// solves or solves cut into items.
+//   0: every operand loaded a step ahead into registers, 8 warps per SM, items
+//   1: the same, whole solves
+//   2: cell constants loaded at the visit, 12 warps per SM, items
 //   3: cell constants loaded at the visit, 8 warps per SM, whole solves
-//   4: register prefetch, 8 warps per SM, items, adjoint fields in the solve
-//      kernel (one step ahead)
-constexpr int kFp32wVariants = 5;
+constexpr int kFp32wVariants = 4;
 int fp32w_variant_count() { return kFp32wVariants; }
-bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2 || variant == 4; }
-bool fp32w_variant_split(int variant) { return variant == 0; }
-int fp32w_items_for_mode(int mode, int split_adj) { return w_items_for_mode(mode, split_adj); }
+bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2; }
+int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
+
 template <int MB, int PF, int MINW, int NW>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
   k_batch_fp32w<MB, PF, MINW, NW><<<grid, 32 * NW, 0, st>>>(a);
@@ -1063,18 +948,20 @@ static int occupancy_w() {
 template <int MB, int NW>
 static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st) {
   switch (variant) {
+    case 0:
+    case 1: launch_w<MB, 1, 8, NW>(a, grid, st); break;
     case 2: launch_w<MB, 0, 12, NW>(a, grid, st); break;
-    case 3: launch_w<MB, 0, 8, NW>(a, grid, st); break;
-    default: launch_w<MB, 1, 8, NW>(a, grid, st); break;
+    default: launch_w<MB, 0, 8, NW>(a, grid, st); break;
   }
 }
 
 template <int MB, int NW>
 static int occupancy_mb(int variant) {
   switch (variant) {
+    case 0:
+    case 1: return occupancy_w<MB, 1, 8, NW>();
     case 2: return occupancy_w<MB, 0, 12, NW>();
-    case 3: return occupancy_w<MB, 0, 8, NW>();
-    default: return occupancy_w<MB, 1, 8, NW>();
+    default: return occupancy_w<MB, 0, 8, NW>();
   }
 }
 

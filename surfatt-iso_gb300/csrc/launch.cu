@@ -80,7 +80,6 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
       p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
       p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
       p.cut = fp32w_variant_items(p.pf);
-      p.split = fp32w_variant_split(p.pf);
     } else {
       p.per_sm = batch_fp32d_max_blocks_per_sm(p.bands, p.pf);
       p.ws_doubles = batch_fp32d_ws_doubles(sh.max_dcells, sh.max_nx);
@@ -96,13 +95,7 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.ws_doubles = batch_fp32_ws_doubles(sh.max_cells);
   }
   if (p.per_sm < 1) p.per_sm = 1;
-  const int units_per_solve = p.cut ? fp32w_items_for_mode(3, p.split ? 1 : 0) : 1;
-  // adjoint kernel of a split plan: up to two field units per solve
-  auto adj_grid_for = [&](int bands, int nsolve) {
-    int g = nsm * std::max(1, adj_fp32w_max_blocks_per_sm(bands));
-    if (max_grid > 0) g = std::min(g, max_grid);
-    return std::max(1, std::min(g, 2 * std::max(1, nsolve)));
-  };
+  const int units_per_solve = p.cut ? fp32w_items_for_mode(3) : 1;
   auto grid_for = [&](int per_sm, int nsolve) {
     int g = nsm * std::max(1, per_sm);
     if (max_grid > 0) g = std::min(g, max_grid);
@@ -111,7 +104,6 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     return std::max(1, std::min(g, need));
   };
   p.grid = grid_for(p.per_sm, sh.nsolve);
-  if (p.split) p.adj_grid = adj_grid_for(p.bands, sh.nsolve);
   // several team classes: one launch per class (the processing order holds
   // the classes contiguously, the largest team first)
   int nonempty = 0, counted = 0;
@@ -128,7 +120,6 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
         p.block = 32 * fp32w_team(sh.team_max_ny[c]);
         p.per_sm = std::max(1, batch_fp32w_max_blocks_per_sm(p.bands, p.pf));
         p.grid = grid_for(p.per_sm, sh.nsolve);
-        if (p.split) p.adj_grid = adj_grid_for(p.bands, sh.nsolve);
       }
   }
   if (p.kind == KK_FP32_WARP && nonempty > 1 && counted == sh.nsolve) {
@@ -143,7 +134,6 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
       p.class_bands[k] = fp32w_bands(sh.team_max_ny[c]);
       p.class_grid[k] =
           grid_for(batch_fp32w_max_blocks_per_sm(p.class_bands[k], p.pf), sh.team_count[c]);
-      if (p.split) p.class_adj_grid[k] = adj_grid_for(p.class_bands[k], sh.team_count[c]);
       p.grid += p.class_grid[k];
       off += sh.team_count[c];
     }
@@ -199,18 +189,15 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   A.smem_bytes = plan.smem;
   A.items = 1;
   A.sstate = nullptr;
-  const bool split = plan.kind == KK_FP32_WARP && plan.cut && plan.split && mode >= 2;
-  A.split_adj = split ? 1 : 0;
-  A.queue_adj = split ? queue + kTeamClasses : nullptr;
   if (plan.kind == KK_FP32_WARP && plan.cut) {
     const long long n = std::max(1, sh.nsolve);
-    A.items = fp32w_items_for_mode(mode, A.split_adj);
+    A.items = fp32w_items_for_mode(mode);
     A.sstate = reinterpret_cast<int*>(ws + n * plan.ws_doubles);
     if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
       return -ST_CUDA_ERROR;
   }
   int launches = 0;
-  if (cudaMemsetAsync(queue, 0, 2 * kTeamClasses * sizeof(int), st) != cudaSuccess)
+  if (cudaMemsetAsync(queue, 0, std::max(1, plan.classes) * sizeof(int), st) != cudaSuccess)
     return -ST_CUDA_ERROR;
   if (A.phase_cycles &&
       cudaMemsetAsync(A.phase_cycles, 0, PH_COUNT * sizeof(unsigned long long), st) != cudaSuccess)
@@ -248,11 +235,6 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
       }
       launch_batch_fp32w(C, plan.class_grid[k], plan.class_bands[k], plan.pf, sk);
       ++launches;
-      if (split) {
-        C.queue_adj = A.queue_adj + k;
-        launch_adj_fp32w(C, plan.class_adj_grid[k], plan.class_bands[k], sk);
-        ++launches;
-      }
       if (cs && k > 0 && (cudaEventRecord(cs->join[k - 1], sk) != cudaSuccess ||
                           cudaStreamWaitEvent(st, cs->join[k - 1], 0) != cudaSuccess))
         return -ST_CUDA_ERROR;
@@ -260,13 +242,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   } else if (sh.nsolve > 0) {
     if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_BLOCK) launch_batch_fp32(A, plan.grid, plan.block, st);
-    else if (plan.kind == KK_FP32_WARP) {
-      launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
-      if (split) {
-        launch_adj_fp32w(A, plan.adj_grid, plan.bands, st);
-        ++launches;
-      }
-    }
+    else if (plan.kind == KK_FP32_WARP) launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
     else launch_batch_fp32d(A, plan.grid, plan.bands, plan.pf, st);
     ++launches;
   }

@@ -63,8 +63,6 @@ struct LaunchPlan {
   int grid = 0, block = 0, per_sm = 0, smem_tau = 0, bands = 0, pf = 1;
   int slots_per_block = 1;   // solves resident per block (warps for KK_FP32_WARP)
   bool cut = false;          // solves cut into work items: one workspace slot per solve
-  bool split = false;        // KK_FP32_WARP: adjoint fields in k_adj_fp32w
-  int adj_grid = 0;          // its grid (one class), class_adj_grid per class
   size_t smem = 0;
   long long ws_doubles = 0;  // per resident solve
   // KK_FP32_WARP on a batch of several team classes: one launch per class
@@ -74,7 +72,6 @@ struct LaunchPlan {
   int classes = 1;
   int class_solves[kTeamClasses] = {}, class_off[kTeamClasses] = {};
   int class_grid[kTeamClasses] = {}, class_bands[kTeamClasses] = {};
-  int class_adj_grid[kTeamClasses] = {};
 };
 
 // Launch configuration for `prec` (0 FP64, 1 FP32) on `device`; grid capped
@@ -106,10 +103,9 @@ struct ClassStreams {
 // per-period reductions (modes 2, 3) and the misfit sum.  `ws` must hold
 // plan_ws_doubles(plan, nsolve) doubles; `queue` plan.classes ints.  The
 // class launches of a split plan run concurrently on `cs` (one after
-// another on `st` when null).  `queue` holds 2 * kTeamClasses ints (the
-// solve kernels' counters, then the adjoint kernels').  Records ev_k0/ev_k1
-// around the solve kernels when given.  Returns the number of kernel
-// launches, or a negative status.
+// another on `st` when null).  Records ev_k0/ev_k1 around the solve
+// kernels when given.  Returns the number of kernel launches, or a negative
+// status.
 int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan& plan, int mode,
                        int prec, double* ws, int* queue, cudaStream_t st, cudaEvent_t ev_k0,
                        cudaEvent_t ev_k1, const ClassStreams* cs = nullptr);

@@ -321,7 +321,7 @@ int start_request(surfatt_server* S, Request& r) {
     r.status_d = cv.take<int>(ns);
     r.fit = cv.take<int>(ns);
     r.ait = cv.take<int>(ns);
-    r.queue = cv.take<int>(2 * kTeamClasses);
+    r.queue = cv.take<int>(kTeamClasses);
     r.ws = cv.take<double>((size_t)plan_ws_doubles(r.plan, L.nsolve));
   };
   Carver sizer;
