@@ -91,17 +91,19 @@ __device__ __forceinline__ void tsum_max2(double& a, double& b, double& c) {
 }
 
 
-// Workspace per warp slot: S (float4: T0, T0x, T0y, -), W (float4 adjoint
-// weights), tau, old, 1/d, two scaled adjoint sources.
+// Workspace per warp slot: W (float4 adjoint weights), G (float2: T0x,
+// T0y), T0, tau, old, 1/d, two scaled adjoint sources (4 bytes each per
+// cell), per-column half-angle sines and cosines.
 long long batch_fp32w_ws_doubles(long long N) {
-  const long long floats = 8 * N + 5 * N + 2 * 4096;
+  const long long floats = 4 * N + 2 * N + 6 * N + 2 * 4096;
   long long d = (floats + 1) / 2 + 64;
   return (d + 31) / 32 * 32;  // keep every slot 256-byte aligned
 }
 
 struct WSlot {
-  float4* S;
   float4* W;
+  float2* G;
+  float* T0;
   float* tau;
   float* old;
   float* id;
@@ -111,9 +113,10 @@ struct WSlot {
 
 __device__ inline WSlot wcarve(double* base, size_t N) {
   WSlot V;
-  V.S = reinterpret_cast<float4*>(base);
-  V.W = V.S + N;
-  V.tau = reinterpret_cast<float*>(V.W + N);
+  V.W = reinterpret_cast<float4*>(base);
+  V.G = reinterpret_cast<float2*>(V.W + N);
+  V.T0 = reinterpret_cast<float*>(V.G + N);
+  V.tau = V.T0 + N;
   V.old = V.tau + N;
   V.id = V.old + N;
   V.src[0] = V.id + N;
@@ -123,7 +126,7 @@ __device__ inline WSlot wcarve(double* base, size_t N) {
 }
 
 
-// T0, T0x, T0y of every cell into S; tau initialised (1 in the frozen box).
+// T0 and (T0x, T0y) of every cell; tau initialised (1 in the frozen box).
 template <int NW>
 __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSolve& w,
                             const WSlot& V, const Tm<NW>& T) {
@@ -139,7 +142,9 @@ __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSol
     const T0Row row = t0_row(P, src, j);
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
-      V.S[k] = t0_cell(P, src, row, i, j, V.col[i], V.col[nx + i]);
+      const float4 c = t0_cell(P, src, row, i, j, V.col[i], V.col[nx + i]);
+      V.T0[k] = c.x;
+      V.G[k] = make_float2(c.y, c.z);
       V.tau[k] = w.box.has(i, j) ? 1.0f : 10.0f;
     }
   }
@@ -147,67 +152,49 @@ __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSol
 }
 
 
-// The cell's constants (T0 gradient, metric, slowness, one-sided terms).
-__device__ __forceinline__ void wf_load_heavy(WFwd& o, int k, const PeriodDev& P, const WSlot& V) {
-  const float4 sv = V.S[k];
-  o.gx = sv.y;
-  o.gy = sv.z;
-  o.pa = P.p4a[k];
-  const float4 pb = P.p4b[k];
-  o.dsx = pb.x;
-  o.dsy = pb.y;
-}
+// The sweep's constants of one lane row (logical row v of the sweep's
+// frame, physical row j): the cell visited at step t is on the grid when
+// 0 <= t - lo < nx and is then cell kb + xdir * t; it is frozen when
+// 0 <= t - flo <= flen (flo far away for a row outside the frozen box).
+struct WRow {
+  int lo, kb, flo;
+  bool hass, hasn;  // the row has a south / north neighbour
+};
 
-// HEAVY: also load the constants now (a step ahead of their use) rather
-// than at the visit.
-// EXCH: also the values the lanes exchange (own, t0); else the caller
-// supplies them.
-template <bool HEAVY, bool EXCH = true>
-__device__ __forceinline__ void wf_load(WFwd& o, int t, int v, int nx, int ny, int xdir, int ydir,
-                                        const PeriodDev& P, const WSlot& V, const Box& box,
-                                        bool last) {
-  const int u = t - v;
-  o.on = v < ny && u >= 0 && u < nx;
-  if (!o.on) {
-    o.own = 0.f;
-    o.t0 = 0.f;
-    return;
+__device__ __forceinline__ WRow w_row(int v, int nx, int ny, int xdir, int ydir, const Box& box) {
+  WRow r;
+  constexpr int kFar = 1 << 29;
+  if (v >= ny) {
+    r.lo = kFar;
+    r.kb = 0;
+    r.flo = kFar;
+    r.hass = r.hasn = false;
+    return r;
   }
-  const int i = xdir > 0 ? u : nx - 1 - u;
   const int j = ydir > 0 ? v : ny - 1 - v;
-  const int k = i + nx * j;
-  o.frz = box.has(i, j);
-  if (EXCH) {
-    o.own = V.tau[k];
-    o.t0 = reinterpret_cast<const float*>(V.S)[4 * k];
-  }
-  if (HEAVY) {
-    wf_load_heavy(o, k, P, V);
-    if (last) o.old = V.old[k];
-  }
+  r.lo = v;
+  r.kb = nx * j + (xdir > 0 ? -v : nx - 1 + v);
+  const bool rib = box.i0 <= box.i1 && box.j0 <= j && j <= box.j1;
+  r.flo = rib ? v + (xdir > 0 ? box.i0 : nx - 1 - box.i1) : kFar;
+  r.hass = v > 0;
+  r.hasn = v < ny - 1;
+  return r;
 }
 
-
-// The value and T0 of row v's cell at step t (0 off the grid).
-__device__ __forceinline__ void wf_exch(float& own, float& t0, int t, int v, int nx, int ny,
-                                        int xdir, int ydir, const WSlot& V) {
-  const int u = t - v;
-  own = 0.f;
-  t0 = 0.f;
-  if (v < ny && u >= 0 && u < nx) {
-    const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? v : ny - 1 - v);
-    own = V.tau[k];
-    t0 = reinterpret_cast<const float*>(V.S)[4 * k];
-  }
-}
-
-// PF = 1: every operand of the next step is loaded a step ahead; PF = 0:
-// only the values exchanged between lanes are, the cell's constants are
-// loaded at the visit (they stream along the lane's row and hit in L1),
-// which frees registers for more resident warps.
 // Iterations it0 .. it1 (1-based; the reference runs 1 .. MaxIter): status
 // ST_OK and the iteration count when one of them converges, otherwise
 // ST_NOT_CONVERGED and it1.
+//
+// Per band, a lane holds three kinds of operands.  The values it exchanges
+// with its neighbours -- old tau and T0 of its cell at steps t and t + 1 --
+// sit in a ring loaded two steps ahead (a cell is written only at its own
+// visit, so an early read sees the value a read at the visit would).  The
+// cell constants of step t (T0 gradient, metric and slowness record,
+// one-sided terms, iteration-start tau) are loaded into the band's
+// registers right after the band's visit of step t - 1 (PF = 1: they have a
+// whole step to arrive and are never copied) or at the visit itself
+// (PF = 0: fewer live registers).  Row constants (WRow) are computed once
+// per sweep, so a step costs a few integer operations per band.
 template <int MB, int PF, int NW>
 __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w,
                                     const Tm<NW>& T, int it0, int it1, int* status_out,
@@ -215,6 +202,12 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const int nsteps = nx + ny - 1;
+  const float* const T0a = V.T0;
+  const float* const tau = V.tau;
+  const float2* const G = V.G;
+  const float4* const PA = P.p4a;
+  const float2* const PB = reinterpret_cast<const float2*>(P.p4b);  // {disx, disy} at 2k
+  const int flen = w.box.i1 > w.box.i0 ? w.box.i1 - w.box.i0 : 0;
   // Teams: warp w owns the rows vb .. vb + 32 MB - 1.  The south neighbour
   // of its first row is the last row of warp w-1, visited a step earlier:
   // it comes through a shared slot (double-buffered by step parity, one
@@ -233,60 +226,70 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
       const bool last = s == 3;
-      // old tau and T0 of the cell north of the top row at step tau
-      auto north_of_top = [&](int tau, float& own, float& t0) {
-        const int u = tau - vtop;
+      WRow R[MB];
+#pragma unroll
+      for (int m = 0; m < MB; ++m) R[m] = w_row(vb + lane + 32 * m, nx, ny, xdir, ydir, w.box);
+      // old tau and T0 of band m's cell at step tt (0 off the grid)
+      auto exch = [&](int m, int tt, float& own, float& t0) {
+        own = 0.f;
+        t0 = 0.f;
+        if ((unsigned)(tt - R[m].lo) < (unsigned)nx) {
+          const int k = R[m].kb + xdir * tt;
+          own = tau[k];
+          t0 = T0a[k];
+        }
+      };
+      // the cell constants of band m at step tt
+      float gx[MB], gy[MB], dsx[MB], dsy[MB], old[MB];
+      float4 pa[MB];
+      auto heavy = [&](int m, int tt) {
+        if ((unsigned)(tt - R[m].lo) < (unsigned)nx) {
+          const int k = R[m].kb + xdir * tt;
+          const float2 g = G[k];
+          gx[m] = g.x;
+          gy[m] = g.y;
+          pa[m] = PA[k];
+          const float2 d = PB[2 * k];
+          dsx[m] = d.x;
+          dsy[m] = d.y;
+          if (last) old[m] = V.old[k];
+        }
+      };
+      // old tau and T0 of the cell north of the top row at step tt
+      auto north_of_top = [&](int tt, float& own, float& t0) {
+        const int u = tt - vtop;
         own = 0.f;
         t0 = 0.f;
         if (u >= 0 && u < nx && vtop + 1 < ny) {
           const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? vtop + 1 : ny - 2 - vtop);
-          own = V.tau[k];
-          t0 = reinterpret_cast<const float*>(V.S)[4 * k];
+          own = tau[k];
+          t0 = T0a[k];
         }
       };
-      // With register prefetch a single warp loads the values the lanes
-      // exchange within a step (the next cell's tau and T0) two steps ahead,
-      // the other operands one (a cell is written only at its own visit).
-      // (Teams keep one step: the extra registers spill in their loop.)
-      constexpr bool EX2 = PF == 1 && NW == 1;
-      float res[MB], t0prev[MB], own2[MB], t02[MB];
-      WFwd cur[MB];
+      // exchange ring: steps t (x0), t + 1 (x1), t + 2 (x2, in flight)
+      float res[MB], t0prev[MB], x0o[MB], x0t[MB], x1o[MB], x1t[MB], x2o[MB], x2t[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
         t0prev[m] = 0.f;
-        wf_load<PF == 1>(cur[m], 0, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box, last);
-        if (EX2) wf_exch(own2[m], t02[m], 1, vb + lane + 32 * m, nx, ny, xdir, ydir, V);
+        exch(m, 0, x0o[m], x0t[m]);
+        exch(m, 1, x1o[m], x1t[m]);
+        exch(m, 2, x2o[m], x2t[m]);
+        if (PF == 1) heavy(m, 0);
       }
       float pn_own = 0.f, pn_t0 = 0.f;
       if (top) north_of_top(0, pn_own, pn_t0);
       for (int t = 0; t < nsteps; ++t) {
-        WFwd nxt[MB];
-#pragma unroll
-        for (int m = 0; m < MB; ++m) {
-          if (EX2) {
-            wf_load<true, false>(nxt[m], t + 1, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V,
-                                 w.box, last);
-            nxt[m].own = own2[m];
-            nxt[m].t0 = t02[m];
-            wf_exch(own2[m], t02[m], t + 2, vb + lane + 32 * m, nx, ny, xdir, ydir, V);
-          } else {
-            wf_load<PF == 1>(nxt[m], t + 1, vb + lane + 32 * m, nx, ny, xdir, ydir, P, V, w.box,
-                             last);
-          }
-        }
         float qn_own = 0.f, qn_t0 = 0.f;
         if (top) north_of_top(t + 1, qn_own, qn_t0);
         // Bands in descending order: band m's south neighbours include lane 31
-        // of band m-1, whose value must still be the previous step's.  Each
-        // band exchanges its values right before its visit, which keeps the
-        // live registers to one band's worth.
+        // of band m-1, whose value must still be the previous step's.
         float dds[MB];
 #pragma unroll
         for (int mm = 0; mm < MB; ++mm) {
           const int m = MB - 1 - mm;
           float south = w_below<MB>(res, m, lane), t0s = w_below<MB>(t0prev, m, lane);
-          float north = w_above_own<MB>(nxt, m, lane), t0n = w_above_t0<MB>(nxt, m, lane);
+          float north = w_above<MB>(x1o, m, lane), t0n = w_above<MB>(x1t, m, lane);
           if (NW > 1) {
             if (m == 0 && bot) {
               south = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
@@ -298,36 +301,48 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
             }
           }
           dds[m] = 0.f;
-          if (cur[m].on) {
-            const int v = vb + lane + 32 * m, u = t - v;
-            const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? v : ny - 1 - v);
+          const int tl = t - R[m].lo;
+          if ((unsigned)tl < (unsigned)nx) {
+            const int k = R[m].kb + xdir * t;
+            const bool frz = (unsigned)(t - R[m].flo) <= (unsigned)flen;
             float nv;
-            if (cur[m].frz) {
-              nv = cur[m].own;
+            if (frz) {
+              nv = x0o[m];
             } else {
-              if (PF == 0) {
-                wf_load_heavy(cur[m], k, P, V);
-                if (last) cur[m].old = V.old[k];
-              }
-              nv = wf_visit(cur[m], res[m], nxt[m].own, south, north, t0prev[m], nxt[m].t0, t0s,
-                            t0n, u > 0, v > 0, u < nx - 1, v < ny - 1, xdir, ydir, idx, idy);
+              if (PF == 0) heavy(m, t);
+              WFwd o;
+              o.own = x0o[m];
+              o.t0 = x0t[m];
+              o.gx = gx[m];
+              o.gy = gy[m];
+              o.pa = pa[m];
+              o.dsx = dsx[m];
+              o.dsy = dsy[m];
+              nv = wf_visit(o, res[m], x1o[m], south, north, t0prev[m], x1t[m], t0s, t0n, tl > 0,
+                            R[m].hass, tl < nx - 1, R[m].hasn, xdir, ydir, idx, idy);
             }
             V.tau[k] = nv;
-            if (s == 0) V.old[k] = cur[m].own;
-            if (last && !cur[m].frz) dds[m] = fabsf(nv - cur[m].old) * cur[m].t0;
+            if (s == 0) V.old[k] = x0o[m];
+            if (last && !frz) dds[m] = fabsf(nv - old[m]) * x0t[m];
             res[m] = nv;
-            t0prev[m] = cur[m].t0;
+            t0prev[m] = x0t[m];
           }
           if (NW > 1 && m == MB - 1 && top) {
             xs_val[t & 1][T.wid] = res[m];
             xs_t0[t & 1][T.wid] = t0prev[m];
           }
+          // the band's cell constants of the next step, into the registers
+          // its visit has just consumed
+          if (PF == 1) heavy(m, t + 1);
         }
-        // the next step's operands, after every band's visit (the latest
-        // point: the loads issued at the start of this step have the whole
-        // step to arrive)
 #pragma unroll
-        for (int m = 0; m < MB; ++m) cur[m] = nxt[m];
+        for (int m = 0; m < MB; ++m) {
+          x0o[m] = x1o[m];
+          x0t[m] = x1t[m];
+          x1o[m] = x2o[m];
+          x1t[m] = x2t[m];
+          exch(m, t + 3, x2o[m], x2t[m]);
+        }
         if (last) {
           // in band order (the order of the row-major visit of a lane)
 #pragma unroll
@@ -363,10 +378,10 @@ template <int NW>
 __device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, const Tm<NW>& TM) {
   const int nx = P.nx, ny = P.ny, lane = TM.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
-  const float* T0 = reinterpret_cast<const float*>(V.S);
+  const float* T0 = V.T0;
   const float4* PA = P.p4a;
   // T = tau*T0 rounded on its own (no contraction with the differences below)
-  auto T = [&](size_t k) { return __fmul_rn(V.tau[k], T0[4 * k]); };
+  auto T = [&](size_t k) { return __fmul_rn(V.tau[k], T0[k]); };
   for (int j = TM.wid; j < ny; j += NW) {  // rows by warp, columns by lane
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
@@ -538,7 +553,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
 
 // T = tau*T0 at a node (FP64 product of the FP32 factors)
 __device__ __forceinline__ double w_T(const WSlot& V, size_t k) {
-  return (double)V.tau[k] * (double)reinterpret_cast<const float*>(V.S)[4 * k];
+  return (double)V.tau[k] * (double)V.T0[k];
 }
 
 // interp2_0_dp on the caller's increasing degree grid (src/shared/utils.f90:917-942)

@@ -153,6 +153,12 @@ __device__ __forceinline__ float w_above_own(const WFwd (&x)[MB], int m, int lan
   const float offer = lane == 0 ? x[m + 1 < MB ? m + 1 : m].own : x[m].own;
   return __shfl_sync(FULL, offer, (lane + 1) & 31);
 }
+// The same for a per-band value array.
+template <int MB>
+__device__ __forceinline__ float w_above(const float (&x)[MB], int m, int lane) {
+  const float offer = lane == 0 ? x[m + 1 < MB ? m + 1 : m] : x[m];
+  return __shfl_sync(FULL, offer, (lane + 1) & 31);
+}
 template <int MB>
 __device__ __forceinline__ float w_above_t0(const WFwd (&x)[MB], int m, int lane) {
   const float offer = lane == 0 ? x[m + 1 < MB ? m + 1 : m].t0 : x[m].t0;
