@@ -353,12 +353,14 @@ def run_ours(args):
     fp64_peak, fp32_peak = sg.measure_peaks(dev)
     eng = sg.Engine(dev)
     eng.load(pb)
+    # both paths get the autotuner (FP64: solves cut into work items or whole)
+    tuned64 = eng.autotune(pb.mode, sg.PREC_FP64)
     # correctness of the headline against the plain FP64 path on this workload
     eng.run(pb.mode, sg.PREC_FP64)
     eng.sync()
     r64 = eng.results()
     fwd64, adj64 = eng.work()
-    launch64 = eng.launch_config()
+    launch64 = dict(eng.launch_config(), **eng.kernel_variant())
     tuned = eng.autotune(pb.mode, sg.PREC_FP32)
     eng.run(pb.mode, sg.PREC_FP32)
     eng.sync()
@@ -495,7 +497,8 @@ def run_ours(args):
                          "hbm_view": _hbm_view(traffic, k32_ms)},
             "cpu_baseline": cpu, "parity": parity,
             "phase_mcycles_per_solve": phases,
-            "launch": {"fp32": launch32, "fp64": launch64, "autotune": tuned},
+            "launch": {"fp32": launch32, "fp64": launch64, "autotune": tuned,
+                       "autotune_fp64": tuned64},
             "iterations": {"fwd_mean": float(np.mean(r32["fwd_iters"])),
                            "adj_mean": float(np.mean(r32["adj_iters"]))},
             "wall_s_timed_region": wall,
@@ -663,6 +666,7 @@ def _side_config4(sg, flush, dev):
     pb = W.config4()
     eng = sg.Engine(dev)
     eng.load(pb)
+    eng.autotune(pb.mode, sg.PREC_FP64)
     eng.run(pb.mode, sg.PREC_FP64)
     eng.sync()
     r64 = eng.results()

@@ -154,36 +154,105 @@ __device__ inline SolveLayout carve(double* base, size_t N) {
   return L;
 }
 
+// With A.items == kFp64Items a solve is cut into work items as in the FP32
+// row kernel: the queue hands out every solve's item 0, then every item 1,
+// ..., so the last round of a batch is one short item rather than whole
+// solves (1280 solves on 608 resident blocks are 2.1 rounds of whole
+// solves: a third of the last round's SMs would idle).  Items 0 ..
+// kFp64Items - 2 run kFp64SplitIter forward iterations; the last runs the
+// sweeps to convergence and the solve's tail (receivers, misfit, adjoints,
+// mask, kernel slot).  Only tau persists between items, in the solve's own
+// array (A.ws_solve at the solve's kernel-slot offset): every item
+// recomputes T0 and the hoisted constants in its block's scratch, to the
+// same bits, so the results equal the whole-solve kernel's.  An item waits,
+// bounded, for its solve's previous item (taken earlier by a resident
+// block); running out reports SURFATT_TIMEOUT for the solve.
 __global__ void __launch_bounds__(128) k_batch_fp64(BatchArgs A) {
   __shared__ SolveShared sh;
-  __shared__ int next;
+  __shared__ int next, prev_done, prev_fit, prev_fst;
   double* base = A.ws + (size_t)blockIdx.x * (size_t)A.ws_doubles;
+  const bool cut = A.items > 1;
+  const int nitem = cut ? A.items : 1;
   for (;;) {
     if (threadIdx.x == 0) next = atomicAdd(A.queue, 1);
     __syncthreads();
     const int q = next;
     __syncthreads();
-    if (q >= A.nsolve) break;
-    const int s = A.order[q];
+    if (q >= A.nsolve * nitem) break;
+    const int item = q / A.nsolve;
+    const int s = A.order[q % A.nsolve];
+    int* const ss = cut ? A.sstate + (size_t)kSolveStateInts * s : nullptr;
     const PeriodDev P = A.periods[A.pidx[s]];
     const size_t N = (size_t)P.nx * P.ny;
+    if (cut && item > 0) {
+      if (threadIdx.x == 0) {
+        int d = ld_acquire(ss + SS_DONE), it = 0;
+        while (d >= 0 && d < item && it < kItemWaitLimit) {
+          __nanosleep(128);
+          d = ld_acquire(ss + SS_DONE);
+          ++it;
+        }
+        prev_done = d;
+        prev_fit = ss[SS_FIT];
+        prev_fst = ss[SS_FST];
+      }
+      __syncthreads();
+      const int d = prev_done;
+      if (d < 0) continue;  // the solve failed in an earlier item
+      if (d < item) {       // wait limit: report and drop the solve
+        solve_fail(A, P, s, ST_TIMEOUT);
+        if (threadIdx.x == 0) {
+          __threadfence();
+          st_release(ss + SS_DONE, -1);
+        }
+        __syncthreads();
+        continue;
+      }
+    }
     if (threadIdx.x == 0) sh.flag = ST_OK;
     SolveLayout L = carve(base, N);
+    FwdWs fw = L.fw;
+    if (cut) fw.tau = A.ws_solve + A.kslot[s];
     double x0 = A.srcx[s], y0 = A.srcy[s];
     if (P.lonlat) {
       x0 = x0 / 180.0 * PI_S;
       y0 = y0 / 180.0 * PI_S;
     }
-    fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, L.fw, true, sh);
+    fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, fw, true, sh, !cut || item == 0);
     if (sh.status != ST_OK) {
       const int st = sh.status;
       __syncthreads();
       solve_fail(A, P, s, st);
+      if (cut && threadIdx.x == 0) {
+        __threadfence();
+        st_release(ss + SS_DONE, -1);
+      }
+      __syncthreads();
       continue;
     }
-    uw_sweeps(P, L.fw, sh, MAXITER_UW);
-    const int fst = sh.status, fit = sh.iters;
-    for (size_t k = threadIdx.x; k < N; k += blockDim.x) L.T[k] = L.fw.tau[k] * L.fw.T0[k];
+    const bool last = !cut || item == nitem - 1;
+    int fst, fit;
+    if (cut && item > 0 && prev_fst == ST_OK) {  // converged in an earlier item
+      fst = ST_OK;
+      fit = prev_fit;
+    } else {
+      const int it0 = cut && item > 0 ? prev_fit + 1 : 1;
+      const int it1 = last ? MAXITER_UW : (item + 1) * kFp64SplitIter;
+      uw_sweeps(P, fw, sh, it1, it0);
+      fst = sh.status;
+      fit = sh.iters;
+    }
+    if (!last) {
+      if (threadIdx.x == 0) {
+        ss[SS_FIT] = fit;
+        ss[SS_FST] = fst;
+        __threadfence();
+        st_release(ss + SS_DONE, item + 1);
+      }
+      __syncthreads();
+      continue;
+    }
+    for (size_t k = threadIdx.x; k < N; k += blockDim.x) L.T[k] = fw.tau[k] * L.fw.T0[k];
     if (A.fwd_updates && threadIdx.x == 0) {
       const Box b = sh.box;
       const double frozen = (double)(b.i1 - b.i0 + 1) * (b.j1 - b.j0 + 1);
@@ -191,6 +260,11 @@ __global__ void __launch_bounds__(128) k_batch_fp64(BatchArgs A) {
     }
     __syncthreads();
     solve_tail(A, P, s, L.T, L.aw, sh, fst, fit);
+    if (cut && threadIdx.x == 0) {
+      __threadfence();
+      st_release(ss + SS_DONE, nitem);
+    }
+    __syncthreads();
   }
 }
 

@@ -63,6 +63,7 @@ struct BatchArgs {
   // workspace
   double* ws;              // slots of ws_doubles each
   long long ws_doubles;
+  double* ws_solve = nullptr;  // FP64 kernel with items: per-solve tau, at kslot[s]
   int* queue;              // work counter (zeroed before launch)
   int block;               // threads per block (for info)
   int max_nx;              // largest nx over periods (shared-memory column arrays)
@@ -147,6 +148,29 @@ int fp32w_variant_count();
 bool fp32w_variant_items(int variant);
 int fp32w_items_for_mode(int mode);
 constexpr int kSolveStateInts = 5;
+// Per-solve state record (ints) of a solve cut into items: items done (-1:
+// failed), forward iterations, forward status, running status, adjoint
+// iterations of field 0.
+enum SolveStateSlot { SS_DONE = 0, SS_FIT, SS_FST, SS_ST, SS_ITS0 };
+// Bounded wait for a solve's previous item (polls, each followed by a short
+// sleep).
+constexpr int kItemWaitLimit = 1 << 24;
+// Release / acquire of a solve's state record between the warps or blocks
+// that run its consecutive items.
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Plain FP64 kernel cut into work items (BatchArgs::items = kFp64Items):
+// items 0 .. kFp64Items - 2 run kFp64SplitIter forward iterations each, the
+// last runs the forward sweeps to convergence and the rest of the solve.
+constexpr int kFp64Items = 3;
+constexpr int kFp64SplitIter = 2;
 // The same solve on the diagonal layouts (PeriodDev::qa / qd prepared), its
 // operands staged in shared memory; `variant` < fp32d_variant_count().
 void launch_batch_fp32d(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st);

@@ -705,20 +705,6 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlo
 // earlier, so the waits cannot form a cycle.
 constexpr int kSplitIter = 2;
 constexpr int kFwdItems = 3;
-// Per-solve state record (ints): items done (-1: failed), forward
-// iterations, forward status, running status, adjoint iterations of field 0.
-enum { SS_DONE = 0, SS_FIT, SS_FST, SS_ST, SS_ITS0 };
-// Bounded wait for the previous item (polls, each followed by a short sleep).
-constexpr int kItemWaitLimit = 1 << 24;
-
-__device__ __forceinline__ int ld_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release(int* p, int v) {
-  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // Items per solve for `mode` when solves are cut.
 __host__ __device__ inline int w_items_for_mode(int mode) {

@@ -26,8 +26,10 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
     max_dcells = std::max(max_dcells, diag_cells(nxs[p], nys[p]));
   }
   for (int c = 0; c < kTeamClasses; ++c) team_count[c] = team_max_ny[c] = 0;
+  solve_cells = 0;
   if (pidx)
     for (int s = 0; s < ns; ++s) {
+      solve_cells += (long long)nxs[pidx[s]] * nys[pidx[s]];
       const int y = nys[pidx[s]], c = team_class_key(y) - 1;
       if (c >= kTeamClasses) continue;  // taller than any team
       ++team_count[c];
@@ -38,7 +40,8 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
 std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
   std::vector<KernelChoice> c;
   if (prec == 0) {
-    c.push_back({KK_FP64, 0});
+    c.push_back({KK_FP64, 0});  // work items
+    c.push_back({KK_FP64, 1});  // whole solves
     return c;
   }
   if (sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)
@@ -56,10 +59,16 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     return ST_CUDA_ERROR;
   LaunchPlan p;
   if (prec == 0) {
+    // variant 0: solves cut into work items (per-solve tau arrays, needs the
+    // solves' cells); variant 1: whole solves
     p.kind = KK_FP64;
     p.block = 128;
     p.per_sm = batch_fp64_max_blocks_per_sm(p.block);
     p.ws_doubles = batch_fp64_ws_doubles(sh.max_cells);
+    p.pf = force.variant == 1 ? 1 : 0;
+    p.cut = p.pf == 0 && sh.solve_cells > 0;
+    if (!p.cut) p.pf = 1;
+    p.solve_doubles = p.cut ? sh.solve_cells : 0;
   } else if ((force.kind == KK_FP32_DIAG &&
               !(sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)) ||
              (force.kind == KK_FP32_WARP &&
@@ -95,7 +104,8 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.ws_doubles = batch_fp32_ws_doubles(sh.max_cells);
   }
   if (p.per_sm < 1) p.per_sm = 1;
-  const int units_per_solve = p.cut ? fp32w_items_for_mode(3) : 1;
+  const int units_per_solve =
+      p.cut ? (p.kind == KK_FP64 ? kFp64Items : fp32w_items_for_mode(3)) : 1;
   auto grid_for = [&](int per_sm, int nsolve) {
     int g = nsm * std::max(1, per_sm);
     if (max_grid > 0) g = std::min(g, max_grid);
@@ -144,9 +154,11 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
 
 long long plan_ws_doubles(const LaunchPlan& plan, int nsolve) {
   const long long n = std::max(1, nsolve);
+  const long long state = plan.cut ? (n * kSolveStateInts + 1) / 2 : 0;
+  if (plan.kind == KK_FP64 && plan.cut)  // block slots, per-solve tau, state
+    return (long long)plan.grid * plan.ws_doubles + plan.solve_doubles + state;
   // (a split plan's grid is the sum of its class grids: disjoint slots)
   const long long slots = plan.cut ? n : (long long)plan.grid * plan.slots_per_block;
-  const long long state = plan.cut ? (n * kSolveStateInts + 1) / 2 : 0;
   return slots * plan.ws_doubles + state;
 }
 
@@ -193,6 +205,14 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
     const long long n = std::max(1, sh.nsolve);
     A.items = fp32w_items_for_mode(mode);
     A.sstate = reinterpret_cast<int*>(ws + n * plan.ws_doubles);
+    if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
+      return -ST_CUDA_ERROR;
+  }
+  if (plan.kind == KK_FP64 && plan.cut) {
+    const long long n = std::max(1, sh.nsolve);
+    A.items = kFp64Items;
+    A.ws_solve = ws + (long long)plan.grid * plan.ws_doubles;
+    A.sstate = reinterpret_cast<int*>(A.ws_solve + plan.solve_doubles);
     if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
       return -ST_CUDA_ERROR;
   }

@@ -21,6 +21,7 @@ struct EvalShape {
   long long ncell = 0, max_cells = 0, max_pitched = 0;
   int max_nx = 0, max_ny = 0, max_diag = 0;
   long long max_dcells = 0;  // largest diag_cells over the periods
+  long long solve_cells = 0;  // sum over the solves of their grids' cells (with pidx)
   // Solves per team class and the class's tallest grid, counted when
   // from_grids is given the solves' period indices (else all zero: the
   // evaluation is launched as one class).
@@ -65,6 +66,7 @@ struct LaunchPlan {
   bool cut = false;          // solves cut into work items: one workspace slot per solve
   size_t smem = 0;
   long long ws_doubles = 0;  // per resident solve
+  long long solve_doubles = 0;  // KK_FP64 with items: per-solve tau arrays (all solves)
   // KK_FP32_WARP on a batch of several team classes: one launch per class
   // (largest team first), each over its contiguous part of the processing
   // order, with its own queue counter, band count and grid.  classes == 1:

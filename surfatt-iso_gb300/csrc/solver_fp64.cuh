@@ -70,9 +70,12 @@ struct SolveShared {
 // lon/lat: :801-872 (T0 = great-circle distance * fun0).  Cartesian UW:
 // :47-90.  (x0, y0) in sweep units.  Returns status via sh.status.
 // ---------------------------------------------------------------------------
+// init_tau = false leaves tau alone (a solve resumed from a previous work
+// item: only T0 and the hoisted constants, which are recomputed to the same
+// bits, are written).
 __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, double frozen_r,
                                  double tau_frozen, double tau_init, const FwdWs& W,
-                                 bool hoist, SolveShared& sh) {
+                                 bool hoist, SolveShared& sh, bool init_tau = true) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
   if (threadIdx.x == 0) {
@@ -150,7 +153,7 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
       }
     }
     W.T0[k] = t0;
-    W.tau[k] = box.has(i, j) ? tau_frozen : tau_init;
+    if (init_tau) W.tau[k] = box.has(i, j) ? tau_frozen : tau_init;
     if (!hoist) {
       W.K[(size_t)0 * N + k] = t0x;
       W.K[(size_t)1 * N + k] = t0y;
@@ -247,8 +250,10 @@ __device__ __forceinline__ double uw_update(const double* __restrict__ Kall, siz
 // Forward sweeps until |dtau|*T0 is below tol in L1 (mean) and Linf
 // (:881-1122).  tau_old is captured on each cell's first visit of an
 // iteration and the change is accumulated on its last visit.
+// Iterations it0 .. max_iter: sh.status = ST_OK and sh.iters = the
+// iteration that converged, or ST_NOT_CONVERGED and max_iter.
 __device__ inline void uw_sweeps(const PeriodDev& P, const FwdWs& W, SolveShared& sh,
-                                 int max_iter) {
+                                 int max_iter, int it0 = 1) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
   const Box box = sh.box;
@@ -258,7 +263,7 @@ __device__ inline void uw_sweeps(const PeriodDev& P, const FwdWs& W, SolveShared
   const double* __restrict__ T0 = W.T0;
   int iter;
   int status = ST_NOT_CONVERGED;
-  for (iter = 1; iter <= max_iter; ++iter) {
+  for (iter = it0; iter <= max_iter; ++iter) {
     double l1 = 0.0, linf = 0.0;
     for (int s = 0; s < 4; ++s) {
       SweepGeom g;

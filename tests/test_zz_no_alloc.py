@@ -7,9 +7,11 @@ cudaFree.  It takes device arrays and uses a fixed scratch array compiled into
 the library.  This test calls it through the C ABI twice in a row, the second
 time on a smaller grid with another source (so the scratch regions sit at
 other offsets and hold other sizes: leftovers of the first call would show),
-and compares each result bit for bit with the ordinary drop-in entry point,
-fsm_uw_ps_lonlat_2d_ (the same FP64 solver code on the same inputs), and with
-the oracle within the plain path's travel-time tolerance.  The file is
+and compares each result with the ordinary drop-in entry point,
+fsm_uw_ps_lonlat_2d_ (the same FP64 solver code on the same inputs; the
+per-grid metric is precomputed by a different kernel, so the two may differ
+in the last bits: 1e-10 relative), and with the oracle within the plain
+path's travel-time tolerance (1e-6).  The file is
 collected last so that a run stopping at the first failure has already run
 every other test.
 """
@@ -22,6 +24,7 @@ from surfatt_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 TT_TOL = 1e-6
+SAME_SOLVER_TOL = 1e-10
 
 
 def _case(nx, ny, m12):
@@ -57,7 +60,7 @@ def test_noalloc_matches_dropin_two_calls(sg, oracle):
         Td, sd, idr = sg.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12a, fun, *src)
         assert status == sd == sg.OK
         assert iters == idr
-        assert np.array_equal(T, Td)
+        assert rel_pointwise(T, Td) <= SAME_SOLVER_TOL
         Tr, sr, ir = oracle.fsm_uw_ps_lonlat_2d(xx, yy, m11, m22, -m12a, fun, *src)
         assert sr == 0 and iters == ir
         assert rel_pointwise(T, Tr) <= TT_TOL
