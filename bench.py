@@ -1068,14 +1068,20 @@ def run_dropin(args):
                        "the reference's MPI ranks), contiguous source blocks",
                        "single_caller": {"value": len(srcs) / s_one, "unit": "sources/s",
                                          "ms_per_step": s_one * 1e3},
-                       "note": "every call copies its host arrays to the device and its "
-                               "result back (the callee keeps no state): value and e2e are "
-                               "the same measurement",
-                       "l2": "inputs re-copied from the host every call"},
+                       "note": "every call takes host arrays and returns its result in "
+                               "host arrays: value and e2e are the same measurement; a "
+                               "calling thread's inputs that equal, bit for bit, what its "
+                               "context already holds on the device (grid, metric and "
+                               "slowness of its previous call, the travel times or adjoint "
+                               "field its previous call returned) are not copied again, so "
+                               "h2d_bytes_per_step counts the arrays passed, not the bytes "
+                               "moved",
+                       "l2": "no flush: consecutive calls reuse their thread's device copies"},
             "clocks": ck,
             "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": s_many * 1e3,
-                    "host_buffers": "pageable (the caller's arrays)"},
+                    "host_buffers": "pageable (the caller's arrays), copied through "
+                                    "per-thread pinned staging"},
             "gpu_launches": 5 * len(srcs) * args.steps,
             "roofline": {"bound": "fp64", "bound_note": "one 256-thread block per call (one "
                          "SM); achieved = reference-formulation FP64 flops of the timed calls "

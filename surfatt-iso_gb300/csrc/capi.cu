@@ -95,6 +95,25 @@ struct ThreadCtx {
   SmoothPlan sm_plan;            // plan of the table on the device
   std::vector<double> sm_key;    // nx, ny, sigma, lons, lats of that table
   int* si_host = nullptr;  // pinned {status, iters}
+  // Pinned staging for the host <-> device copies of a call.  The caller's
+  // arrays are pageable (Fortran arrays); a copy from pageable memory goes
+  // through the driver's own staging buffer, which the threads of a process
+  // share and take turns on.  Each call copies through its own thread's
+  // pinned buffer instead (sized per call, offsets bumped per copy, reused
+  // after the call's final synchronisation).
+  double* hst = nullptr;
+  size_t hst_cap = 0, hst_off = 0;
+  // What the device already holds, as host copies of the inputs it came
+  // from (compared bit for bit at the next call): consecutive calls of a
+  // rank share the grid, metric and slowness, the adjoint takes the travel
+  // times the forward call just returned, and the mask the adjoint field
+  // the adjoint call just returned.  A matching input is not sent again.
+  bool grid_ok = false, v_ok = false, v_null = false, t_ok = false, out_ok = false;
+  int gk_nx = -1, gk_ny = -1, gk_flags = -1;
+  std::vector<double> gk;  // xx | yy | A | B | C of the grid on the device
+  std::vector<double> vk;  // its V (slowness or velocity)
+  std::vector<double> tk;  // content of T (device)
+  std::vector<double> ok;  // content of out (device)
   ~ThreadCtx() {
     if (!init) return;
     pb.release();
@@ -102,6 +121,7 @@ struct ThreadCtx {
                     &sm_tab, &sm_nyw, &sm_per})
       d->release();
     if (si_host) cudaFreeHost(si_host);
+    if (hst) cudaFreeHost(hst);
     if (st) cudaStreamDestroy(st);
   }
   int setup() {
@@ -110,6 +130,27 @@ struct ThreadCtx {
     if (cudaMallocHost(&si_host, 4 * sizeof(int)) != cudaSuccess) return SURFATT_CUDA_ERROR;
     init = true;
     return SURFATT_OK;
+  }
+  // start of a call: room for `doubles` staged doubles
+  int stage_begin(size_t doubles) {
+    hst_off = 0;
+    if (doubles <= hst_cap) return SURFATT_OK;
+    if (hst) cudaFreeHost(hst);
+    hst = nullptr;
+    hst_cap = 0;
+    if (cudaMallocHost(&hst, doubles * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return SURFATT_OOM;
+    }
+    hst_cap = doubles;
+    return SURFATT_OK;
+  }
+  // n doubles of the staging buffer (filled from src when given)
+  double* stage(const double* src, size_t n) {
+    double* p = hst + hst_off;
+    if (src && n) std::memcpy(p, src, n * sizeof(double));
+    hst_off += (n + 1) & ~(size_t)1;  // 16-byte steps
+    return p;
   }
 };
 
@@ -121,24 +162,71 @@ int record(int st, int iters) {
   return st;
 }
 
-// Upload one grid + fields and run the per-period precompute.
-// conv: coordinates are degrees on a sphere (lon/lat) or Cartesian.
+// Whether v[off, off + n) holds x[0, n) bit for bit.
+bool same_as(const std::vector<double>& v, size_t off, const double* x, size_t n) {
+  return v.size() >= off + n && (n == 0 || std::memcmp(v.data() + off, x, n * sizeof(double)) == 0);
+}
+
+// Host -> device through the thread's pinned staging.
+int h2d(ThreadCtx& c, void* dev, const double* src, size_t n) {
+  if (!n) return SURFATT_OK;
+  double* p = c.stage(src, n);
+  CK(cudaMemcpyAsync(dev, p, n * sizeof(double), cudaMemcpyHostToDevice, c.st));
+  return SURFATT_OK;
+}
+
+// Staged doubles per call for an nx x ny grid and nr receivers.
+size_t stage_doubles(int nx, int ny, int nr) {
+  return 8 * (size_t)nx * ny + nx + ny + 3 * (size_t)(nr > 0 ? nr : 0) + 64;
+}
+
+// Upload one grid + fields and run the per-period precompute, unless the
+// device already holds them.  need_v = false: the caller uses only the
+// metric (the adjoint), so a grid whose metric matches is reused whatever
+// slowness came with it.
 int prep_single(ThreadCtx& c, const double* xx, const double* yy, int nx, int ny, const double* A,
                 const double* B, const double* C, const double* V, int lonlat, int from_model,
-                PeriodDev* P) {
+                PeriodDev* P, bool need_v = true) {
   const size_t N = (size_t)nx * ny;
+  const void* before = c.pb.A.p;
   if (c.pb.ensure(nx, ny)) return SURFATT_OOM;
-  CK(cudaMemcpyAsync(c.pb.xdeg.p, xx, nx * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.pb.ydeg.p, yy, ny * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.pb.A.p, A, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.pb.B.p, B, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  CK(cudaMemcpyAsync(c.pb.C.p, C, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  if (V) CK(cudaMemcpyAsync(c.pb.V.p, V, N * sizeof(double), cudaMemcpyHostToDevice, c.st));
-  else CK(cudaMemsetAsync(c.pb.V.p, 0, N * sizeof(double), c.st));
-  PrepIn in{nx, ny, lonlat, c.pb.xdeg.as<double>(), c.pb.ydeg.as<double>(), c.pb.A.as<double>(),
-            c.pb.B.as<double>(), c.pb.C.as<double>(), c.pb.V.as<double>(), from_model};
-  launch_prep(in, c.pb.out(), c.st);
-  CK(cudaGetLastError());
+  if (c.pb.A.p != before) c.grid_ok = c.v_ok = false;  // buffers moved
+  const int flags = lonlat | (from_model << 1);
+  const bool gsame = c.grid_ok && c.gk_nx == nx && c.gk_ny == ny && c.gk_flags == flags &&
+                     same_as(c.gk, 0, xx, nx) && same_as(c.gk, nx, yy, ny) &&
+                     same_as(c.gk, nx + ny, A, N) && same_as(c.gk, nx + ny + N, B, N) &&
+                     same_as(c.gk, nx + ny + 2 * N, C, N);
+  const bool vsame = gsame && c.v_ok && (V ? (!c.v_null && same_as(c.vk, 0, V, N)) : c.v_null);
+  if (!gsame || (need_v && !vsame)) {
+    if (!gsame) {
+      c.grid_ok = c.v_ok = false;
+      int e = h2d(c, c.pb.xdeg.p, xx, nx) | h2d(c, c.pb.ydeg.p, yy, ny) |
+              h2d(c, c.pb.A.p, A, N) | h2d(c, c.pb.B.p, B, N) | h2d(c, c.pb.C.p, C, N);
+      if (e) return SURFATT_CUDA_ERROR;
+      c.gk.resize(nx + ny + 3 * N);
+      std::memcpy(c.gk.data(), xx, nx * sizeof(double));
+      std::memcpy(c.gk.data() + nx, yy, ny * sizeof(double));
+      std::memcpy(c.gk.data() + nx + ny, A, N * sizeof(double));
+      std::memcpy(c.gk.data() + nx + ny + N, B, N * sizeof(double));
+      std::memcpy(c.gk.data() + nx + ny + 2 * N, C, N * sizeof(double));
+      c.gk_nx = nx;
+      c.gk_ny = ny;
+      c.gk_flags = flags;
+    }
+    if (V) {
+      if (h2d(c, c.pb.V.p, V, N)) return SURFATT_CUDA_ERROR;
+      c.vk.assign(V, V + N);
+    } else {
+      CK(cudaMemsetAsync(c.pb.V.p, 0, N * sizeof(double), c.st));
+      c.vk.clear();
+    }
+    c.v_null = V == nullptr;
+    PrepIn in{nx, ny, lonlat, c.pb.xdeg.as<double>(), c.pb.ydeg.as<double>(), c.pb.A.as<double>(),
+              c.pb.B.as<double>(), c.pb.C.as<double>(), c.pb.V.as<double>(), from_model};
+    launch_prep(in, c.pb.out(), c.st);
+    CK(cudaGetLastError());
+    c.grid_ok = c.v_ok = true;
+  }
   // dx, dy in sweep units: xx(2)-xx(1) after the same conversion as the device
   double dx, dy;
   if (lonlat) {
@@ -152,10 +240,14 @@ int prep_single(ThreadCtx& c, const double* xx, const double* yy, int nx, int ny
   return SURFATT_OK;
 }
 
-int finish_single(ThreadCtx& c, double* out_host, size_t n, const DBuf& out_dev) {
+// Status + iterations back (and n doubles of out_dev into staging, returned
+// in *staged), then wait for the stream.
+int finish_single(ThreadCtx& c, const DBuf& out_dev, size_t n, double** staged) {
   CK(cudaMemcpyAsync(c.si_host, c.si.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.st));
-  if (out_host)
-    CK(cudaMemcpyAsync(out_host, out_dev.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  if (staged) {
+    *staged = c.stage(nullptr, n);
+    CK(cudaMemcpyAsync(*staged, out_dev.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+  }
   CK(cudaStreamSynchronize(c.st));
   return SURFATT_OK;
 }
@@ -176,22 +268,25 @@ int uw_dropin(const double* xx, const double* yy, int nx, int ny, const double* 
     return record(SURFATT_BAD_ARG, 0);
   ThreadCtx& c = g_ctx;
   int e = c.setup();
+  if (!e) e = c.stage_begin(stage_doubles(nx, ny, 0));
   if (e) return record(e, 0);
   PeriodDev P;
   e = prep_single(c, xx, yy, nx, ny, A, B, C, fun, lonlat, 0, &P);
   if (e) return record(e, 0);
   const size_t N = (size_t)nx * ny;
-  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.out.ensure(N * sizeof(double)) ||
+  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.T.ensure(N * sizeof(double)) ||
       c.si.ensure(4 * sizeof(int)))
     return record(SURFATT_OOM, 0);
   const double xs0 = lonlat ? x0 / 180.0 * PI_S : x0;
   const double ys0 = lonlat ? y0 / 180.0 * PI_S : y0;
+  c.t_ok = false;  // T is rewritten
   if (weno)
-    launch_weno_single(P, xs0, ys0, multi, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+    launch_weno_single(P, xs0, ys0, multi, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
   else
-    launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+    launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
   if (cudaGetLastError() != cudaSuccess) return record(SURFATT_CUDA_ERROR, 0);
-  e = finish_single(c, nullptr, 0, c.out);
+  double* staged = nullptr;
+  e = finish_single(c, c.T, N, &staged);
   if (e) return record(e, 0);
   const int st = c.si_host[0], it = c.si_host[1];
   if (st == SURFATT_SOURCE_ON_BOUNDARY) {
@@ -199,8 +294,9 @@ int uw_dropin(const double* xx, const double* yy, int nx, int ny, const double* 
     return record(st, 0);
   }
   if (st == SURFATT_OK || st == SURFATT_NOT_CONVERGED) {
-    if (cudaMemcpy(T, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
-      return record(SURFATT_CUDA_ERROR, 0);
+    std::memcpy(T, staged, N * sizeof(double));
+    c.tk.assign(staged, staged + N);
+    c.t_ok = true;
   }
   return record(st, it);
 }
@@ -213,9 +309,10 @@ int jse_dropin(const double* xx, const double* yy, int nx, int ny, const double*
     return record(SURFATT_BAD_ARG, 0);
   ThreadCtx& c = g_ctx;
   int e = c.setup();
+  if (!e) e = c.stage_begin(stage_doubles(nx, ny, nr));
   if (e) return record(e, 0);
   PeriodDev P;
-  e = prep_single(c, xx, yy, nx, ny, A, B, C, nullptr, lonlat, 0, &P);
+  e = prep_single(c, xx, yy, nx, ny, A, B, C, nullptr, lonlat, 0, &P, false);
   if (e) return record(e, 0);
   const size_t N = (size_t)nx * ny;
   const size_t R = (size_t)(nr > 0 ? nr : 1) * sizeof(double);
@@ -223,20 +320,27 @@ int jse_dropin(const double* xx, const double* yy, int nx, int ny, const double*
       c.out.ensure(N * sizeof(double)) || c.rx.ensure(R) || c.ry.ensure(R) || c.sa.ensure(R) ||
       c.si.ensure(4 * sizeof(int)))
     return record(SURFATT_OOM, 0);
-  if (cudaMemcpyAsync(c.T.p, T, N * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
-      (nr > 0 && (cudaMemcpyAsync(c.rx.p, xr, nr * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
-                  cudaMemcpyAsync(c.ry.p, yr, nr * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
-                  cudaMemcpyAsync(c.sa.p, sadj, nr * sizeof(double), cudaMemcpyHostToDevice, c.st))))
+  if (!(c.t_ok && c.tk.size() == N && same_as(c.tk, 0, T, N))) {
+    c.t_ok = false;
+    if (h2d(c, c.T.p, T, N)) return record(SURFATT_CUDA_ERROR, 0);
+    c.tk.assign(T, T + N);
+    c.t_ok = true;
+  }
+  if (nr > 0 && (h2d(c, c.rx.p, xr, nr) || h2d(c, c.ry.p, yr, nr) || h2d(c, c.sa.p, sadj, nr)))
     return record(SURFATT_CUDA_ERROR, 0);
+  c.out_ok = false;  // out is rewritten
   launch_jse_single(P, c.T.as<double>(), c.rx.as<double>(), c.ry.as<double>(), c.sa.as<double>(),
                     nr, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
   if (cudaGetLastError() != cudaSuccess) return record(SURFATT_CUDA_ERROR, 0);
-  e = finish_single(c, nullptr, 0, c.out);
+  double* staged = nullptr;
+  e = finish_single(c, c.out, N, &staged);
   if (e) return record(e, 0);
   const int st = c.si_host[0], it = c.si_host[1];
-  if (st == SURFATT_OK || st == SURFATT_NOT_CONVERGED)
-    if (cudaMemcpy(Ta, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
-      return record(SURFATT_CUDA_ERROR, 0);
+  if (st == SURFATT_OK || st == SURFATT_NOT_CONVERGED) {
+    std::memcpy(Ta, staged, N * sizeof(double));
+    c.ok.assign(staged, staged + N);
+    c.out_ok = true;
+  }
   return record(st, it);
 }
 
@@ -245,19 +349,34 @@ int mask_dropin(const double* xx, const double* yy, int nx, int ny, double* tab,
   if (!xx || !yy || !tab || nx < 2 || ny < 2) return record(SURFATT_BAD_ARG, 0);
   ThreadCtx& c = g_ctx;
   int e = c.setup();
+  if (!e) e = c.stage_begin(stage_doubles(nx, ny, 0));
   if (e) return record(e, 0);
   const size_t N = (size_t)nx * ny;
+  const void* before = c.pb.A.p;
   if (c.pb.ensure(nx, ny) || c.out.ensure(N * sizeof(double))) return record(SURFATT_OOM, 0);
-  if (cudaMemcpyAsync(c.pb.xdeg.p, xx, nx * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
-      cudaMemcpyAsync(c.pb.ydeg.p, yy, ny * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
-      cudaMemcpyAsync(c.out.p, tab, N * sizeof(double), cudaMemcpyHostToDevice, c.st))
-    return record(SURFATT_CUDA_ERROR, 0);
+  if (c.pb.A.p != before) c.grid_ok = c.v_ok = false;
+  // the node coordinates: those of the grid on the device when they match
+  if (!(c.grid_ok && c.gk_nx == nx && c.gk_ny == ny && same_as(c.gk, 0, xx, nx) &&
+        same_as(c.gk, nx, yy, ny))) {
+    c.grid_ok = c.v_ok = false;  // the device's axes change
+    if (h2d(c, c.pb.xdeg.p, xx, nx) || h2d(c, c.pb.ydeg.p, yy, ny))
+      return record(SURFATT_CUDA_ERROR, 0);
+  }
+  if (!(c.out_ok && c.ok.size() == N && same_as(c.ok, 0, tab, N))) {
+    c.out_ok = false;
+    if (h2d(c, c.out.p, tab, N)) return record(SURFATT_CUDA_ERROR, 0);
+  }
+  c.out_ok = false;
   PeriodDev P = c.pb.dev(nx, ny, 0, 0, 0, nullptr);
   launch_mask_single(P, c.out.as<double>(), x0, y0, c.st);
+  double* staged = c.stage(nullptr, N);
   if (cudaGetLastError() != cudaSuccess ||
-      cudaMemcpyAsync(tab, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
+      cudaMemcpyAsync(staged, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
       cudaStreamSynchronize(c.st))
     return record(SURFATT_CUDA_ERROR, 0);
+  std::memcpy(tab, staged, N * sizeof(double));
+  c.ok.assign(staged, staged + N);
+  c.out_ok = true;
   return record(SURFATT_OK, 0);
 }
 
@@ -341,32 +460,39 @@ surfatt_status_t surfatt_measadj_run_forward(const double* xgrids, const double*
     return (surfatt_status_t)record(SURFATT_BAD_ARG, 0);
   ThreadCtx& c = g_ctx;
   int e = c.setup();
+  if (!e) e = c.stage_begin(stage_doubles(nx, ny, nrec));
   if (e) return (surfatt_status_t)record(e, 0);
   PeriodDev P;
   e = prep_single(c, xgrids, ygrids, nx, ny, m11, m22, m12, vel2d, 1, 1, &P);
   if (e) return (surfatt_status_t)record(e, 0);
   const size_t N = (size_t)nx * ny;
   const size_t R = (size_t)(nrec > 0 ? nrec : 1) * sizeof(double);
-  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.out.ensure(N * sizeof(double)) ||
+  if (c.ws.ensure(single_ws_doubles(N) * sizeof(double)) || c.T.ensure(N * sizeof(double)) ||
       c.si.ensure(4 * sizeof(int)) || c.rx.ensure(R) || c.ry.ensure(R) || c.sa.ensure(R))
     return (surfatt_status_t)record(SURFATT_OOM, 0);
   const double xs0 = srcx / 180.0 * PI_S, ys0 = srcy / 180.0 * PI_S;
-  launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.out.as<double>(), c.si.as<int>(), c.st);
+  c.t_ok = false;  // T is rewritten
+  launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
   if (cudaMemsetAsync(c.si.as<int>() + 2, 0, sizeof(int), c.st) != cudaSuccess)
     return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
   if (nrec > 0) {
-    if (cudaMemcpyAsync(c.rx.p, recx, nrec * sizeof(double), cudaMemcpyHostToDevice, c.st) ||
-        cudaMemcpyAsync(c.ry.p, recy, nrec * sizeof(double), cudaMemcpyHostToDevice, c.st))
+    if (h2d(c, c.rx.p, recx, nrec) || h2d(c, c.ry.p, recy, nrec))
       return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
-    launch_interp(P, c.out.as<double>(), nrec, c.rx.as<double>(), c.ry.as<double>(),
+    launch_interp(P, c.T.as<double>(), nrec, c.rx.as<double>(), c.ry.as<double>(),
                   c.sa.as<double>(), c.si.as<int>() + 2, c.st);
   }
   if (cudaGetLastError() != cudaSuccess) return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
+  double* st_T = c.stage(nullptr, N);
+  double* st_k = c.stage(nullptr, nrec > 0 ? nrec : 0);
   if (cudaMemcpyAsync(c.si_host, c.si.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, c.st) ||
-      cudaMemcpyAsync(timetable, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
-      (nrec > 0 && cudaMemcpyAsync(tekio, c.sa.p, nrec * sizeof(double), cudaMemcpyDeviceToHost, c.st)) ||
+      cudaMemcpyAsync(st_T, c.T.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
+      (nrec > 0 && cudaMemcpyAsync(st_k, c.sa.p, nrec * sizeof(double), cudaMemcpyDeviceToHost, c.st)) ||
       cudaStreamSynchronize(c.st))
     return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
+  std::memcpy(timetable, st_T, N * sizeof(double));
+  if (nrec > 0) std::memcpy(tekio, st_k, nrec * sizeof(double));
+  c.tk.assign(st_T, st_T + N);
+  c.t_ok = true;
   int st = c.si_host[0];
   if (st == SURFATT_SOURCE_ON_BOUNDARY) return (surfatt_status_t)record(st, 0);
   if (nrec > 0 && c.si_host[2] != 0 && st == SURFATT_OK) st = SURFATT_BAD_ARG;
