@@ -1082,7 +1082,9 @@ def run_dropin(args):
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": s_many * 1e3,
                     "host_buffers": "pageable (the caller's arrays), copied through "
                                     "per-thread pinned staging"},
-            "gpu_launches": 5 * len(srcs) * args.steps,
+            # per source: forward, adjoint and mask kernels (the grid's
+            # precompute runs only when a thread's model changes)
+            "gpu_launches": 3 * len(srcs) * args.steps,
             "roofline": {"bound": "fp64", "bound_note": "one 256-thread block per call (one "
                          "SM); achieved = reference-formulation FP64 flops of the timed calls "
                          "over wall time, copies included",
