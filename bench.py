@@ -37,7 +37,7 @@ sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
 # this workload by `python oracle/count_flops.py config2 32`.
 FWD_FLOPS_PER_VISIT = 351.8
 ADJ_FLOPS_PER_VISIT = 16.0
-KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w", 3: "k_batch_fp32d"}
+KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w"}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # FP32 row kernel (k_batch_fp32w), from one ncu capture of the 320-solve case
 # (1.670 GB read + 0.641 GB written), scaled by the solves for the 1280-solve

@@ -442,22 +442,21 @@ surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* engine, int* gri
                                               int* blocks_per_sm, size_t* smem_bytes);
 
 /* Time every solve-kernel variant that applies to the loaded problem (plain
- * FP64: one; FP32: the row-per-lane kernel's variants -- 0 / 1: every
- * operand loaded a step ahead, 8 resident warps per SM, solves cut into work
- * items / whole; 2 / 3: cell constants loaded at the visit, 12 / 8 warps,
- * items / whole -- the diagonal-layout kernel's variants and the
+ * FP64: 0 solves cut into work items, 1 whole solves; FP32: the
+ * row-per-lane kernel's variants -- 0 / 1: cell constants loaded a step
+ * ahead, 8 resident warps per SM, solves cut into work items / whole; 2 / 3:
+ * cell constants loaded at the visit, 12 / 8 warps, items / whole -- and the
  * block-per-solve kernel) with one warm-up and one timed evaluation each,
  * and use the fastest for later runs of this precision until the next load.
- * Returns the chosen kernel (0 FP64, 1 FP32 block, 2 / 3 FP32 warp), its variant
+ * Returns the chosen kernel (0 FP64, 1 FP32 block, 2 FP32 warp), its variant
  * and its solve-kernel time. */
 surfatt_status_t surfatt_engine_autotune(surfatt_engine_t* engine, surfatt_mode_t mode,
                                          surfatt_precision_t precision, int* kind, int* variant,
                                          double* best_ms);
 /* Choose the solve kernel of later runs at `precision` by hand (as
- * surfatt_engine_autotune would): kind (0 FP64, 1 FP32 block, 2 FP32 warp
- * on row-major arrays, 3 FP32 warp on the diagonal layouts) and warp-kernel
- * variant (0..3); -1 leaves a field automatic.  A kernel that
- * does not apply to the loaded grids makes the next run return
+ * surfatt_engine_autotune would): kind (0 FP64, 1 FP32 block, 2 FP32 warp)
+ * and variant (as above); -1 leaves a field automatic.  A kernel that does
+ * not apply to the loaded grids makes the next run return
  * SURFATT_BAD_ARG. */
 surfatt_status_t surfatt_engine_set_kernel(surfatt_engine_t* engine, surfatt_precision_t precision,
                                           int kind, int variant);
@@ -465,9 +464,7 @@ surfatt_status_t surfatt_engine_set_kernel(surfatt_engine_t* engine, surfatt_pre
  * on, every run sums clock64() intervals per solve phase over all solves:
  * [0] source cell + T0, [1] forward sweeps, [2] receiver times + misfit,
  * [3] adjoint coefficients + sources, [4] adjoint sweeps, [5] mask + kernel
- * slot, and [6] the part of [1] and [4] spent waiting for staged operands
- * (diagonal-layout kernel); surfatt_engine_phase_cycles copies the seven sums
- * of the last run. */
+ * slot; surfatt_engine_phase_cycles copies the six sums of the last run. */
 surfatt_status_t surfatt_engine_set_profile(surfatt_engine_t* engine, int enable);
 surfatt_status_t surfatt_engine_phase_cycles(surfatt_engine_t* engine, double* cycles);
 /* Kernel and variant used by the last run. */

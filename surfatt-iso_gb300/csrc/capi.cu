@@ -80,8 +80,6 @@ struct PeriodBufs {
     P.isv = nullptr;
     P.p4a = nullptr;
     P.p4b = nullptr;
-    P.qa[0] = P.qa[1] = nullptr;
-    P.qd[0] = P.qd[1] = nullptr;
     return P;
   }
 };
@@ -629,13 +627,12 @@ struct surfatt_engine {
   std::vector<PeriodDev> periods;
   std::vector<int> order, plist_off, plist;
   std::vector<long long> kslot;
-  std::vector<long long> qoff;  // per period: offset of its diagonal-layout records (-1: none)
   // device buffers
   DBuf d_periods, d_xdeg, d_ydeg, d_xs, d_ys, d_cosy, d_siny, d_A, d_B, d_C, d_V, d_a, d_b, d_c,
       d_fun, d_f2, d_disx, d_disy, d_f32, d_isv, d_p4a, d_p4b, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
       d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
   DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
-      d_fupd, d_aupd, d_ws, d_queue, d_phase, d_q;
+      d_fupd, d_aupd, d_ws, d_queue, d_phase;
   // kernel smoothing of adj_s (gaussian_smooth_geo_2 per period)
   DBuf d_ker, d_smtab, d_smnyw, d_smper;
   std::vector<double> hx, hy;  // host copies of the grid axes (window plan)
@@ -677,7 +674,7 @@ struct surfatt_engine {
             &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
             &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
             &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
-            &d_aupd, &d_ws, &d_queue, &d_phase, &d_q, &d_ker, &d_smtab, &d_smnyw, &d_smper,
+            &d_aupd, &d_ws, &d_queue, &d_phase, &d_ker, &d_smtab, &d_smnyw, &d_smper,
             &d_T};
   }
 };
@@ -714,9 +711,6 @@ int run_prep_all(surfatt_engine* e) {
                 e->d_f32.as<float>() + 6 * g, e->d_isv.as<double>() + 2 * g,
                 e->d_p4a.as<float4>() + g, e->d_p4b.as<float4>() + g};
     launch_prep(in, out, e->st);
-    if (e->qoff[p] >= 0)
-      launch_prep_diag(e->nx[p], e->ny[p], e->d_p4a.as<float4>() + g, e->d_p4b.as<float4>() + g,
-                       e->d_q.as<float4>() + e->qoff[p], e->st);
   }
   CK(cudaGetLastError());
   return SURFATT_OK;
@@ -846,20 +840,6 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
     r |= up(e, *b, (double*)nullptr, NC);
   r |= up(e, e->d_f32, (float*)nullptr, 6 * NC) | up(e, e->d_isv, (double*)nullptr, 2 * NC);
   r |= up(e, e->d_p4a, (float4*)nullptr, NC) | up(e, e->d_p4b, (float4*)nullptr, NC);
-  // diagonal-layout records, when every grid fits the warp-per-solve kernels
-  e->qoff.assign(np, -1);
-  {
-    bool fits = true;
-    for (int p = 0; p < np; ++p)
-      fits = fits && e->ny[p] <= kWarpMaxRows && e->nx[p] <= kWarpMaxCols;
-    long long qn = 0;
-    if (fits)
-      for (int p = 0; p < np; ++p) {
-        e->qoff[p] = qn;
-        qn += diag_qrecords(e->nx[p], e->ny[p]);
-      }
-    r |= up(e, e->d_q, (float4*)nullptr, (size_t)qn);
-  }
   r |= up(e, e->d_pidx, pb->pidx, ns) | up(e, e->d_srcx, pb->srcx, ns) |
        up(e, e->d_srcy, pb->srcy, ns) | up(e, e->d_rec_off, pb->rec_off, ns) |
        up(e, e->d_nrec, pb->nrec, ns);
@@ -913,12 +893,6 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
     P.isv = e->d_isv.as<double>() + 2 * g;
     P.p4a = e->d_p4a.as<float4>() + g;
     P.p4b = e->d_p4b.as<float4>() + g;
-    if (e->qoff[p] >= 0) {
-      diag_q_arrays(e->d_q.as<float4>() + e->qoff[p], P.nx, P.ny, P.qa, P.qd);
-    } else {
-      P.qa[0] = P.qa[1] = nullptr;
-    P.qd[0] = P.qd[1] = nullptr;
-    }
   }
   r = up(e, e->d_periods, e->periods.data(), np);
   if (r) return (surfatt_status_t)r;
@@ -1085,8 +1059,7 @@ surfatt_status_t surfatt_engine_set_kernel(surfatt_engine_t* e, surfatt_precisio
   if (prec != SURFATT_PREC_FP64 && prec != SURFATT_PREC_FP32) return SURFATT_BAD_ARG;
   const int p = prec == SURFATT_PREC_FP64 ? 0 : 1;
   if (p == 0 && kind != -1 && kind != KK_FP64) return SURFATT_BAD_ARG;
-  if (p == 1 && kind != -1 && kind != KK_FP32_BLOCK && kind != KK_FP32_WARP &&
-      kind != KK_FP32_DIAG)
+  if (p == 1 && kind != -1 && kind != KK_FP32_BLOCK && kind != KK_FP32_WARP)
     return SURFATT_BAD_ARG;
   if (variant < -1 || variant >= fp32w_variant_count()) return SURFATT_BAD_ARG;
   e->tuned[p] = KernelChoice{kind, variant};

@@ -61,24 +61,7 @@ struct PeriodDev {
   // per-cell FP32 records: {a, b, c, fun**2} and {disx, disy, 1/svel**2, 1/svel**3}
   const float4* p4a;
   const float4* p4b;
-  // in the diagonal layouts (null when not prepared), at diag_index(f, i, j):
-  // qa[f] = {a, b, c, fun**2}, qd[f] = {disx, disy}
-  const float4* qa[2];
-  const float2* qd[2];
 };
-
-// Diagonal layouts of an nx x ny grid (the FP32 diagonal-layout kernel).
-// Family 0 holds node (i, j) on diagonal d = i + j, family 1 on
-// d = i - j + ny - 1; it is stored at (d + 1) * pitch + j with the pitch ny
-// rounded up to 32, so that every diagonal is contiguous and 128-byte
-// aligned for 4-byte elements, with one padding diagonal at either end.
-__host__ __device__ inline int diag_pitch(int ny) { return (ny + 31) & ~31; }
-__host__ __device__ inline long long diag_cells(int nx, int ny) {
-  return (long long)(nx + ny + 1) * diag_pitch(ny);
-}
-__host__ __device__ inline int diag_index(int fam, int i, int j, int ny, int pitch) {
-  return ((fam == 0 ? i + j : i - j + ny - 1) + 1) * pitch + j;
-}
 
 // Source/receiver cell and REAL(4) bilinear weights:
 //   idx0 = floor((x0-xx(1))/dx+1);  r1 = min(1.0,(x0-xx(idx0))/dx)   (:828-829)

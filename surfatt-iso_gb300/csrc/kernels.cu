@@ -92,32 +92,6 @@ void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st) {
   k_prep<<<grid, 256, 0, st>>>(in, out);
 }
 
-__global__ void k_prep_diag(int nx, int ny, const float4* p4a, const float4* p4b, float4* q) {
-  const int pitch = diag_pitch(ny);
-  const long long D = diag_cells(nx, ny);
-  const size_t N = (size_t)nx * ny;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < N;
-       k += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(k % nx), j = (int)(k / nx);
-    const int a = diag_index(0, i, j, ny, pitch), b = diag_index(1, i, j, ny, pitch);
-    const float4 va = p4a[k], vb = p4b[k];
-    float2* qd = reinterpret_cast<float2*>(q + 2 * D);
-    q[a] = va;
-    q[D + b] = va;
-    qd[a] = make_float2(vb.x, vb.y);
-    qd[D + b] = make_float2(vb.x, vb.y);
-  }
-}
-
-void launch_prep_diag(int nx, int ny, const float4* p4a, const float4* p4b, float4* q,
-                      cudaStream_t st) {
-  const long long D = diag_cells(nx, ny);
-  cudaMemsetAsync(q, 0, 3 * (size_t)D * sizeof(float4), st);
-  const size_t N = (size_t)nx * ny;
-  const int grid = (int)std::min<size_t>((N + 255) / 256, 1024);
-  k_prep_diag<<<grid, 256, 0, st>>>(nx, ny, p4a, p4b, q);
-}
-
 // ---------------------------------------------------------------------------
 // Fused batched solve (FP64).  Persistent blocks pull solves from a device
 // work queue; each runs forward -> interp2 -> misfit -> adjoint(s) -> mask

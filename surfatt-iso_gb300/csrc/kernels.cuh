@@ -89,27 +89,12 @@ enum SolvePhase {
   PH_ADJ_SETUP = 3, // adjoint coefficients and sources
   PH_ADJ = 4,       // adjoint sweeps
   PH_SLOT = 5,      // mask and kernel slot
-  PH_WAIT = 6,      // of PH_FWD and PH_ADJ: waits for staged operands (diagonal kernel)
-  PH_COUNT = 7
+  PH_COUNT = 6
 };
 
 void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st);
-// Records of one period in the two diagonal layouts: q holds
-// diag_qrecords(nx, ny) float4 = qa[0], qa[1] (D float4 each) then qd[0],
-// qd[1] (D float2 each), D = diag_cells(nx, ny); padding zeroed.
-void launch_prep_diag(int nx, int ny, const float4* p4a, const float4* p4b, float4* q,
-                      cudaStream_t st);
-inline long long diag_qrecords(int nx, int ny) { return 3 * diag_cells(nx, ny); }
-// Pointers of the four arrays inside q.
-inline void diag_q_arrays(float4* q, int nx, int ny, const float4** qa, const float2** qd) {
-  const long long D = diag_cells(nx, ny);
-  qa[0] = q;
-  qa[1] = q + D;
-  qd[0] = reinterpret_cast<const float2*>(q + 2 * D);
-  qd[1] = qd[0] + D;
-}
-// Largest grid the diagonal-layout kernel and the single-warp form of the
-// row kernel take; the row kernel's warp teams take up to kTeamMaxRows.
+// Largest grid the single-warp form of the row kernel takes; its warp
+// teams take up to kTeamMaxRows.
 constexpr int kWarpMaxRows = 128;
 constexpr int kWarpMaxCols = 4096;
 constexpr int kTeamMaxRows = 512;
@@ -171,12 +156,6 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 // last runs the forward sweeps to convergence and the rest of the solve.
 constexpr int kFp64Items = 3;
 constexpr int kFp64SplitIter = 2;
-// The same solve on the diagonal layouts (PeriodDev::qa / qd prepared), its
-// operands staged in shared memory; `variant` < fp32d_variant_count().
-void launch_batch_fp32d(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st);
-int batch_fp32d_max_blocks_per_sm(int bands, int variant);
-int fp32d_variant_count();
-long long batch_fp32d_ws_doubles(long long max_dcells, int max_nx);
 long long batch_fp32w_ws_doubles(long long N);
 int fp32w_bands(int max_ny);
 // chi = sum of per-solve misfits in work-list order (src/acqui.f90:135)

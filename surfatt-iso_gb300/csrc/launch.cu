@@ -13,7 +13,7 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
   nperiod = np;
   nsolve = ns;
   npath = npth;
-  ncell = max_cells = max_pitched = max_dcells = 0;
+  ncell = max_cells = max_pitched = 0;
   max_nx = max_ny = max_diag = 0;
   for (int p = 0; p < np; ++p) {
     const long long N = (long long)nxs[p] * nys[p];
@@ -23,7 +23,6 @@ void EvalShape::from_grids(const int* nxs, const int* nys, const long long* goff
     max_ny = std::max(max_ny, nys[p]);
     max_diag = std::max(max_diag, std::min(nxs[p], nys[p]));
     max_pitched = std::max(max_pitched, (long long)batch_fp32_pitch(nxs[p]) * nys[p]);
-    max_dcells = std::max(max_dcells, diag_cells(nxs[p], nys[p]));
   }
   for (int c = 0; c < kTeamClasses; ++c) team_count[c] = team_max_ny[c] = 0;
   solve_cells = 0;
@@ -44,8 +43,6 @@ std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
     c.push_back({KK_FP64, 1});  // whole solves
     return c;
   }
-  if (sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)
-    for (int v = 0; v < fp32d_variant_count(); ++v) c.push_back({KK_FP32_DIAG, v});
   if (sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols)
     for (int v = 0; v < fp32w_variant_count(); ++v) c.push_back({KK_FP32_WARP, v});
   if (sh.max_diag <= kFp32MaxThreads) c.push_back({KK_FP32_BLOCK, 0});
@@ -69,30 +66,21 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.cut = p.pf == 0 && sh.solve_cells > 0;
     if (!p.cut) p.pf = 1;
     p.solve_doubles = p.cut ? sh.solve_cells : 0;
-  } else if ((force.kind == KK_FP32_DIAG &&
-              !(sh.max_ny <= kWarpMaxRows && sh.max_nx <= kWarpMaxCols)) ||
-             (force.kind == KK_FP32_WARP &&
-              !(sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols))) {
-    return ST_BAD_ARG;  // the diagonal kernel holds 128 rows, the row kernel 512
+  } else if (force.kind == KK_FP32_WARP &&
+             !(sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols)) {
+    return ST_BAD_ARG;  // the row kernel holds 512 rows
   } else if (force.kind != KK_FP32_BLOCK && sh.max_ny <= kTeamMaxRows &&
-             sh.max_nx <= kWarpMaxCols &&
-             (force.kind != KK_FP32_DIAG || sh.max_ny <= kWarpMaxRows)) {
+             sh.max_nx <= kWarpMaxCols) {
     // one warp (a team of warps above 128 rows) per solve, lanes own the rows
     // automatic: the row-per-lane kernel (the faster on the measured shapes)
-    p.kind = force.kind == KK_FP32_DIAG ? KK_FP32_DIAG : KK_FP32_WARP;
-    p.block = p.kind == KK_FP32_WARP ? 32 * fp32w_team(sh.max_ny) : 32;
+    p.kind = KK_FP32_WARP;
+    p.block = 32 * fp32w_team(sh.max_ny);
     p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
-    const int nvar = p.kind == KK_FP32_WARP ? fp32w_variant_count() : fp32d_variant_count();
-    p.pf = force.variant >= 0 && force.variant < nvar ? force.variant : 0;
-    if (p.kind == KK_FP32_WARP) {
-      p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
-      p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
-      p.cut = fp32w_variant_items(p.pf);
-    } else {
-      p.per_sm = batch_fp32d_max_blocks_per_sm(p.bands, p.pf);
-      p.ws_doubles = batch_fp32d_ws_doubles(sh.max_dcells, sh.max_nx);
-    }
+    p.pf = force.variant >= 0 && force.variant < fp32w_variant_count() ? force.variant : 0;
+    p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
+    p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
+    p.cut = fp32w_variant_items(p.pf);
   } else {
     // one block per solve, one thread per cell of the longest anti-diagonal
     if (sh.max_diag > kFp32MaxThreads) return ST_BAD_ARG;
@@ -263,7 +251,6 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
     if (plan.kind == KK_FP64) launch_batch_fp64(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_BLOCK) launch_batch_fp32(A, plan.grid, plan.block, st);
     else if (plan.kind == KK_FP32_WARP) launch_batch_fp32w(A, plan.grid, plan.bands, plan.pf, st);
-    else launch_batch_fp32d(A, plan.grid, plan.bands, plan.pf, st);
     ++launches;
   }
   if (ev_k1) cudaEventRecordWithFlags(ev_k1, st, ev_flags);
@@ -272,7 +259,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
     for (int f = 0; f < nf; ++f) {
       double* kc = f == 0 ? A.kcontrib : A.kcontrib_den;
       double* out = f == 0 ? dev.adj_s : dev.adj_density;
-      if (plan.kind == KK_FP32_WARP || plan.kind == KK_FP32_DIAG)
+      if (plan.kind == KK_FP32_WARP)
         launch_kernel_reduce_f32(sh.nperiod, dev.plist_off, dev.plist, A.kslot,
                                  reinterpret_cast<const float*>(kc), out, dev.goff, dev.nx,
                                  dev.ny, st);

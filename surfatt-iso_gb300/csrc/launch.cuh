@@ -20,7 +20,6 @@ struct EvalShape {
   int nperiod = 0, nsolve = 0, npath = 0;
   long long ncell = 0, max_cells = 0, max_pitched = 0;
   int max_nx = 0, max_ny = 0, max_diag = 0;
-  long long max_dcells = 0;  // largest diag_cells over the periods
   long long solve_cells = 0;  // sum over the solves of their grids' cells (with pidx)
   // Solves per team class and the class's tallest grid, counted when
   // from_grids is given the solves' period indices (else all zero: the
@@ -49,9 +48,9 @@ struct EvalDev {
 };
 
 // Solve kernels: plain FP64 (one block per solve), FP32 one block per solve
-// (any grid), FP32 one warp per solve on row-major arrays and on the
-// diagonal layouts (grids of at most 128 rows).
-enum KernelKind { KK_FP64 = 0, KK_FP32_BLOCK = 1, KK_FP32_WARP = 2, KK_FP32_DIAG = 3 };
+// (any grid), FP32 one warp (or a team of warps) per solve, lanes owning
+// the rows (grids of at most 512 rows and 4096 columns).
+enum KernelKind { KK_FP64 = 0, KK_FP32_BLOCK = 1, KK_FP32_WARP = 2 };
 
 // A solve-kernel choice; -1 fields are picked automatically.  `variant`
 // indexes the warp kernel's operand-prefetch / register-cap variants.

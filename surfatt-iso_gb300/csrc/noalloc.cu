@@ -115,8 +115,6 @@ __global__ void __launch_bounds__(256) k_uw_noalloc(const double* xdeg, const do
   P.isv = nullptr;
   P.p4a = nullptr;
   P.p4b = nullptr;
-  P.qa[0] = P.qa[1] = nullptr;
-  P.qd[0] = P.qd[1] = nullptr;
   fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, W, true, sh);
   if (sh.status != ST_OK) {
     if (threadIdx.x == 0) { si[0] = sh.status; si[1] = 0; }

@@ -117,14 +117,13 @@ struct PeriodArrays {
   float* f32;
   double* isv;
   float4 *p4a, *p4b;
-  float4* q;  // diagonal-layout records of every period (Model::qoff), or null
   PeriodDev* periods;
   long long *goff;
   int *nx, *ny;
 };
 
 void carve_periods(Carver& cv, long long nxs, long long nys, long long NC, int np,
-                   long long qcells, PeriodArrays* a) {
+                   PeriodArrays* a) {
   a->xdeg = cv.take<double>(nxs);
   a->ydeg = cv.take<double>(nys);
   a->xs = cv.take<double>(nxs);
@@ -146,7 +145,6 @@ void carve_periods(Carver& cv, long long nxs, long long nys, long long NC, int n
   a->isv = cv.take<double>(2 * NC);
   a->p4a = cv.take<float4>(NC);
   a->p4b = cv.take<float4>(NC);
-  a->q = qcells > 0 ? cv.take<float4>(qcells) : nullptr;
   a->periods = cv.take<PeriodDev>(np);
   a->goff = cv.take<long long>(np);
   a->nx = cv.take<int>(np);
@@ -161,8 +159,6 @@ struct Model {
   std::vector<int> nx, ny;
   std::vector<long long> goff, xoff, yoff;
   std::vector<double> dx, dy;
-  std::vector<long long> qoff;  // per period: diagonal-layout record offset (-1: none)
-  long long qcells = 0;
   PeriodArrays d{};
   int refs = 0;
 };
@@ -244,8 +240,6 @@ int prep_periods(const Model& m, const PeriodArrays& src_axes, const PeriodArray
               out.a + g, out.b + g, out.c + g, out.fun + g, out.f2 + g, out.disx + g, out.disy + g,
               out.f32 + 6 * g, out.isv + 2 * g, out.p4a + g, out.p4b + g};
     launch_prep(in, o, st);
-    if (m.qoff[p] >= 0 && out.q)
-      launch_prep_diag(m.nx[p], m.ny[p], out.p4a + g, out.p4b + g, out.q + m.qoff[p], st);
   }
   return cudaGetLastError() == cudaSuccess ? ST_OK : ST_CUDA_ERROR;
 }
@@ -280,12 +274,6 @@ std::vector<PeriodDev> period_descs(const Model& m, const PeriodArrays& axes,
     P.isv = f.isv + 2 * g;
     P.p4a = f.p4a + g;
     P.p4b = f.p4b + g;
-    if (m.qoff[p] >= 0 && f.q) {
-      diag_q_arrays(f.q + m.qoff[p], P.nx, P.ny, P.qa, P.qd);
-    } else {
-      P.qa[0] = P.qa[1] = nullptr;
-      P.qd[0] = P.qd[1] = nullptr;
-    }
   }
   return out;
 }
@@ -305,7 +293,7 @@ int start_request(surfatt_server* S, Request& r) {
   int e = plan_evaluation(r.shape, r.prec, S->device, 0, &r.plan, choice);
   if (e) return e;
   auto layout = [&](Carver& cv) {
-    if (own_vel) carve_periods(cv, M.nxs, M.nys, M.ncell, M.nperiod, M.qcells, &r.d);
+    if (own_vel) carve_periods(cv, M.nxs, M.nys, M.ncell, M.nperiod, &r.d);
     const int nr = std::max(1, L.nrec_total), ns = std::max(1, L.nsolve);
     r.tekio = cv.take<double>(nr);
     r.wgt = cv.take<double>(nr);
@@ -564,25 +552,13 @@ surfatt_status_t surfatt_server_add_model(surfatt_server_t* S, const surfatt_pro
     m->dx.push_back(xg[1] / 180.0 * PI_S - xg[0] / 180.0 * PI_S);
     m->dy.push_back(yg[1] / 180.0 * PI_S - yg[0] / 180.0 * PI_S);
   }
-  // diagonal-layout records, when every grid fits the warp-per-solve kernels
-  m->qoff.assign(m->nperiod, -1);
-  {
-    bool fits = true;
-    for (int p = 0; p < m->nperiod; ++p)
-      fits = fits && m->ny[p] <= kWarpMaxRows && m->nx[p] <= kWarpMaxCols;
-    if (fits)
-      for (int p = 0; p < m->nperiod; ++p) {
-        m->qoff[p] = m->qcells;
-        m->qcells += diag_qrecords(m->nx[p], m->ny[p]);
-      }
-  }
   Carver sizer;
-  carve_periods(sizer, m->nxs, m->nys, m->ncell, m->nperiod, m->qcells, &m->d);
+  carve_periods(sizer, m->nxs, m->nys, m->ncell, m->nperiod, &m->d);
   m->bytes = sizer.off;
   if (!S->arena.alloc(m->bytes, &m->off)) return SURFATT_OOM;
   Carver cv;
   cv.base = S->arena.ptr(m->off);
-  carve_periods(cv, m->nxs, m->nys, m->ncell, m->nperiod, m->qcells, &m->d);
+  carve_periods(cv, m->nxs, m->nys, m->ncell, m->nperiod, &m->d);
   cudaStream_t st = nullptr;
   int e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess ? ST_OK : ST_CUDA_ERROR;
   const size_t NC = m->ncell;

@@ -824,7 +824,7 @@ class Engine:
         if st != OK:
             raise SurfattError(st, "engine_set_kernel")
 
-    PHASES = ("setup", "forward", "receivers", "adjoint_setup", "adjoint", "slot", "stage_wait")
+    PHASES = ("setup", "forward", "receivers", "adjoint_setup", "adjoint", "slot")
 
     def set_profile(self, enable):
         """Per-phase cycle counters of the FP32 warp kernel (default off)."""

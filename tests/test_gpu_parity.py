@@ -491,7 +491,9 @@ def test_fp32_warp_variants(sg, oracle, variant):
 
 
 def test_forced_kernels_reject_too_tall_grids(sg):
-    """The row kernel takes 512 rows (teams), the diagonal kernel 128."""
+    """The row kernel takes 512 rows (teams); forcing it on a taller grid
+    fails the run, the automatic choice (block kernel) runs; an unknown
+    kernel kind is rejected."""
     pb = W.flat_case(nx=20, ny=520, d=0.01, nsta=3, nperiod=1, mode=2, seed=32)
     eng = sg.Engine(0)
     eng.load(pb)
@@ -501,16 +503,8 @@ def test_forced_kernels_reject_too_tall_grids(sg):
     eng.set_kernel(sg.PREC_FP32)
     eng.run(2, sg.PREC_FP32)
     assert eng.sync() == sg.OK
-    eng.close()
-    pb = W.flat_case(nx=40, ny=140, nsta=3, nperiod=1, mode=2, seed=32)
-    eng = sg.Engine(0)
-    eng.load(pb)
-    eng.set_kernel(sg.PREC_FP32, kind=3)
     with pytest.raises(sg.SurfattError):
-        eng.run(2, sg.PREC_FP32)
-    eng.set_kernel(sg.PREC_FP32)
-    eng.run(2, sg.PREC_FP32)
-    assert eng.sync() == sg.OK
+        eng.set_kernel(sg.PREC_FP32, kind=3)
     eng.close()
 
 
@@ -527,21 +521,21 @@ def _run_kernel(sg, pb, mode, kind, variant):
 
 
 @pytest.mark.parametrize("case", ["square", "mixed", "mode2", "mode0"])
-def test_fp32_diagonal_layout_kernel(sg, oracle, case):
-    """The staged diagonal-layout kernel computes the row-per-lane kernel's
-    values (same visits in the same order, arithmetic without compiler
-    contraction: bitwise) and meets the FP32 tolerances against the oracle,
-    on one grid and on uneven grids of one evaluation."""
+def test_fp32_row_kernel_items_and_whole_solves(sg, oracle, case):
+    """The row kernel with solves cut into work items and with whole solves
+    gives the same bits (same visits in the same order) in every mode, on
+    one grid and on uneven grids of one evaluation, and meets the FP32
+    tolerances against the oracle."""
     if case == "mixed":
         pb = W.config4(nsrc=3, nperiod=4, nmax=120, nmin=36, span_deg=2.0)
         mode = 3
     else:
         mode = {"square": 3, "mode2": 2, "mode0": 0}[case]
         pb = W.flat_case(nx=97, ny=75, nsta=5, nperiod=2, mode=mode, seed=41)
-    st_d, kv_d, d = _run_kernel(sg, pb, mode, 3, 1)
+    st_i, kv_i, d = _run_kernel(sg, pb, mode, 2, 0)
     st_w, kv_w, w = _run_kernel(sg, pb, mode, 2, 1)
-    assert kv_d["kind"] == 3 and kv_w["kind"] == 2
-    assert st_d == st_w
+    assert kv_i == dict(kind=2, variant=0) and kv_w == dict(kind=2, variant=1)
+    assert st_i == st_w
     assert np.array_equal(d["status"], w["status"])
     assert np.array_equal(d["fwd_iters"], w["fwd_iters"])
     assert np.array_equal(d["tt_fwd"], w["tt_fwd"])
@@ -558,17 +552,6 @@ def test_fp32_diagonal_layout_kernel(sg, oracle, case):
             assert rel_max(d["adj_s"][sl], ref["adj_s"][sl]) <= KER_TOL_F32
             if mode == 3:
                 assert rel_max(d["adj_density"][sl], ref["adj_density"][sl]) <= KER_TOL_F32
-
-
-@pytest.mark.parametrize("variant", [0, 2])
-def test_fp32_diagonal_variants(sg, variant):
-    pb = W.flat_case(nx=64, ny=100, nsta=4, nperiod=2, mode=3, seed=42)
-    _, _, base = _run_kernel(sg, pb, 3, 3, 1)
-    st, kv, o = _run_kernel(sg, pb, 3, 3, variant)
-    assert kv == dict(kind=3, variant=variant)
-    assert np.array_equal(o["tt_fwd"], base["tt_fwd"])
-    assert np.array_equal(o["adj_s"], base["adj_s"])
-    assert np.array_equal(o["adj_density"], base["adj_density"])
 
 
 def test_fp64_work_items_equal_whole_solves(sg, oracle):
