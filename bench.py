@@ -38,13 +38,14 @@ sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
 FWD_FLOPS_PER_VISIT = 351.8
 ADJ_FLOPS_PER_VISIT = 16.0
 KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w"}
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# FP32 row kernel (k_batch_fp32w), from one ncu capture of the 320-solve case
-# (1.670 GB read + 0.641 GB written), scaled by the solves for the 1280-solve
-# workload (the per-solve workspace and operands are the same for every
-# solve): profiles/k_batch_fp32w_config2s.md.  Reported only when the
-# autotuner picked that kernel.
-DRAM_BYTES_PER_LAUNCH = {"config2": 9.245e9, "config2s": 2.311e9}
+# DRAM bytes (read + write) per launch of the FP32 row kernel
+# (k_batch_fp32w, variant 0) on the full 1280-solve workload, from one ncu
+# capture of the first launch of this bench command (MemoryWorkloadAnalysis:
+# 1.1585 TB/s x 19.065 ms): profiles/k_batch_fp32w_config3.md.  The
+# per-solve workspaces of the 1216 resident solves (about 1 GB) do not fit
+# in L2, so operands are re-read from DRAM every sweep.  Reported only when
+# the autotuner picked that kernel.
+DRAM_BYTES_PER_LAUNCH = {"config2": 22.09e9}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
 
 
