@@ -135,10 +135,11 @@ __device__ inline SolveLayout carve(double* base, size_t N) {
 // solves: a third of the last round's SMs would idle).  Items 0 ..
 // kFp64Items - 2 run kFp64SplitIter forward iterations; the last runs the
 // sweeps to convergence and the solve's tail (receivers, misfit, adjoints,
-// mask, kernel slot).  Only tau persists between items, in the solve's own
-// array (A.ws_solve at the solve's kernel-slot offset): every item
-// recomputes T0 and the hoisted constants in its block's scratch, to the
-// same bits, so the results equal the whole-solve kernel's.  An item waits,
+// mask, kernel slot).  tau, T0 and the T0 gradient persist between items
+// in the solve's own arrays (A.ws_solve: four planes of solve_cells
+// doubles, the solve at its kernel-slot offset); every later item rebuilds
+// only the hoisted constants in its block's scratch, to the same bits, so
+// the results equal the whole-solve kernel's.  An item waits,
 // bounded, for its solve's previous item (taken earlier by a resident
 // block); running out reports SURFATT_TIMEOUT for the solve.
 __global__ void __launch_bounds__(128) k_batch_fp64(BatchArgs A) {
@@ -186,13 +187,20 @@ __global__ void __launch_bounds__(128) k_batch_fp64(BatchArgs A) {
     if (threadIdx.x == 0) sh.flag = ST_OK;
     SolveLayout L = carve(base, N);
     FwdWs fw = L.fw;
-    if (cut) fw.tau = A.ws_solve + A.kslot[s];
+    double* grad = nullptr;
+    if (cut) {
+      const long long S = A.solve_cells;
+      fw.tau = A.ws_solve + A.kslot[s];
+      fw.T0 = A.ws_solve + S + A.kslot[s];
+      grad = A.ws_solve + 2 * S + A.kslot[s];
+    }
     double x0 = A.srcx[s], y0 = A.srcy[s];
     if (P.lonlat) {
       x0 = x0 / 180.0 * PI_S;
       y0 = y0 / 180.0 * PI_S;
     }
-    fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, fw, true, sh, !cut || item == 0);
+    fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, fw, true, sh, grad, (size_t)A.solve_cells,
+              cut && item > 0);
     if (sh.status != ST_OK) {
       const int st = sh.status;
       __syncthreads();
@@ -226,7 +234,7 @@ __global__ void __launch_bounds__(128) k_batch_fp64(BatchArgs A) {
       __syncthreads();
       continue;
     }
-    for (size_t k = threadIdx.x; k < N; k += blockDim.x) L.T[k] = fw.tau[k] * L.fw.T0[k];
+    for (size_t k = threadIdx.x; k < N; k += blockDim.x) L.T[k] = fw.tau[k] * fw.T0[k];
     if (A.fwd_updates && threadIdx.x == 0) {
       const Box b = sh.box;
       const double frozen = (double)(b.i1 - b.i0 + 1) * (b.j1 - b.j0 + 1);

@@ -63,7 +63,8 @@ struct BatchArgs {
   // workspace
   double* ws;              // slots of ws_doubles each
   long long ws_doubles;
-  double* ws_solve = nullptr;  // FP64 kernel with items: per-solve tau, at kslot[s]
+  double* ws_solve = nullptr;  // FP64 kernel with items: per-solve tau, T0, T0x, T0y planes
+  long long solve_cells = 0;   // cells of one plane (the solves' kslot total)
   int* queue;              // work counter (zeroed before launch)
   int block;               // threads per block (for info)
   int max_nx;              // largest nx over periods (shared-memory column arrays)

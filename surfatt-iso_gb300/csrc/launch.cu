@@ -65,7 +65,7 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.pf = force.variant == 1 ? 1 : 0;
     p.cut = p.pf == 0 && sh.solve_cells > 0;
     if (!p.cut) p.pf = 1;
-    p.solve_doubles = p.cut ? sh.solve_cells : 0;
+    p.solve_doubles = p.cut ? 4 * sh.solve_cells : 0;  // tau, T0, T0x, T0y per solve
   } else if (force.kind == KK_FP32_WARP &&
              !(sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols)) {
     return ST_BAD_ARG;  // the row kernel holds 512 rows
@@ -200,6 +200,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
     const long long n = std::max(1, sh.nsolve);
     A.items = kFp64Items;
     A.ws_solve = ws + (long long)plan.grid * plan.ws_doubles;
+    A.solve_cells = plan.solve_doubles / 4;
     A.sstate = reinterpret_cast<int*>(A.ws_solve + plan.solve_doubles);
     if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
       return -ST_CUDA_ERROR;

@@ -70,12 +70,15 @@ struct SolveShared {
 // lon/lat: :801-872 (T0 = great-circle distance * fun0).  Cartesian UW:
 // :47-90.  (x0, y0) in sweep units.  Returns status via sh.status.
 // ---------------------------------------------------------------------------
-// init_tau = false leaves tau alone (a solve resumed from a previous work
-// item: only T0 and the hoisted constants, which are recomputed to the same
-// bits, are written).
+// Work items (the batched kernel cutting a solve into items): `grad`, when
+// given, holds the solve's T0 gradient (T0x at [k], T0y at [gstride + k]).
+// resume = false: T0 and tau are initialised and the gradient stored there;
+// resume = true: T0 (W.T0) and the gradient are read back, tau is left
+// alone, and only the hoisted constants are rebuilt (to the same bits).
 __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, double frozen_r,
                                  double tau_frozen, double tau_init, const FwdWs& W,
-                                 bool hoist, SolveShared& sh, bool init_tau = true) {
+                                 bool hoist, SolveShared& sh, double* grad = nullptr,
+                                 size_t gstride = 0, bool resume = false) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
   if (threadIdx.x == 0) {
@@ -114,7 +117,11 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
   for (size_t k = threadIdx.x; k < N; k += blockDim.x) {
     const int i = (int)(k % nx), j = (int)(k / nx);
     double t0, t0x, t0y;
-    if (P.lonlat) {
+    if (resume) {
+      t0 = W.T0[k];
+      t0x = grad[k];
+      t0y = grad[gstride + k];
+    } else if (P.lonlat) {
       const double cyy = P.cosy[j], syy = P.siny[j];
       const double cdx = cos(P.xs[i] - x0), sdx = sin(P.xs[i] - x0);
       const double tmp = syy * sy0 + cyy * cy0 * cdx;
@@ -152,8 +159,14 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
         t0y = fun0 * fun0 * (a0 / D * ddy + c0 / D * ddx) / t0;
       }
     }
-    W.T0[k] = t0;
-    if (init_tau) W.tau[k] = box.has(i, j) ? tau_frozen : tau_init;
+    if (!resume) {
+      W.T0[k] = t0;
+      W.tau[k] = box.has(i, j) ? tau_frozen : tau_init;
+      if (grad) {
+        grad[k] = t0x;
+        grad[gstride + k] = t0y;
+      }
+    }
     if (!hoist) {
       W.K[(size_t)0 * N + k] = t0x;
       W.K[(size_t)1 * N + k] = t0y;
