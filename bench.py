@@ -661,13 +661,15 @@ def _side_serving(sg, dev):
 def _side_config4(sg, flush, dev):
     """Config 4 beside the headline: 120 sources x 25 periods = 3000 solves
     on grids of 64^2 .. 384^2 (3-D mode), FP32-factored and plain FP64 on
-    the same engine, each timed with CUDA events on the engine's stream (L2
-    flushed between steps), the FP32 error against the FP64 results."""
+    the same engine (each path's kernel variant picked by the autotuner),
+    each timed with CUDA events on the engine's stream (L2 flushed between
+    steps), the FP32 error against the FP64 results."""
     from surfatt_gb300 import workloads as W
     pb = W.config4()
     eng = sg.Engine(dev)
     eng.load(pb)
     eng.autotune(pb.mode, sg.PREC_FP64)
+    eng.autotune(pb.mode, sg.PREC_FP32)
     eng.run(pb.mode, sg.PREC_FP64)
     eng.sync()
     r64 = eng.results()

@@ -132,6 +132,10 @@ int fp32w_variant_count();
 // Whether a variant cuts solves into work items (one workspace slot per
 // solve), and the items per solve of an evaluation mode.
 bool fp32w_variant_items(int variant);
+// Variants that sweep grids of more than 128 rows in strips by one warp.
+bool fp32w_variant_strips(int variant);
+// Threads per block of the row kernel for `bands` bands.
+int fp32w_block(int bands, int variant);
 int fp32w_items_for_mode(int mode);
 constexpr int kSolveStateInts = 5;
 // Per-solve state record (ints) of a solve cut into items: items done (-1:

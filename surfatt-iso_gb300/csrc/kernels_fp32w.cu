@@ -1,6 +1,8 @@
 // kernels_fp32w.cu -- FP32-factored batched solve, one warp per (period,
-// source) solve for grids of at most 128 rows, a team of up to four warps
-// (one block, 128 rows each) for grids of up to 512 rows.
+// source) solve for grids of at most 128 rows; for grids of up to 512 rows
+// either a team of up to four warps (one block, 128 rows each) or one warp
+// sweeping the same 128-row strips one after another (same results, bit for
+// bit: fewer warp-steps per solve, twice the steps in a row).
 //
 // Wavefront without block barriers.  In each of the four sweeps, lane l owns
 // the logical rows v = l + 32*m (m < MB) and at step t visits the cell
@@ -90,6 +92,36 @@ __device__ __forceinline__ void tsum_max2(double& a, double& b, double& c) {
   }
 }
 
+
+// Strips of one warp (at most a team's warps): the partial sum of strip p
+// kept apart (selects: a run-time index would put the array in local memory)
+// and the strips reduced as a team reduces its warps: each over the lanes by
+// the xor tree, then in strip order.
+constexpr int kMaxStrips = 4;
+
+__device__ __forceinline__ void w_strip_put(float (&l1s)[kMaxStrips], int p, float v) {
+#pragma unroll
+  for (int q = 0; q < kMaxStrips; ++q)
+    if (q == p) l1s[q] = v;
+}
+
+__device__ __forceinline__ double w_strip_sum(const float (&l1s)[kMaxStrips], int nstrip) {
+  double a = 0.0;
+#pragma unroll
+  for (int q = 0; q < kMaxStrips; ++q) {
+    double x = (double)l1s[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    if (q < nstrip) a += x;
+  }
+  return a;
+}
+
+__device__ __forceinline__ double w_warp_max(double b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) b = fmax(b, __shfl_xor_sync(FULL, b, o));
+  return b;
+}
 
 // Workspace per warp slot: W (float4 adjoint weights), G (float2: T0x,
 // T0y), T0, tau, old, 1/d, two scaled adjoint sources (4 bytes each per
@@ -195,10 +227,11 @@ __device__ __forceinline__ WRow w_row(int v, int nx, int ny, int xdir, int ydir,
 // whole step to arrive and are never copied) or at the visit itself
 // (PF = 0: fewer live registers).  Row constants (WRow) are computed once
 // per sweep, so a step costs a few integer operations per band.
-template <int MB, int PF, int NW>
+template <int MB, int PF, int NW, bool ST>
 __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WSolve& w,
                                     const Tm<NW>& T, int it0, int it1, int* status_out,
                                     int* iters_out) {
+  static_assert(!ST || NW == 1, "strips are swept by one warp");
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const int nsteps = nx + ny - 1;
@@ -214,18 +247,36 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
   // team barrier per step).  The north neighbour of its last row is the
   // first row of warp w+1, visited a step later: its old value is read from
   // memory a step ahead (that cell is rewritten two steps later).
-  const int vb = 32 * MB * T.wid;
-  const int vtop = vb + 32 * MB - 1;
-  const bool top = NW > 1 && lane == 31 && T.wid < NW - 1;
-  const bool bot = NW > 1 && lane == 0 && T.wid > 0;
+  //
+  // Strips (ST): one warp sweeps the team's row blocks one after another,
+  // strip p being the rows a team's warp p owns.  When strip p is swept,
+  // strip p-1 is final for this sweep and strip p+1 not yet touched, so the
+  // south neighbours of its first row (new values) and the north
+  // neighbours of its last row (old values) are both in memory, a step
+  // ahead; every visit sees the neighbour values it sees in a team, and
+  // the per-strip partial sums are reduced in the team's order, so the
+  // results are a team's, bit for bit, without the team's barrier per step.
+  const int nstrip = ST ? (ny + 32 * MB - 1) / (32 * MB) : 1;
   __shared__ float xs_val[2][NW > 1 ? NW : 1], xs_t0[2][NW > 1 ? NW : 1];
   int iter, status = ST_NOT_CONVERGED;
   for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f;
+    float l1s[kMaxStrips];  // strips, last sweep: strip p's partial sums
+#pragma unroll
+    for (int p = 0; p < kMaxStrips; ++p) l1s[p] = 0.f;
     for (int s = 0; s < 4; ++s) {
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
       const bool last = s == 3;
+     for (int sp = 0; sp < nstrip; ++sp) {
+      const int vb = 32 * MB * (ST ? sp : T.wid);
+      const int vtop = vb + 32 * MB - 1;
+      const bool top = (NW > 1 || ST) && lane == 31 && (ST ? vtop + 1 < ny : T.wid < NW - 1);
+      const bool bot = (NW > 1 || ST) && lane == 0 && (ST ? sp > 0 : T.wid > 0);
+      // a strip's own steps; a team's warps step together over the grid's
+      const int tbeg = ST ? vb : 0;
+      const int tend = ST ? min(vtop, ny - 1) + nx : nsteps;
+      if (ST) l1 = 0.f;
       WRow R[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) R[m] = w_row(vb + lane + 32 * m, nx, ny, xdir, ydir, w.box);
@@ -266,22 +317,36 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
           t0 = T0a[k];
         }
       };
+      // strips: new tau and T0 of the cell south of the bottom row at step
+      // tt (the strip below visited it at step tt - 1)
+      auto south_of_bot = [&](int tt, float& own, float& t0) {
+        const int u = tt - vb;
+        own = 0.f;
+        t0 = 0.f;
+        if (u >= 0 && u < nx && vb >= 1) {
+          const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? vb - 1 : ny - vb);
+          own = tau[k];
+          t0 = T0a[k];
+        }
+      };
       // exchange ring: steps t (x0), t + 1 (x1), t + 2 (x2, in flight)
       float res[MB], t0prev[MB], x0o[MB], x0t[MB], x1o[MB], x1t[MB], x2o[MB], x2t[MB];
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         res[m] = 0.f;
         t0prev[m] = 0.f;
-        exch(m, 0, x0o[m], x0t[m]);
-        exch(m, 1, x1o[m], x1t[m]);
-        exch(m, 2, x2o[m], x2t[m]);
-        if (PF == 1) heavy(m, 0);
+        exch(m, tbeg, x0o[m], x0t[m]);
+        exch(m, tbeg + 1, x1o[m], x1t[m]);
+        exch(m, tbeg + 2, x2o[m], x2t[m]);
+        if (PF == 1) heavy(m, tbeg);
       }
-      float pn_own = 0.f, pn_t0 = 0.f;
-      if (top) north_of_top(0, pn_own, pn_t0);
-      for (int t = 0; t < nsteps; ++t) {
-        float qn_own = 0.f, qn_t0 = 0.f;
+      float pn_own = 0.f, pn_t0 = 0.f, ps_own = 0.f, ps_t0 = 0.f;
+      if (top) north_of_top(tbeg, pn_own, pn_t0);
+      if (ST && bot) south_of_bot(tbeg, ps_own, ps_t0);
+      for (int t = tbeg; t < tend; ++t) {
+        float qn_own = 0.f, qn_t0 = 0.f, qs_own = 0.f, qs_t0 = 0.f;
         if (top) north_of_top(t + 1, qn_own, qn_t0);
+        if (ST && bot) south_of_bot(t + 1, qs_own, qs_t0);
         // Bands in descending order: band m's south neighbours include lane 31
         // of band m-1, whose value must still be the previous step's.
         float dds[MB];
@@ -290,10 +355,11 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
           const int m = MB - 1 - mm;
           float south = w_below<MB>(res, m, lane), t0s = w_below<MB>(t0prev, m, lane);
           float north = w_above<MB>(x1o, m, lane), t0n = w_above<MB>(x1t, m, lane);
-          if (NW > 1) {
+          if (NW > 1 || ST) {
             if (m == 0 && bot) {
-              south = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
-              t0s = xs_t0[(t + 1) & 1][T.wid - 1];
+              // team: written by warp w-1 at step t-1
+              south = ST ? ps_own : xs_val[(t + 1) & 1][T.wid - 1];
+              t0s = ST ? ps_t0 : xs_t0[(t + 1) & 1][T.wid - 1];
             }
             if (m == MB - 1 && top) {
               north = pn_own;
@@ -353,12 +419,22 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
         }
         pn_own = qn_own;
         pn_t0 = qn_t0;
+        ps_own = qs_own;
+        ps_t0 = qs_t0;
         tsync<NW>();
       }
+      if (ST && last) w_strip_put(l1s, sp, l1);
+     }
     }
     // FP64 decision over the lanes' partial sums (:1091-1115)
-    double sl1 = (double)l1, smax = (double)lmax, unused = 0.0;
-    tsum_max2<NW>(sl1, smax, unused);
+    double sl1, smax = (double)lmax, unused = 0.0;
+    if (ST) {
+      sl1 = w_strip_sum(l1s, nstrip);
+      smax = w_warp_max(smax);
+    } else {
+      sl1 = (double)l1;
+      tsum_max2<NW>(sl1, smax, unused);
+    }
     sl1 = sl1 / (double)nx / (double)ny;
     if (fabs(sl1) < TOL_UW && smax < TOL_UW) {
       status = ST_OK;
@@ -443,9 +519,10 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
 // a fixed set of registers and no operand is ever copied.  The solve kernel
 // affords D = 2 for a single warp (its forward sweeps hold the register
 // file: deeper rings spill) and D = 3 for teams.
-template <int MB, int NW, int D>
+template <int MB, int NW, int D, bool ST>
 __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src,
                                     const Tm<NW>& T, int* status_out, int* iters_out) {
+  static_assert(!ST || NW == 1, "strips are swept by one warp");
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   const int nu = nx - 2, nv = ny - 2;
   const int nsteps = nu + nv - 1;
@@ -457,23 +534,38 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
   tsync<NW>();
   // Teams: as in the forward sweeps, the first row's south value comes
   // through a shared slot from the warp below, the last row's north value
+  // from memory a step ahead.  Strips (ST): as in the forward sweeps, both
   // from memory a step ahead.
-  const int vb = 32 * MB * T.wid;
-  const int vtop = vb + 32 * MB - 1;
-  const bool top = NW > 1 && lane == 31 && T.wid < NW - 1;
-  const bool bot = NW > 1 && lane == 0 && T.wid > 0;
+  const int nstrip = ST ? (nv + 32 * MB - 1) / (32 * MB) : 1;
   __shared__ float xs_val[2][NW > 1 ? NW : 1];
   int iter, status = ST_NOT_CONVERGED;
   for (iter = 1; iter <= MAXITER_JSE; ++iter) {
     float l1 = 0.f, lmax = 0.f, vmax = 0.f;
+    float l1s[kMaxStrips];  // strips, last sweep: strip p's partial sums
+#pragma unroll
+    for (int p = 0; p < kMaxStrips; ++p) l1s[p] = 0.f;
     for (int s = 0; s < 4; ++s) {
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
       const bool last = s == 3;
+     for (int sp = 0; sp < nstrip; ++sp) {
+      const int vb = 32 * MB * (ST ? sp : T.wid);
+      const int vtop = vb + 32 * MB - 1;
+      const bool top = (NW > 1 || ST) && lane == 31 && (ST ? vtop + 1 < nv : T.wid < NW - 1);
+      const bool bot = (NW > 1 || ST) && lane == 0 && (ST ? sp > 0 : T.wid > 0);
+      const int tbeg = ST ? vb : 0;
+      const int tend = ST ? min(vtop, nv - 1) + nu : nsteps;
+      if (ST) l1 = 0.f;
       auto north_of_top = [&](int tau) {
         const int u = tau - vtop;
         if (u < 0 || u >= nu || vtop + 1 >= nv) return 0.f;
         return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
+      };
+      // strips: the new value south of the bottom row at step tau
+      auto south_of_bot = [&](int tau) {
+        const int u = tau - vb;
+        if (u < 0 || u >= nu || vb < 1) return 0.f;
+        return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? vb : nv + 1 - vb)];
       };
       // A cell is written only at its own visit and the weights, sources and
       // iteration-start values are fixed within a sweep, so operands loaded
@@ -485,24 +577,28 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
         res[m] = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d)
-          wa_load<true>(ring[d][m], d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src, last);
+          wa_load<true>(ring[d][m], tbeg + d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
+                        last);
       }
-      float pn = top ? north_of_top(0) : 0.f;
-      for (int t0 = 0; t0 < nsteps; t0 += D) {
+      float pn = top ? north_of_top(tbeg) : 0.f;
+      float ps = (ST && bot) ? south_of_bot(tbeg) : 0.f;
+      for (int t0 = tbeg; t0 < tend; t0 += D) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
           const int t = t0 + d;
-          if (t >= nsteps) break;  // the same for every thread of the team
+          if (t >= tend) break;  // the same for every thread of the team
           WAdj(&cur)[MB] = ring[d];
           const WAdj(&nxt)[MB] = ring[(d + 1) % D];
           const float qn = top ? north_of_top(t + 1) : 0.f;
+          const float qs = (ST && bot) ? south_of_bot(t + 1) : 0.f;
           float south[MB], north[MB], nown[MB];
 #pragma unroll
           for (int m = 0; m < MB; ++m) nown[m] = nxt[m].own;
           w_from_below<MB>(res, south, lane);
           w_from_above<MB>(nown, north, lane);
-          if (NW > 1) {
-            if (bot) south[0] = xs_val[(t + 1) & 1][T.wid - 1];  // written at step t-1
+          if (NW > 1 || ST) {
+            // team: written by warp w-1 at step t-1
+            if (bot) south[0] = ST ? ps : xs_val[(t + 1) & 1][T.wid - 1];
             if (top) north[MB - 1] = pn;
           }
 #pragma unroll
@@ -535,12 +631,22 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
                           last);
           if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
           pn = qn;
+          ps = qs;
           tsync<NW>();
         }
       }
+      if (ST && last) w_strip_put(l1s, sp, l1);
+     }
     }
-    double sl1 = (double)l1, smax = (double)lmax, svmax = (double)vmax;
-    tsum_max2<NW>(sl1, smax, svmax);
+    double sl1, smax = (double)lmax, svmax = (double)vmax;
+    if (ST) {
+      sl1 = w_strip_sum(l1s, nstrip);
+      smax = w_warp_max(smax);
+      svmax = w_warp_max(svmax);
+    } else {
+      sl1 = (double)l1;
+      tsum_max2<NW>(sl1, smax, svmax);
+    }
     sl1 = sl1 / (double)(nx * ny);
     if ((fabs(sl1) < TOL_JSE && smax < TOL_JSE) || smax <= svmax * 0x1p-21) {
       status = ST_OK;
@@ -711,7 +817,7 @@ __host__ __device__ inline int w_items_for_mode(int mode) {
   return kFwdItems + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
 }
 
-template <int MB, int PF, int MINW, int NW>
+template <int MB, int PF, int MINW, int NW, bool ST>
 __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A) {
   const Tm<NW> T = this_team<NW>();
   const int lane = T.lane;
@@ -856,7 +962,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
       const int it0 = first == 0 ? 1 : fit + 1;
       const int it1 = (cut && first < kFwdItems - 1) ? (first + 1) * kSplitIter : MAXITER_UW;
       int n = 0;
-      w_fwd_sweeps<MB, PF, NW>(P, V, w, T, it0, it1, &fst, &n);
+      w_fwd_sweeps<MB, PF, NW, ST>(P, V, w, T, it0, it1, &fst, &n);
       fit = n;
       mark(PH_FWD);
     }
@@ -893,8 +999,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     const int f1 = A.mode >= 2 ? (cut ? lastit - kFwdItems : nf - 1) : -1;
     for (int f = f0; f <= f1; ++f) {
       int ast = ST_OK, n = 0;
-      w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2>(P, V, f ? V.src[1] : V.src[0], T, &ast,
-                                                        &n);
+      w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(P, V, f ? V.src[1] : V.src[0], T,
+                                                            &ast, &n);
       mark(PH_ADJ);
       if (f == 0) its0 = n; else its1 = n;
       if (ast != ST_OK && st == ST_OK) st = ast;
@@ -924,25 +1030,30 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
 int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 
 // Variants of the warp kernel: operand loads, resident warps per SM, whole
-// solves or solves cut into items.
+// solves or solves cut into items, teams or strips above 128 rows.
 //   0: every operand loaded a step ahead into registers, 8 warps per SM, items
 //   1: the same, whole solves
 //   2: cell constants loaded at the visit, 12 warps per SM, items
 //   3: cell constants loaded at the visit, 8 warps per SM, whole solves
-constexpr int kFp32wVariants = 4;
+//   4: as 0, grids of more than 128 rows swept in strips by one warp
+//   5: as 1, the same strips
+// On grids of at most 128 rows variants 4 and 5 are variants 0 and 1.
+constexpr int kFp32wVariants = 6;
 int fp32w_variant_count() { return kFp32wVariants; }
-bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2; }
+bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2 || variant == 4; }
+bool fp32w_variant_strips(int variant) { return variant >= 4; }
 int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
 
-template <int MB, int PF, int MINW, int NW>
+template <int MB, int PF, int MINW, int NW, bool ST>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {
-  k_batch_fp32w<MB, PF, MINW, NW><<<grid, 32 * NW, 0, st>>>(a);
+  k_batch_fp32w<MB, PF, MINW, NW, ST><<<grid, 32 * NW, 0, st>>>(a);
 }
 
-template <int MB, int PF, int MINW, int NW>
+template <int MB, int PF, int MINW, int NW, bool ST>
 static int occupancy_w() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF, MINW, NW>, 32 * NW, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_fp32w<MB, PF, MINW, NW, ST>, 32 * NW,
+                                                0);
   return n;
 }
 
@@ -950,9 +1061,11 @@ template <int MB, int NW>
 static void launch_mb(const BatchArgs& a, int grid, int variant, cudaStream_t st) {
   switch (variant) {
     case 0:
-    case 1: launch_w<MB, 1, 8, NW>(a, grid, st); break;
-    case 2: launch_w<MB, 0, 12, NW>(a, grid, st); break;
-    default: launch_w<MB, 0, 8, NW>(a, grid, st); break;
+    case 1:
+    case 4:
+    case 5: launch_w<MB, 1, 8, NW, false>(a, grid, st); break;
+    case 2: launch_w<MB, 0, 12, NW, false>(a, grid, st); break;
+    default: launch_w<MB, 0, 8, NW, false>(a, grid, st); break;
   }
 }
 
@@ -960,14 +1073,21 @@ template <int MB, int NW>
 static int occupancy_mb(int variant) {
   switch (variant) {
     case 0:
-    case 1: return occupancy_w<MB, 1, 8, NW>();
-    case 2: return occupancy_w<MB, 0, 12, NW>();
-    default: return occupancy_w<MB, 0, 8, NW>();
+    case 1:
+    case 4:
+    case 5: return occupancy_w<MB, 1, 8, NW, false>();
+    case 2: return occupancy_w<MB, 0, 12, NW, false>();
+    default: return occupancy_w<MB, 0, 8, NW, false>();
   }
 }
 
 // Grids of more than 128 rows: teams of fp32w_team(ny) warps of four bands.
 int fp32w_team(int max_ny) { return max_ny <= 32 * 4 ? 1 : (max_ny + 127) / 128; }
+
+// Threads per block: a team's warps, or one warp (strips).
+int fp32w_block(int bands, int variant) {
+  return bands <= 4 || fp32w_variant_strips(variant) ? 32 : 32 * fp32w_team(32 * bands);
+}
 
 void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st) {
   switch (bands) {
@@ -976,6 +1096,10 @@ void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cu
     case 3: launch_mb<3, 1>(a, grid, variant, st); break;
     case 4: launch_mb<4, 1>(a, grid, variant, st); break;
     default:
+      if (fp32w_variant_strips(variant)) {
+        launch_w<4, 1, 8, 1, true>(a, grid, st);
+        break;
+      }
       switch (fp32w_team(32 * bands)) {
         case 2: launch_mb<4, 2>(a, grid, variant, st); break;
         case 3: launch_mb<4, 3>(a, grid, variant, st); break;
@@ -991,6 +1115,7 @@ int batch_fp32w_max_blocks_per_sm(int bands, int variant) {
     case 3: return occupancy_mb<3, 1>(variant);
     case 4: return occupancy_mb<4, 1>(variant);
     default:
+      if (fp32w_variant_strips(variant)) return occupancy_w<4, 1, 8, 1, true>();
       switch (fp32w_team(32 * bands)) {
         case 2: return occupancy_mb<4, 2>(variant);
         case 3: return occupancy_mb<4, 3>(variant);

@@ -43,8 +43,10 @@ std::vector<KernelChoice> plan_candidates(const EvalShape& sh, int prec) {
     c.push_back({KK_FP64, 1});  // whole solves
     return c;
   }
+  // (the strip variants differ from 0 and 1 only on grids of more than 128 rows)
   if (sh.max_ny <= kTeamMaxRows && sh.max_nx <= kWarpMaxCols)
-    for (int v = 0; v < fp32w_variant_count(); ++v) c.push_back({KK_FP32_WARP, v});
+    for (int v = 0; v < fp32w_variant_count(); ++v)
+      if (!fp32w_variant_strips(v) || sh.max_ny > 128) c.push_back({KK_FP32_WARP, v});
   if (sh.max_diag <= kFp32MaxThreads) c.push_back({KK_FP32_BLOCK, 0});
   return c;
 }
@@ -74,10 +76,10 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     // one warp (a team of warps above 128 rows) per solve, lanes own the rows
     // automatic: the row-per-lane kernel (the faster on the measured shapes)
     p.kind = KK_FP32_WARP;
-    p.block = 32 * fp32w_team(sh.max_ny);
     p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
     p.pf = force.variant >= 0 && force.variant < fp32w_variant_count() ? force.variant : 0;
+    p.block = fp32w_block(p.bands, p.pf);
     p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
     p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);
     p.cut = fp32w_variant_items(p.pf);
@@ -115,7 +117,7 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     for (int c = 0; c < kTeamClasses; ++c)
       if (sh.team_count[c] > 0) {
         p.bands = fp32w_bands(sh.team_max_ny[c]);
-        p.block = 32 * fp32w_team(sh.team_max_ny[c]);
+        p.block = fp32w_block(p.bands, p.pf);
         p.per_sm = std::max(1, batch_fp32w_max_blocks_per_sm(p.bands, p.pf));
         p.grid = grid_for(p.per_sm, sh.nsolve);
       }

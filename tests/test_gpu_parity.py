@@ -260,10 +260,11 @@ def test_engine_fp32_tall_grids(sg, oracle):
 
 
 @pytest.mark.parametrize("nx,ny", [(60, 200), (150, 257), (96, 384), (40, 512)])
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_fp32_warp_teams(sg, oracle, nx, ny, variant):
-    """Warp teams (2 to 4 warps of 128 rows): every variant gives the same
-    bits and matches the oracle within the FP32 tolerances."""
+    """Warp teams (2 to 4 warps of 128 rows) and one warp sweeping the same
+    row blocks as strips (variants 4, 5): every variant gives the same bits
+    and matches the oracle within the FP32 tolerances."""
     pb = W.flat_case(nx=nx, ny=ny, d=0.02, nsta=4, nperiod=1, mode=3, seed=40 + ny)
     st0, kv0, base = _run_kernel(sg, pb, 3, 2, 0)
     st, kv, o = _run_kernel(sg, pb, 3, 2, variant)
@@ -294,7 +295,7 @@ def test_fp32_team_batch_small_grids_unchanged(sg):
     eng.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_fp32_team_classes(sg, oracle, variant):
     """A batch of three team classes (grids of 48 to 304 rows) runs as one
     concurrent launch per class; every solve gives the bits it gives as
@@ -460,7 +461,7 @@ def test_engine_source_on_boundary_status(sg, oracle):
     eng.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_fp32_warp_variants(sg, oracle, variant):
     """Every warp-kernel variant agrees with the oracle within the FP32
     tolerances, and all variants give the same bits (they differ only in when
