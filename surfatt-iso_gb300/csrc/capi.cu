@@ -280,7 +280,8 @@ int uw_dropin(const double* xx, const double* yy, int nx, int ny, const double* 
   c.t_ok = false;  // T is rewritten
   if (weno)
     launch_weno_single(P, xs0, ys0, multi, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
-  else
+  else if (!launch_uw_cluster(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(),
+                              c.st))
     launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
   if (cudaGetLastError() != cudaSuccess) return record(SURFATT_CUDA_ERROR, 0);
   double* staged = nullptr;
@@ -470,7 +471,8 @@ surfatt_status_t surfatt_measadj_run_forward(const double* xgrids, const double*
     return (surfatt_status_t)record(SURFATT_OOM, 0);
   const double xs0 = srcx / 180.0 * PI_S, ys0 = srcy / 180.0 * PI_S;
   c.t_ok = false;  // T is rewritten
-  launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
+  if (!launch_uw_cluster(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st))
+    launch_uw_single(P, xs0, ys0, c.ws.as<double>(), c.T.as<double>(), c.si.as<int>(), c.st);
   if (cudaMemsetAsync(c.si.as<int>() + 2, 0, sizeof(int), c.st) != cudaSuccess)
     return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
   if (nrec > 0) {

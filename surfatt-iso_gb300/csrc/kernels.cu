@@ -5,6 +5,8 @@
 
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "kernels.cuh"
 #include "solver_fp64.cuh"
 #include "batch_tail.cuh"
@@ -97,11 +99,13 @@ void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st) {
 // work queue; each runs forward -> interp2 -> misfit -> adjoint(s) -> mask
 // -> kernel contribution for one (period, source).
 // ---------------------------------------------------------------------------
-long long batch_fp64_ws_doubles(long long N) {
-  // tau, tau_old, T0, T + max(forward constants, adjoint constants + 6 fields)
-  const long long fwd = (long long)KC_COUNT, adj = (long long)KA_COUNT + 6;
-  return (4 + (fwd > adj ? fwd : adj)) * N;
+// tau, tau_old, T0, T + max(forward constants, adjoint constants + 6 fields)
+__host__ __device__ constexpr long long fp64_slot_doubles(long long N) {
+  return (4 + ((long long)KC_COUNT > (long long)KA_COUNT + 6 ? (long long)KC_COUNT
+                                                              : (long long)KA_COUNT + 6)) * N;
 }
+
+long long batch_fp64_ws_doubles(long long N) { return fp64_slot_doubles(N); }
 
 struct SolveLayout {
   FwdWs fw;
@@ -449,7 +453,8 @@ __device__ inline void weno_sweeps(const PeriodDev& P, const FwdWs& W, SolveShar
 // ---------------------------------------------------------------------------
 // Single-solve kernels (one block) for the drop-in symbols
 // ---------------------------------------------------------------------------
-long long single_ws_doubles(long long N) { return batch_fp64_ws_doubles(N); }
+// (+ four N-cell arrays: the cluster forward's per-block iteration-start tau)
+long long single_ws_doubles(long long N) { return batch_fp64_ws_doubles(N) + 4 * N; }
 
 __global__ void __launch_bounds__(256) k_uw_single(PeriodDev P, double x0, double y0, double* ws,
                                                    double* T, int* si) {
@@ -469,6 +474,170 @@ __global__ void __launch_bounds__(256) k_uw_single(PeriodDev P, double x0, doubl
 void launch_uw_single(const PeriodDev& P, double x0, double y0, double* ws, double* T,
                       int* si, cudaStream_t st) {
   k_uw_single<<<1, 256, 0, st>>>(P, x0, y0, ws, T, si);
+}
+
+// One plain FP64 forward solve on a cluster of kUwRanks blocks, one per SM.
+//
+// A call of the drop-in is one solve, a chain of anti-diagonal steps, and an
+// FP64 warp instruction holds a scheduler for the same time whatever the
+// number of its active lanes: one block's step costs the whole visit's FP64
+// instruction sequence however the diagonal's cells are spread over warps.
+// Here the visit itself is spread: block r evaluates only case r of the
+// update (two-sided case r and one-sided case r, a quarter of the FP64
+// instructions) for every cell of the diagonal and writes its candidate
+// minimum into every block's shared memory; after one cluster barrier each
+// block takes min(tau, the four candidates) -- the same minimum over the
+// same roots as uw_update -- into its own shared copy of tau.  Every block
+// therefore holds the same field, accumulates the same convergence sums
+// (same thread-to-cell map and block reduction as k_uw_single) and takes
+// the same decisions, so all blocks run the same number of barriers.
+// Candidates are double-buffered by diagonal parity: a block writes
+// diagonal d+1's only after the barrier of diagonal d, which every block
+// reaches after reading diagonal d-1's.  The cell constants, T0 and the
+// setup's outputs stay in global memory (the setup is shared out by
+// chunks); the per-block iteration-start values in ws beyond the single
+// solve's layout.  Results equal k_uw_single's.
+constexpr int kUwRanks = 4;
+
+__global__ void __launch_bounds__(256) k_uw_cluster(PeriodDev P, double x0, double y0, double* ws,
+                                                    double* T, int* si) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  extern __shared__ double uw_dyn[];
+  __shared__ SolveShared sh;
+  const int nx = P.nx, ny = P.ny;
+  const size_t N = (size_t)nx * ny;
+  SolveLayout L = carve(ws, N);
+  fwd_setup(P, x0, y0, 1.0, 1.0, 10.0, L.fw, true, sh, nullptr, 0, false, rank, kUwRanks);
+  if (sh.status != ST_OK) {  // the same in every block
+    if (rank == 0 && threadIdx.x == 0) { si[0] = sh.status; si[1] = 0; }
+    return;
+  }
+  cl.sync();  // every block's part of the setup is visible
+  double* tau = uw_dyn;
+  const int maxd = nx < ny ? nx : ny;
+  double* cand = uw_dyn + N;  // [2][kUwRanks][maxd]
+  double* told = ws + fp64_slot_doubles((long long)N) + (size_t)rank * N;
+  for (size_t k = threadIdx.x; k < N; k += blockDim.x) tau[k] = L.fw.tau[k];
+  __syncthreads();
+  const double* __restrict__ K = L.fw.K;
+  const double* __restrict__ T0 = L.fw.T0;
+  const Box box = sh.box;
+  const double inf = __longlong_as_double(0x7ff0000000000000LL);
+  int iter, status = ST_NOT_CONVERGED;
+  for (iter = 1; iter <= MAXITER_UW; ++iter) {
+    double l1 = 0.0, linf = 0.0;
+    for (int s = 0; s < 4; ++s) {
+      SweepGeom g;
+      g.ilo = 0; g.ihi = nx - 1; g.jlo = 0; g.jhi = ny - 1;
+      sweep_dirs(s, g.xdir, g.ydir);
+      const int nd = g.ndiag();
+      for (int d = 0; d < nd; ++d) {
+        const int vlo = g.vmin(d), vhi = g.vmax(d);
+        double* const cb = cand + (size_t)(d & 1) * kUwRanks * maxd;
+        for (int v = vlo + (int)threadIdx.x; v <= vhi; v += blockDim.x) {
+          int i, j;
+          g.cell(d, v, i, j);
+          double m = inf;
+          if (!box.has(i, j)) {
+            const size_t k = (size_t)i + (size_t)nx * j;
+            m = uw_case(rank, K, k, i, j, nx, ny, tau, T0, P.a[k], P.b[k], P.c[k], P.f2[k],
+                        P.disx[k], P.disy[k]);
+          }
+          const int slot = rank * maxd + (v - vlo);
+#pragma unroll
+          for (int q = 0; q < kUwRanks; ++q) cl.map_shared_rank(cb, q)[slot] = m;
+        }
+        cl.sync();
+        for (int v = vlo + (int)threadIdx.x; v <= vhi; v += blockDim.x) {
+          int i, j;
+          g.cell(d, v, i, j);
+          if (box.has(i, j)) continue;
+          const size_t k = (size_t)i + (size_t)nx * j;
+          const double tb = tau[k];
+          if (s == 0) told[k] = tb;
+          double tn = tb;
+#pragma unroll
+          for (int q = 0; q < kUwRanks; ++q) {
+            const double mq = cb[q * maxd + (v - vlo)];
+            if (mq < tn) tn = mq;
+          }
+          tau[k] = tn;
+          if (s == 3) {
+            const double dd = fabs(tn - told[k]) * T0[k];
+            l1 += dd;
+            linf = fmax(linf, dd);
+          }
+        }
+        __syncthreads();
+      }
+    }
+    block_sum_max(l1, linf, sh.red);
+    l1 = l1 / (double)nx / (double)ny;
+    // Every block reaches the same decision from the same field; block 0's
+    // is nevertheless the one all follow, so the blocks' barrier counts can
+    // never differ.
+    if (rank == 0 && threadIdx.x == 0) {
+      const int conv = fabs(l1) < TOL_UW && linf < TOL_UW;
+#pragma unroll
+      for (int q = 0; q < kUwRanks; ++q) cl.map_shared_rank(&sh.flag, q)[0] = conv;
+    }
+    cl.sync();
+    if (sh.flag) { status = ST_OK; break; }
+  }
+  for (size_t k = threadIdx.x + (size_t)rank * blockDim.x; k < N;
+       k += (size_t)blockDim.x * kUwRanks)
+    T[k] = tau[k] * T0[k];
+  if (rank == 0 && threadIdx.x == 0) {
+    si[0] = status;
+    si[1] = iter > MAXITER_UW ? MAXITER_UW : iter;
+  }
+  cl.sync();  // no block leaves while another may still address its shared memory
+}
+
+// Shared memory of k_uw_cluster: tau and the candidate buffers, at least
+// 116 KB so that two of its blocks never share an SM (their FP64 pipes are
+// what the cluster spreads the visit over).
+static size_t uw_cluster_smem(int nx, int ny) {
+  const size_t need = ((size_t)nx * ny + (size_t)2 * kUwRanks * (nx < ny ? nx : ny)) *
+                      sizeof(double);
+  return need < (size_t)116 * 1024 ? (size_t)116 * 1024 : need;
+}
+
+bool launch_uw_cluster(const PeriodDev& P, double x0, double y0, double* ws, double* T, int* si,
+                       cudaStream_t st) {
+  static const size_t max_smem = [] {
+    int dev = 0, opt = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&opt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t lim = (size_t)opt - sizeof(SolveShared) - 1024;
+    if (cudaFuncSetAttribute(k_uw_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)lim) != cudaSuccess) {
+      cudaGetLastError();
+      return (size_t)0;
+    }
+    return lim;
+  }();
+  const size_t smem = uw_cluster_smem(P.nx, P.ny);
+  if (smem > max_smem) return false;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kUwRanks);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kUwRanks;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k_uw_cluster, P, x0, y0, ws, T, si) != cudaSuccess) {
+    cudaGetLastError();  // this launch's own error: the caller takes the one-block kernel
+    return false;
+  }
+  return true;
 }
 
 __global__ void __launch_bounds__(256) k_weno_single(PeriodDev P, double x0, double y0, int multi,

@@ -169,6 +169,11 @@ void launch_chi_reduce(const double* chi_s, int nsolve, double* chi_out, cudaStr
 // Single-solve kernels of the drop-in symbols (one block).
 void launch_uw_single(const PeriodDev& P, double x0, double y0, double* ws, double* T,
                       int* status_iters, cudaStream_t st);
+// The same solve on a cluster of four blocks (one per SM), each evaluating
+// one case of the update; false (nothing launched) when the grid's tau does
+// not fit one block's shared memory or the cluster cannot be launched.
+bool launch_uw_cluster(const PeriodDev& P, double x0, double y0, double* ws, double* T,
+                       int* status_iters, cudaStream_t st);
 void launch_weno_single(const PeriodDev& P, double x0, double y0, int multiplicative, double* ws,
                         double* T, int* status_iters, cudaStream_t st);
 void launch_jse_single(const PeriodDev& P, const double* T, const double* recx,

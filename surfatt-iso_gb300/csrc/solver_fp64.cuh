@@ -75,10 +75,13 @@ struct SolveShared {
 // resume = false: T0 and tau are initialised and the gradient stored there;
 // resume = true: T0 (W.T0) and the gradient are read back, tau is left
 // alone, and only the hoisted constants are rebuilt (to the same bits).
+// part / nparts: this block sets up cells of the block-sized chunks
+// part, part + nparts, ... (several blocks share one solve's setup).
 __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, double frozen_r,
                                  double tau_frozen, double tau_init, const FwdWs& W,
                                  bool hoist, SolveShared& sh, double* grad = nullptr,
-                                 size_t gstride = 0, bool resume = false) {
+                                 size_t gstride = 0, bool resume = false, int part = 0,
+                                 int nparts = 1) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
   if (threadIdx.x == 0) {
@@ -114,7 +117,8 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
   const double dx = P.dx, dy = P.dy;
   double cy0 = 0, sy0 = 0;
   if (P.lonlat) { cy0 = cos(y0); sy0 = sin(y0); }
-  for (size_t k = threadIdx.x; k < N; k += blockDim.x) {
+  for (size_t k = threadIdx.x + (size_t)part * blockDim.x; k < N;
+       k += (size_t)blockDim.x * nparts) {
     const int i = (int)(k % nx), j = (int)(k / nx);
     double t0, t0x, t0y;
     if (resume) {
@@ -200,9 +204,62 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
   __syncthreads();
 }
 
+// Two-sided case cs of the plain first-order upwind update (:904-993):
+// lowers t to each causal root of the case's quadratic.  q* are the scaled
+// neighbour values (qw = -cx*tw, qe = cx*te, qs = -cy*ts, qn = cy*tn).
+__device__ __forceinline__ void uw_two_sided(int cs, const double* __restrict__ K, bool hw,
+                                             bool he, bool hs, bool hn, double qw, double qe,
+                                             double qs, double qn, double a, double b, double c,
+                                             double f2, double& t) {
+  const bool ok = (cs < 2 ? hw : he) && ((cs == 0 || cs == 2) ? hs : hn);
+  if (!ok) return;
+  const double qx = cs < 2 ? qw : qe;
+  const double qy = (cs == 0 || cs == 2) ? qs : qn;
+  const double ea = K[KC_EA + cs];
+  const double bx = K[KC_BX + cs], by = K[KC_BY + cs];
+  const double Cx = a * qx - c * qy;
+  const double Cy = b * qy - c * qx;
+  const double ec = qx * Cx + qy * Cy - f2;
+  const double hb = bx * qx + by * qy;
+  const double del = hb * hb - ea * ec;
+  if (del >= 0) {
+    const double iea = K[KC_IEA + cs];
+    const double s = sqrt(del);
+    const double r1 = (-hb + s) * iea, r2 = (-hb - s) * iea;
+    const double x1 = bx * r1 + Cx, y1 = by * r1 + Cy;
+    const double x2 = bx * r2 + Cx, y2 = by * r2 + Cy;
+    const bool sx = cs < 2, sy = (cs == 0 || cs == 2);  // true: >= 0 required
+    const bool c1 = (sx ? x1 >= 0 : x1 <= 0) && (sy ? y1 >= 0 : y1 <= 0);
+    const bool c2 = (sx ? x2 >= 0 : x2 <= 0) && (sy ? y2 >= 0 : y2 <= 0);
+    if (c1 && r1 < t) t = r1;
+    if (c2 && r2 < t) t = r2;
+  }
+}
+
+// One-sided case cs (0 west, 1 east, 2 south, 3 north) of the same update
+// (:996-1075): lowers t to each admissible root along one axis.
+__device__ __forceinline__ void uw_one_sided(int cs, const double* __restrict__ K, size_t k,
+                                             int nx, const double* __restrict__ T0, bool hw,
+                                             bool he, bool hs, bool hn, double qw, double qe,
+                                             double qs, double qn, double tw, double te,
+                                             double ts, double tn, double disx, double disy,
+                                             double t0, double& t) {
+  const bool ok = cs == 0 ? hw : cs == 1 ? he : cs == 2 ? hs : hn;
+  if (!ok) return;
+  const double q = cs == 0 ? qw : cs == 1 ? qe : cs == 2 ? qs : qn;
+  const double tnb = cs == 0 ? tw : cs == 1 ? te : cs == 2 ? ts : tn;
+  const size_t nb = cs == 0 ? k - 1 : cs == 1 ? k + 1 : cs == 2 ? k - nx : k + nx;
+  const double dis = cs < 2 ? disx : disy;
+  const double ip = K[KC_IPXM + cs];
+  const double lim = tnb * T0[nb], half = tnb * 0.5;
+  const double r1 = (dis - q) * ip, r2 = (-dis - q) * ip;
+  if (r1 * t0 >= lim && r1 > half && r1 < t) t = r1;
+  if (r2 * t0 >= lim && r2 > half && r2 < t) t = r2;
+}
+
 // One visit of cell k by the plain first-order upwind update (:904-1079):
 // returns min(tau, every causal two-sided root, every admissible one-sided
-// root).
+// root).  `tau` may be global or shared memory (same layout).
 __device__ __forceinline__ double uw_update(const double* __restrict__ Kall, size_t N, size_t k,
                                             int i, int j, int nx, int ny,
                                             const double* __restrict__ tau,
@@ -216,47 +273,32 @@ __device__ __forceinline__ double uw_update(const double* __restrict__ Kall, siz
   const double ts = hs ? tau[k - nx] : 0.0, tn = hn ? tau[k + nx] : 0.0;
   const double qw = -(cx * tw), qe = cx * te, qs = -(cy * ts), qn = cy * tn;
 #pragma unroll
-  for (int cs = 0; cs < 4; ++cs) {
-    const bool ok = (cs < 2 ? hw : he) && ((cs == 0 || cs == 2) ? hs : hn);
-    if (!ok) continue;
-    const double qx = cs < 2 ? qw : qe;
-    const double qy = (cs == 0 || cs == 2) ? qs : qn;
-    const double ea = K[KC_EA + cs];
-    const double bx = K[KC_BX + cs], by = K[KC_BY + cs];
-    const double Cx = a * qx - c * qy;
-    const double Cy = b * qy - c * qx;
-    const double ec = qx * Cx + qy * Cy - f2;
-    const double hb = bx * qx + by * qy;
-    const double del = hb * hb - ea * ec;
-    if (del >= 0) {
-      const double iea = K[KC_IEA + cs];
-      const double s = sqrt(del);
-      const double r1 = (-hb + s) * iea, r2 = (-hb - s) * iea;
-      const double x1 = bx * r1 + Cx, y1 = by * r1 + Cy;
-      const double x2 = bx * r2 + Cx, y2 = by * r2 + Cy;
-      const bool sx = cs < 2, sy = (cs == 0 || cs == 2);  // true: >= 0 required
-      const bool c1 = (sx ? x1 >= 0 : x1 <= 0) && (sy ? y1 >= 0 : y1 <= 0);
-      const bool c2 = (sx ? x2 >= 0 : x2 <= 0) && (sy ? y2 >= 0 : y2 <= 0);
-      if (c1 && r1 < t) t = r1;
-      if (c2 && r2 < t) t = r2;
-    }
-  }
+  for (int cs = 0; cs < 4; ++cs) uw_two_sided(cs, K, hw, he, hs, hn, qw, qe, qs, qn, a, b, c, f2, t);
   const double t0 = T0[k];
-  // one-sided (:996-1075)
 #pragma unroll
-  for (int cs = 0; cs < 4; ++cs) {
-    const bool ok = cs == 0 ? hw : cs == 1 ? he : cs == 2 ? hs : hn;
-    if (!ok) continue;
-    const double q = cs == 0 ? qw : cs == 1 ? qe : cs == 2 ? qs : qn;
-    const double tnb = cs == 0 ? tw : cs == 1 ? te : cs == 2 ? ts : tn;
-    const size_t nb = cs == 0 ? k - 1 : cs == 1 ? k + 1 : cs == 2 ? k - nx : k + nx;
-    const double dis = cs < 2 ? disx : disy;
-    const double ip = K[KC_IPXM + cs];
-    const double lim = tnb * T0[nb], half = tnb * 0.5;
-    const double r1 = (dis - q) * ip, r2 = (-dis - q) * ip;
-    if (r1 * t0 >= lim && r1 > half && r1 < t) t = r1;
-    if (r2 * t0 >= lim && r2 > half && r2 < t) t = r2;
-  }
+  for (int cs = 0; cs < 4; ++cs)
+    uw_one_sided(cs, K, k, nx, T0, hw, he, hs, hn, qw, qe, qs, qn, tw, te, ts, tn, disx, disy, t0,
+                 t);
+  return t;
+}
+
+// The candidates of one case only (two-sided case cs and one-sided case cs):
+// their minimum, +inf when the case has none.  The minimum over the four
+// cases and the old value is uw_update's result.
+__device__ __forceinline__ double uw_case(int cs, const double* __restrict__ Kall, size_t k, int i,
+                                          int j, int nx, int ny, const double* __restrict__ tau,
+                                          const double* __restrict__ T0, double a, double b,
+                                          double c, double f2, double disx, double disy) {
+  const bool hw = i > 0, he = i < nx - 1, hs = j > 0, hn = j < ny - 1;
+  const double* __restrict__ K = Kall + k * (size_t)KC_COUNT;
+  const double cx = K[KC_CX], cy = K[KC_CY];
+  const double tw = hw ? tau[k - 1] : 0.0, te = he ? tau[k + 1] : 0.0;
+  const double ts = hs ? tau[k - nx] : 0.0, tn = hn ? tau[k + nx] : 0.0;
+  const double qw = -(cx * tw), qe = cx * te, qs = -(cy * ts), qn = cy * tn;
+  double t = __longlong_as_double(0x7ff0000000000000LL);
+  uw_two_sided(cs, K, hw, he, hs, hn, qw, qe, qs, qn, a, b, c, f2, t);
+  uw_one_sided(cs, K, k, nx, T0, hw, he, hs, hn, qw, qe, qs, qn, tw, te, ts, tn, disx, disy, T0[k],
+               t);
   return t;
 }
 
