@@ -952,7 +952,6 @@ def run_dropin(args):
     out: `value` and `e2e` are the same measurement."""
     import ctypes
     import multiprocessing as mp
-    import threading
     from concurrent.futures import ThreadPoolExecutor
     import torch
     import surfatt_gb300 as sg
@@ -974,40 +973,62 @@ def run_dropin(args):
     nx, ny = len(xx), len(yy)
     N = nx * ny
     L = sg.lib()
+    # The callers are Python threads: every drop-in call releases the GIL,
+    # but a thread returning from one waits for the GIL up to the switch
+    # interval (5 ms by default) while another runs Python code between its
+    # calls.  Fortran callers (MPI ranks) have no such lock: a short switch
+    # interval keeps the harness's own lock out of the measured calls.
+    sys.setswitchinterval(1e-5)
     dp = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     ci = lambda v: ctypes.byref(ctypes.c_int(v))
     cd = lambda v: ctypes.byref(ctypes.c_double(v))
-    common = (dp(xx), dp(yy), ci(nx), ci(ny), dp(a), dp(b), dp(c))
-    tl = threading.local()
+    fwd_fn, adj_fn, mask_fn = L.fsm_uw_ps_lonlat_2d_, L.fsm_o1_jse_lonlat_2d_, L.mask_
+    status, iterations = L.surfatt_last_status, L.surfatt_last_iterations
 
-    def run_block(block):
-        if not hasattr(tl, "T"):
-            tl.T = np.zeros((nx, ny), order="F")
-            tl.Ta = np.zeros((nx, ny), order="F")
-            tl.u = np.zeros((nx, ny), order="F")
+    def prepare(blocks):
+        """Per caller (block of sources): its own T, Ta and scratch arrays and
+        the ctypes arguments of every call, built once outside the timed
+        region (Fortran passes its arrays by reference; building ctypes
+        pointers would hold the GIL inside the measurement)."""
+        out = []
+        for block in blocks:
+            T = np.zeros((nx, ny), order="F")
+            Ta = np.zeros((nx, ny), order="F")
+            u = np.zeros((nx, ny), order="F")
+            common = (dp(xx), dp(yy), ci(nx), ci(ny), dp(a), dp(b), dp(c))
+            calls = []
+            for k in block:
+                d = srcs[k]
+                calls.append(((*common, dp(T), dp(fun), cd(d["x0"]), cd(d["y0"]), dp(u)),
+                              (*common, dp(T), dp(Ta), dp(d["xr"]), dp(d["yr"]), dp(d["sadj"]),
+                               ci(len(d["xr"]))),
+                              (dp(xx), dp(yy), ci(nx), ci(ny), dp(Ta), cd(d["x0"]),
+                               cd(d["y0"]))))
+            out.append((calls, (T, Ta, u)))
+        return out
+
+    def run_block(job):
+        calls, _ = job
         its = [0, 0]
-        for k in block:
-            d = srcs[k]
-            L.fsm_uw_ps_lonlat_2d_(*common, dp(tl.T), dp(fun), cd(d["x0"]), cd(d["y0"]),
-                                   dp(tl.u))
-            if sg.last_status() != sg.OK:
-                raise RuntimeError(f"forward drop-in status {sg.last_status()}")
-            its[0] += sg.last_iterations()
-            L.fsm_o1_jse_lonlat_2d_(*common, dp(tl.T), dp(tl.Ta), dp(d["xr"]), dp(d["yr"]),
-                                    dp(d["sadj"]), ci(len(d["xr"])))
-            if sg.last_status() != sg.OK:
-                raise RuntimeError(f"adjoint drop-in status {sg.last_status()}")
-            its[1] += sg.last_iterations()
-            L.mask_(dp(xx), dp(yy), ci(nx), ci(ny), dp(tl.Ta), cd(d["x0"]), cd(d["y0"]))
+        for fa, aa, ma in calls:
+            fwd_fn(*fa)
+            if status() != sg.OK:
+                raise RuntimeError(f"forward drop-in status {status()}")
+            its[0] += iterations()
+            adj_fn(*aa)
+            if status() != sg.OK:
+                raise RuntimeError(f"adjoint drop-in status {status()}")
+            its[1] += iterations()
+            mask_fn(*ma)
         return its
 
     def timed(nthreads):
-        blocks = _dropin_blocks(len(srcs), nthreads)
+        jobs = prepare(_dropin_blocks(len(srcs), nthreads))
         ts, its = [], [0, 0]
         with ThreadPoolExecutor(max_workers=nthreads) as ex:
             for i in range(args.warmup + args.steps):
                 t0 = time.perf_counter()
-                res = list(ex.map(run_block, blocks))
+                res = list(ex.map(run_block, jobs))
                 t1 = time.perf_counter()
                 if i >= args.warmup:
                     ts.append(t1 - t0)
@@ -1079,7 +1100,8 @@ def run_dropin(args):
                                "field its previous call returned) are not copied again, so "
                                "h2d_bytes_per_step counts the arrays passed, not the bytes "
                                "moved",
-                       "l2": "no flush: consecutive calls reuse their thread's device copies"},
+                       "l2": "no flush: consecutive calls reuse their thread's device copies",
+                       "harness": "Python threads, GIL switch interval 10 us"},
             "clocks": ck,
             "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": s_many * 1e3,
@@ -1088,13 +1110,15 @@ def run_dropin(args):
             # per source: forward, adjoint and mask kernels (the grid's
             # precompute runs only when a thread's model changes)
             "gpu_launches": 3 * len(srcs) * args.steps,
-            "roofline": {"bound": "fp64", "bound_note": "one 256-thread block per call (one "
-                         "SM); achieved = reference-formulation FP64 flops of the timed calls "
-                         "over wall time, copies included",
+            "roofline": {"bound": "fp64", "bound_note": "a call is one solve: the forward "
+                         "on a cluster of six blocks (six SMs, one share of the update's cases "
+                         "each), the adjoint on one block; achieved = reference-formulation FP64 "
+                         "flops of the timed calls over wall time, copies included, against the "
+                         "whole GPU's FP64 peak",
                          "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": ach / fp64_peak, "traffic": None,
                          "peak_source": "surfatt_measure_peaks (FP64 FMA chains), this run",
-                         "kernel": "k_uw_single + k_jse_single"},
+                         "kernel": "k_uw_cluster + k_jse_single"},
             "iterations": {"fwd_per_source": its[0] / args.steps / len(srcs),
                            "adj_per_source": its[1] / args.steps / len(srcs)},
             "cpu_baseline": cpu, "parity": parity,

@@ -453,8 +453,8 @@ __device__ inline void weno_sweeps(const PeriodDev& P, const FwdWs& W, SolveShar
 // ---------------------------------------------------------------------------
 // Single-solve kernels (one block) for the drop-in symbols
 // ---------------------------------------------------------------------------
-// (+ four N-cell arrays: the cluster forward's per-block iteration-start tau)
-long long single_ws_doubles(long long N) { return batch_fp64_ws_doubles(N) + 4 * N; }
+// (+ one N-cell array: the cluster forward's iteration-start tau)
+long long single_ws_doubles(long long N) { return batch_fp64_ws_doubles(N) + N; }
 
 __global__ void __launch_bounds__(256) k_uw_single(PeriodDev P, double x0, double y0, double* ws,
                                                    double* T, int* si) {
@@ -476,29 +476,94 @@ void launch_uw_single(const PeriodDev& P, double x0, double y0, double* ws, doub
   k_uw_single<<<1, 256, 0, st>>>(P, x0, y0, ws, T, si);
 }
 
+// Blocks of the cluster forward: blocks 0 - 3 evaluate the two-sided cases
+// 0 - 3 of the update, block 4 the one-sided cases west and east, block 5
+// south and north (about 35, 14 and 14 FP64 instructions a cell).
+constexpr int kUwRanks = 6;
+
+// What one thread needs from global memory for its cell of one diagonal:
+// the cell and its block's constants, loaded while the cluster barrier of
+// the previous diagonal completes.
+struct UwPre {
+  bool on;  // a cell of this diagonal, not in the frozen box
+  int i, j;
+  size_t k;
+  double cx, cy, t0, old;
+  double ea, bx, by, iea, a, b, c, f2;  // two-sided blocks
+  double ip0, ip1, t0nb0, t0nb1, dis;   // one-sided blocks (faces f0, f0 + 1)
+};
+
+__device__ __forceinline__ void uw_fetch(const PeriodDev& P, const double* __restrict__ K,
+                                         const double* __restrict__ T0,
+                                         const double* __restrict__ told, const Box& box,
+                                         int rank, int s, int d, UwPre& p) {
+  const int nx = P.nx, ny = P.ny;
+  SweepGeom g;
+  g.ilo = 0; g.ihi = nx - 1; g.jlo = 0; g.jhi = ny - 1;
+  sweep_dirs(s, g.xdir, g.ydir);
+  const int v = g.vmin(d) + (int)threadIdx.x;
+  p.on = v <= g.vmax(d);
+  if (!p.on) return;
+  g.cell(d, v, p.i, p.j);
+  p.on = !box.has(p.i, p.j);
+  if (!p.on) return;
+  const size_t k = (size_t)p.i + (size_t)nx * p.j;
+  p.k = k;
+  const double* Kc = K + k * (size_t)KC_COUNT;
+  p.cx = Kc[KC_CX];
+  p.cy = Kc[KC_CY];
+  p.t0 = T0[k];
+  p.old = (s == 3 && rank == 0) ? told[k] : 0.0;
+  if (rank < 4) {
+    p.ea = Kc[KC_EA + rank];
+    p.bx = Kc[KC_BX + rank];
+    p.by = Kc[KC_BY + rank];
+    p.iea = Kc[KC_IEA + rank];
+    p.a = P.a[k];
+    p.b = P.b[k];
+    p.c = P.c[k];
+    p.f2 = P.f2[k];
+  } else {
+    const int f0 = rank == 4 ? 0 : 2;
+    const bool lo = f0 == 0 ? p.i > 0 : p.j > 0, hi = f0 == 0 ? p.i < nx - 1 : p.j < ny - 1;
+    p.ip0 = Kc[KC_IPXM + f0];
+    p.ip1 = Kc[KC_IPXM + f0 + 1];
+    p.t0nb0 = lo ? T0[uw_nb(f0, k, nx)] : 0.0;
+    p.t0nb1 = hi ? T0[uw_nb(f0 + 1, k, nx)] : 0.0;
+    p.dis = f0 == 0 ? P.disx[k] : P.disy[k];
+  }
+}
+
+// Order-preserving integer key of a double (signed compare = numeric
+// compare; -0 below +0): the phase-2 minimum runs on the integer pipe.
+__device__ __forceinline__ long long uw_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
 // One plain FP64 forward solve on a cluster of kUwRanks blocks, one per SM.
 //
 // A call of the drop-in is one solve, a chain of anti-diagonal steps, and an
 // FP64 warp instruction holds a scheduler for the same time whatever the
 // number of its active lanes: one block's step costs the whole visit's FP64
 // instruction sequence however the diagonal's cells are spread over warps.
-// Here the visit itself is spread: block r evaluates only case r of the
-// update (two-sided case r and one-sided case r, a quarter of the FP64
-// instructions) for every cell of the diagonal and writes its candidate
-// minimum into every block's shared memory; after one cluster barrier each
-// block takes min(tau, the four candidates) -- the same minimum over the
-// same roots as uw_update -- into its own shared copy of tau.  Every block
-// therefore holds the same field, accumulates the same convergence sums
-// (same thread-to-cell map and block reduction as k_uw_single) and takes
-// the same decisions, so all blocks run the same number of barriers.
+// Here the visit itself is spread: each block evaluates only its cases of
+// the update (one two-sided case, or two one-sided cases) for every cell of
+// the diagonal and writes its candidate minimum into every block's shared
+// memory; after one cluster barrier each block takes min(tau, the six
+// candidates) -- the same minimum over the same roots as uw_update -- into
+// its own shared copy of tau.  Every block therefore holds the same field;
+// block 0 accumulates the convergence sums and broadcasts its decision, so
+// all blocks run the same number of barriers.
 // Candidates are double-buffered by diagonal parity: a block writes
 // diagonal d+1's only after the barrier of diagonal d, which every block
-// reaches after reading diagonal d-1's.  The cell constants, T0 and the
-// setup's outputs stay in global memory (the setup is shared out by
-// chunks); the per-block iteration-start values in ws beyond the single
-// solve's layout.  Results equal k_uw_single's.
-constexpr int kUwRanks = 4;
-
+// reaches after reading diagonal d-1's.  Between its arrival at a barrier
+// and the wait, a thread loads the next diagonal's cell constants (global
+// memory, L2-resident), so their latency hides behind the barrier.  The
+// setup is shared out by chunks; block 0's iteration-start values live in
+// ws beyond the single solve's layout.  One cell per thread and diagonal
+// (min(nx, ny) <= 256 = blockDim.x); block 0 adds the convergence sums in
+// k_uw_single's thread order, so the results equal k_uw_single's.
 __global__ void __launch_bounds__(256) k_uw_cluster(PeriodDev P, double x0, double y0, double* ws,
                                                     double* T, int* si) {
   namespace cg = cooperative_groups;
@@ -518,66 +583,80 @@ __global__ void __launch_bounds__(256) k_uw_cluster(PeriodDev P, double x0, doub
   double* tau = uw_dyn;
   const int maxd = nx < ny ? nx : ny;
   double* cand = uw_dyn + N;  // [2][kUwRanks][maxd]
-  double* told = ws + fp64_slot_doubles((long long)N) + (size_t)rank * N;
+  double* told = ws + fp64_slot_doubles((long long)N);  // block 0's
   for (size_t k = threadIdx.x; k < N; k += blockDim.x) tau[k] = L.fw.tau[k];
   __syncthreads();
   const double* __restrict__ K = L.fw.K;
   const double* __restrict__ T0 = L.fw.T0;
   const Box box = sh.box;
   const double inf = __longlong_as_double(0x7ff0000000000000LL);
+  const int nd = nx + ny - 1;  // diagonals per sweep
+  UwPre cur, nxt;
+  uw_fetch(P, K, T0, told, box, rank, 0, 0, cur);
   int iter, status = ST_NOT_CONVERGED;
   for (iter = 1; iter <= MAXITER_UW; ++iter) {
     double l1 = 0.0, linf = 0.0;
     for (int s = 0; s < 4; ++s) {
-      SweepGeom g;
-      g.ilo = 0; g.ihi = nx - 1; g.jlo = 0; g.jhi = ny - 1;
-      sweep_dirs(s, g.xdir, g.ydir);
-      const int nd = g.ndiag();
       for (int d = 0; d < nd; ++d) {
-        const int vlo = g.vmin(d), vhi = g.vmax(d);
         double* const cb = cand + (size_t)(d & 1) * kUwRanks * maxd;
-        for (int v = vlo + (int)threadIdx.x; v <= vhi; v += blockDim.x) {
-          int i, j;
-          g.cell(d, v, i, j);
+        const int slot = (int)threadIdx.x;  // v - vlo
+        if (cur.on) {
+          const size_t k = cur.k;
+          const bool hw = cur.i > 0, he = cur.i < nx - 1, hs = cur.j > 0, hn = cur.j < ny - 1;
+          const double tw = hw ? tau[k - 1] : 0.0, te = he ? tau[k + 1] : 0.0;
+          const double ts = hs ? tau[k - nx] : 0.0, tn = hn ? tau[k + nx] : 0.0;
+          const double qw = -(cur.cx * tw), qe = cur.cx * te, qs = -(cur.cy * ts),
+                       qn = cur.cy * tn;
           double m = inf;
-          if (!box.has(i, j)) {
-            const size_t k = (size_t)i + (size_t)nx * j;
-            m = uw_case(rank, K, k, i, j, nx, ny, tau, T0, P.a[k], P.b[k], P.c[k], P.f2[k],
-                        P.disx[k], P.disy[k]);
+          if (rank < 4) {
+            uw_two_sided_v(rank, cur.ea, cur.bx, cur.by, cur.iea, hw, he, hs, hn, qw, qe, qs, qn,
+                           cur.a, cur.b, cur.c, cur.f2, m);
+          } else {
+            const int f0 = rank == 4 ? 0 : 2;
+            uw_one_sided_v(f0, cur.ip0, cur.t0nb0, cur.dis, hw, he, hs, hn, qw, qe, qs, qn, tw,
+                           te, ts, tn, cur.t0, m);
+            uw_one_sided_v(f0 + 1, cur.ip1, cur.t0nb1, cur.dis, hw, he, hs, hn, qw, qe, qs, qn,
+                           tw, te, ts, tn, cur.t0, m);
           }
-          const int slot = rank * maxd + (v - vlo);
 #pragma unroll
-          for (int q = 0; q < kUwRanks; ++q) cl.map_shared_rank(cb, q)[slot] = m;
+          for (int q = 0; q < kUwRanks; ++q)
+            cl.map_shared_rank(cb, q)[rank * maxd + slot] = m;
         }
-        cl.sync();
-        for (int v = vlo + (int)threadIdx.x; v <= vhi; v += blockDim.x) {
-          int i, j;
-          g.cell(d, v, i, j);
-          if (box.has(i, j)) continue;
-          const size_t k = (size_t)i + (size_t)nx * j;
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+        {  // the next diagonal (of the next sweep, or of the next iteration's first)
+          int s2 = s, d2 = d + 1;
+          if (d2 == nd) { d2 = 0; s2 = s + 1 < 4 ? s + 1 : 0; }
+          uw_fetch(P, K, T0, told, box, rank, s2, d2, nxt);
+        }
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+        if (cur.on) {
+          const size_t k = cur.k;
           const double tb = tau[k];
-          if (s == 0) told[k] = tb;
+          if (s == 0 && rank == 0) told[k] = tb;
+          // min(tb, candidates): no candidate is NaN (each was taken by a
+          // comparison), so the integer keys order them as the values
+          long long best = uw_key(tb);
           double tn = tb;
 #pragma unroll
           for (int q = 0; q < kUwRanks; ++q) {
-            const double mq = cb[q * maxd + (v - vlo)];
-            if (mq < tn) tn = mq;
+            const double mq = cb[q * maxd + slot];
+            const long long kq = uw_key(mq);
+            if (kq < best) { best = kq; tn = mq; }
           }
           tau[k] = tn;
-          if (s == 3) {
-            const double dd = fabs(tn - told[k]) * T0[k];
+          if (s == 3 && rank == 0) {
+            const double dd = fabs(tn - cur.old) * cur.t0;
             l1 += dd;
             linf = fmax(linf, dd);
           }
         }
         __syncthreads();
+        cur = nxt;
       }
     }
     block_sum_max(l1, linf, sh.red);
     l1 = l1 / (double)nx / (double)ny;
-    // Every block reaches the same decision from the same field; block 0's
-    // is nevertheless the one all follow, so the blocks' barrier counts can
-    // never differ.
+    // block 0's decision, followed by every block
     if (rank == 0 && threadIdx.x == 0) {
       const int conv = fabs(l1) < TOL_UW && linf < TOL_UW;
 #pragma unroll
@@ -620,7 +699,7 @@ bool launch_uw_cluster(const PeriodDev& P, double x0, double y0, double* ws, dou
     return lim;
   }();
   const size_t smem = uw_cluster_smem(P.nx, P.ny);
-  if (smem > max_smem) return false;
+  if (smem > max_smem || (P.nx < P.ny ? P.nx : P.ny) > 256) return false;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kUwRanks);
   cfg.blockDim = dim3(256);
@@ -661,10 +740,93 @@ void launch_weno_single(const PeriodDev& P, double x0, double y0, int multi, dou
   k_weno_single<<<1, 256, 0, st>>>(P, x0, y0, multi, ws, T, si);
 }
 
+// One adjoint field swept with the field and its iteration-start copy in
+// shared memory (dynamic, 2N doubles) and each thread's next cell constants
+// loaded before the block barrier of the current diagonal, so that a step
+// is the visit's five FP64 operations on shared operands rather than the
+// latency of its global loads.  Same arithmetic, visit order, thread-to-cell
+// map and reductions as adj_sweeps with one field; one cell per thread and
+// diagonal (min(nx, ny) - 2 <= blockDim.x).
+struct JsePre {
+  bool on;
+  size_t k;
+  double ww, we, ws, wn, id, dl;
+};
+
+__device__ __forceinline__ void jse_fetch(const PeriodDev& P, const double* __restrict__ K,
+                                          const double* __restrict__ delta, int s, int d,
+                                          JsePre& p) {
+  const int nx = P.nx, ny = P.ny;
+  SweepGeom g;
+  g.ilo = 1; g.ihi = nx - 2; g.jlo = 1; g.jhi = ny - 2;
+  sweep_dirs(s, g.xdir, g.ydir);
+  const int v = g.vmin(d) + (int)threadIdx.x;
+  p.on = v <= g.vmax(d);
+  if (!p.on) return;
+  int i, j;
+  g.cell(d, v, i, j);
+  const size_t k = (size_t)i + (size_t)nx * j;
+  p.k = k;
+  const double* Kr = K + k * (size_t)KA_COUNT;
+  p.ww = Kr[KA_WW];
+  p.we = Kr[KA_WE];
+  p.ws = Kr[KA_WS];
+  p.wn = Kr[KA_WN];
+  p.id = Kr[KA_ID];
+  p.dl = delta[k];
+}
+
+__device__ inline void adj_sweeps_shared(const PeriodDev& P, const AdjWs& W, double* ta,
+                                         double* old, SolveShared& sh, int* its, int* sts) {
+  const int nx = P.nx, ny = P.ny;
+  const size_t N = (size_t)nx * ny;
+  const double* __restrict__ K = W.K;
+  const double* __restrict__ delta = W.delta[0];
+  for (size_t k = threadIdx.x; k < N; k += blockDim.x) ta[k] = W.Ta[0][k];
+  __syncthreads();
+  const int nd = (nx - 2) + (ny - 2) - 1;
+  JsePre cur, nxt;
+  jse_fetch(P, K, delta, 0, 0, cur);
+  int iter, status = ST_NOT_CONVERGED;
+  for (iter = 1; iter <= MAXITER_JSE; ++iter) {
+    double l1 = 0, lm = 0;
+    for (int s = 0; s < 4; ++s) {
+      for (int d = 0; d < nd; ++d) {
+        if (cur.on) {
+          const size_t k = cur.k;
+          const double before = ta[k];
+          if (s == 0) old[k] = before;
+          const double nv = cur.dl * cur.id + cur.ww * ta[k - 1] + cur.we * ta[k + 1] +
+                            cur.ws * ta[k - nx] + cur.wn * ta[k + nx];
+          ta[k] = nv;
+          if (s == 3) {
+            const double dd = fabs(nv - old[k]);
+            l1 += dd;
+            lm = fmax(lm, dd);
+          }
+        }
+        int s2 = s, d2 = d + 1;
+        if (d2 == nd) { d2 = 0; s2 = s + 1 < 4 ? s + 1 : 0; }
+        jse_fetch(P, K, delta, s2, d2, nxt);
+        __syncthreads();
+        cur = nxt;
+      }
+    }
+    block_sum_max(l1, lm, sh.red);
+    l1 = l1 / (double)(nx * ny);
+    if (fabs(l1) < TOL_JSE && lm < TOL_JSE) { status = ST_OK; break; }
+  }
+  its[0] = iter > MAXITER_JSE ? MAXITER_JSE : iter;
+  sts[0] = status;
+  for (size_t k = threadIdx.x; k < N; k += blockDim.x) W.Ta[0][k] = ta[k];
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(256) k_jse_single(PeriodDev P, const double* T,
                                                     const double* recx, const double* recy,
                                                     const double* sadj, int nrec, double* ws,
-                                                    double* Ta, int* si) {
+                                                    double* Ta, int* si, int shared_field) {
+  extern __shared__ double jse_dyn[];
   __shared__ SolveShared sh;
   const size_t N = (size_t)P.nx * P.ny;
   SolveLayout L = carve(ws, N);
@@ -680,14 +842,33 @@ __global__ void __launch_bounds__(256) k_jse_single(PeriodDev P, const double* T
   }
   adj_setup(P, L.aw, 1);
   int its[2] = {0, 0}, sts[2] = {ST_OK, ST_OK};
-  adj_sweeps(P, L.aw, 1, sh, its, sts);
+  if (shared_field)
+    adj_sweeps_shared(P, L.aw, jse_dyn, jse_dyn + N, sh, its, sts);
+  else
+    adj_sweeps(P, L.aw, 1, sh, its, sts);
   if (threadIdx.x == 0) { si[0] = sts[0]; si[1] = its[0]; }
 }
 
 void launch_jse_single(const PeriodDev& P, const double* T, const double* recx,
                        const double* recy, const double* sadj, int nrec, double* ws, double* Ta,
                        int* si, cudaStream_t st) {
-  k_jse_single<<<1, 256, 0, st>>>(P, T, recx, recy, sadj, nrec, ws, Ta, si);
+  static const size_t max_smem = [] {
+    int dev = 0, opt = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&opt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t lim = (size_t)opt - sizeof(SolveShared) - 1024;
+    if (cudaFuncSetAttribute(k_jse_single, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)lim) != cudaSuccess) {
+      cudaGetLastError();
+      return (size_t)0;
+    }
+    return lim;
+  }();
+  // the field and its iteration-start copy in shared memory when they fit
+  const size_t smem = (size_t)2 * P.nx * P.ny * sizeof(double);
+  const bool shared = smem <= max_smem && (P.nx < P.ny ? P.nx : P.ny) - 2 <= 256;
+  k_jse_single<<<1, 256, shared ? smem : 0, st>>>(P, T, recx, recy, sadj, nrec, ws, Ta, si,
+                                                   shared ? 1 : 0);
 }
 
 __global__ void k_mask_single(PeriodDev P, double* tab, double x0, double y0) {

@@ -207,23 +207,22 @@ __device__ inline void fwd_setup(const PeriodDev& P, double x0, double y0, doubl
 // Two-sided case cs of the plain first-order upwind update (:904-993):
 // lowers t to each causal root of the case's quadratic.  q* are the scaled
 // neighbour values (qw = -cx*tw, qe = cx*te, qs = -cy*ts, qn = cy*tn).
-__device__ __forceinline__ void uw_two_sided(int cs, const double* __restrict__ K, bool hw,
-                                             bool he, bool hs, bool hn, double qw, double qe,
-                                             double qs, double qn, double a, double b, double c,
-                                             double f2, double& t) {
+// (the case's constants ea, bx, by, 1/ea given: K[KC_EA + cs], ...)
+__device__ __forceinline__ void uw_two_sided_v(int cs, double ea, double bx, double by,
+                                               double iea, bool hw, bool he, bool hs, bool hn,
+                                               double qw, double qe, double qs, double qn,
+                                               double a, double b, double c, double f2,
+                                               double& t) {
   const bool ok = (cs < 2 ? hw : he) && ((cs == 0 || cs == 2) ? hs : hn);
   if (!ok) return;
   const double qx = cs < 2 ? qw : qe;
   const double qy = (cs == 0 || cs == 2) ? qs : qn;
-  const double ea = K[KC_EA + cs];
-  const double bx = K[KC_BX + cs], by = K[KC_BY + cs];
   const double Cx = a * qx - c * qy;
   const double Cy = b * qy - c * qx;
   const double ec = qx * Cx + qy * Cy - f2;
   const double hb = bx * qx + by * qy;
   const double del = hb * hb - ea * ec;
   if (del >= 0) {
-    const double iea = K[KC_IEA + cs];
     const double s = sqrt(del);
     const double r1 = (-hb + s) * iea, r2 = (-hb - s) * iea;
     const double x1 = bx * r1 + Cx, y1 = by * r1 + Cy;
@@ -236,8 +235,40 @@ __device__ __forceinline__ void uw_two_sided(int cs, const double* __restrict__ 
   }
 }
 
+__device__ __forceinline__ void uw_two_sided(int cs, const double* __restrict__ K, bool hw,
+                                             bool he, bool hs, bool hn, double qw, double qe,
+                                             double qs, double qn, double a, double b, double c,
+                                             double f2, double& t) {
+  const bool ok = (cs < 2 ? hw : he) && ((cs == 0 || cs == 2) ? hs : hn);
+  if (!ok) return;
+  uw_two_sided_v(cs, K[KC_EA + cs], K[KC_BX + cs], K[KC_BY + cs], K[KC_IEA + cs], hw, he, hs, hn,
+                 qw, qe, qs, qn, a, b, c, f2, t);
+}
+
+// Neighbour of cell k across face cs (0 west, 1 east, 2 south, 3 north).
+__device__ __forceinline__ size_t uw_nb(int cs, size_t k, int nx) {
+  return cs == 0 ? k - 1 : cs == 1 ? k + 1 : cs == 2 ? k - nx : k + nx;
+}
+
 // One-sided case cs (0 west, 1 east, 2 south, 3 north) of the same update
-// (:996-1075): lowers t to each admissible root along one axis.
+// (:996-1075): lowers t to each admissible root along one axis.  (ip =
+// K[KC_IPXM + cs], t0nb = T0 of the neighbour across face cs, dis = disx for
+// cs < 2 and disy otherwise.)
+__device__ __forceinline__ void uw_one_sided_v(int cs, double ip, double t0nb, double dis,
+                                               bool hw, bool he, bool hs, bool hn, double qw,
+                                               double qe, double qs, double qn, double tw,
+                                               double te, double ts, double tn, double t0,
+                                               double& t) {
+  const bool ok = cs == 0 ? hw : cs == 1 ? he : cs == 2 ? hs : hn;
+  if (!ok) return;
+  const double q = cs == 0 ? qw : cs == 1 ? qe : cs == 2 ? qs : qn;
+  const double tnb = cs == 0 ? tw : cs == 1 ? te : cs == 2 ? ts : tn;
+  const double lim = tnb * t0nb, half = tnb * 0.5;
+  const double r1 = (dis - q) * ip, r2 = (-dis - q) * ip;
+  if (r1 * t0 >= lim && r1 > half && r1 < t) t = r1;
+  if (r2 * t0 >= lim && r2 > half && r2 < t) t = r2;
+}
+
 __device__ __forceinline__ void uw_one_sided(int cs, const double* __restrict__ K, size_t k,
                                              int nx, const double* __restrict__ T0, bool hw,
                                              bool he, bool hs, bool hn, double qw, double qe,
@@ -246,15 +277,8 @@ __device__ __forceinline__ void uw_one_sided(int cs, const double* __restrict__ 
                                              double t0, double& t) {
   const bool ok = cs == 0 ? hw : cs == 1 ? he : cs == 2 ? hs : hn;
   if (!ok) return;
-  const double q = cs == 0 ? qw : cs == 1 ? qe : cs == 2 ? qs : qn;
-  const double tnb = cs == 0 ? tw : cs == 1 ? te : cs == 2 ? ts : tn;
-  const size_t nb = cs == 0 ? k - 1 : cs == 1 ? k + 1 : cs == 2 ? k - nx : k + nx;
-  const double dis = cs < 2 ? disx : disy;
-  const double ip = K[KC_IPXM + cs];
-  const double lim = tnb * T0[nb], half = tnb * 0.5;
-  const double r1 = (dis - q) * ip, r2 = (-dis - q) * ip;
-  if (r1 * t0 >= lim && r1 > half && r1 < t) t = r1;
-  if (r2 * t0 >= lim && r2 > half && r2 < t) t = r2;
+  uw_one_sided_v(cs, K[KC_IPXM + cs], T0[uw_nb(cs, k, nx)], cs < 2 ? disx : disy, hw, he, hs, hn,
+                 qw, qe, qs, qn, tw, te, ts, tn, t0, t);
 }
 
 // One visit of cell k by the plain first-order upwind update (:904-1079):
