@@ -952,7 +952,7 @@ def run_dropin(args):
     out: `value` and `e2e` are the same measurement."""
     import ctypes
     import multiprocessing as mp
-    from concurrent.futures import ThreadPoolExecutor
+    import threading
     import torch
     import surfatt_gb300 as sg
     dist, rank, world, local = _dist()
@@ -1023,16 +1023,44 @@ def run_dropin(args):
         return its
 
     def timed(nthreads):
+        """One persistent thread per caller, each owning its block of sources
+        for the whole run (as an MPI rank owns its sources), started and
+        joined every step by two barriers; a step lasts from the start
+        barrier until the last caller's last call returns."""
         jobs = prepare(_dropin_blocks(len(srcs), nthreads))
+        nstep = args.warmup + args.steps
+        go = threading.Barrier(nthreads + 1)
+        done = threading.Barrier(nthreads + 1)
+        res = [[None] * nthreads for _ in range(nstep)]
+        err = []
+
+        def caller(r):
+            for i in range(nstep):
+                go.wait()
+                try:
+                    res[i][r] = run_block(jobs[r])
+                except Exception as e:  # reported after the step
+                    err.append(e)
+                    res[i][r] = [0, 0]
+                done.wait()
+
+        threads = [threading.Thread(target=caller, args=(r,), daemon=True)
+                   for r in range(nthreads)]
+        for t in threads:
+            t.start()
         ts, its = [], [0, 0]
-        with ThreadPoolExecutor(max_workers=nthreads) as ex:
-            for i in range(args.warmup + args.steps):
-                t0 = time.perf_counter()
-                res = list(ex.map(run_block, jobs))
-                t1 = time.perf_counter()
-                if i >= args.warmup:
-                    ts.append(t1 - t0)
-                    its = [its[0] + sum(r[0] for r in res), its[1] + sum(r[1] for r in res)]
+        for i in range(nstep):
+            go.wait()
+            t0 = time.perf_counter()
+            done.wait()
+            t1 = time.perf_counter()
+            if err:
+                raise err[0]
+            if i >= args.warmup:
+                ts.append(t1 - t0)
+                its = [its[0] + sum(r[0] for r in res[i]), its[1] + sum(r[1] for r in res[i])]
+        for t in threads:
+            t.join()
         return statistics.mean(ts), its
 
     clocks = Clocks(local)
@@ -1088,8 +1116,10 @@ def run_dropin(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "config1 through the drop-ins: 81x81, 25 sources x 24 "
                                    "receivers, 2-D mode (one adjoint per source)",
-                       "callers": ncores, "caller_kind": "host threads (one per core, as "
-                       "the reference's MPI ranks), contiguous source blocks",
+                       "callers": ncores, "caller_kind": "persistent host threads (one "
+                       "per core, as the reference's MPI ranks), each owning a contiguous "
+                       "block of sources; a step runs from a start barrier to the last "
+                       "caller's last call",
                        "single_caller": {"value": len(srcs) / s_one, "unit": "sources/s",
                                          "ms_per_step": s_one * 1e3},
                        "note": "every call takes host arrays and returns its result in "

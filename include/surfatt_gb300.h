@@ -446,8 +446,9 @@ surfatt_status_t surfatt_engine_launch_config(surfatt_engine_t* engine, int* gri
  * row-per-lane kernel's variants -- 0 / 1: cell constants loaded a step
  * ahead, 8 resident warps per SM, solves cut into work items / whole; 2 / 3:
  * cell constants loaded at the visit, 12 / 8 warps, items / whole; 4 / 5, on
- * grids of more than 128 rows only: as 0 / 1 with the tall grids swept by
- * one warp in 128-row strips instead of a team of warps (same results) --
+ * grids of more than 128 rows only: the tall grids swept by one warp in
+ * 128-row strips instead of a team of warps (same results), items (the
+ * whole forward, then one per adjoint field) / whole solves --
  * and the block-per-solve kernel) with one warm-up and one timed evaluation each,
  * and use the fastest for later runs of this precision until the next load.
  * Returns the chosen kernel (0 FP64, 1 FP32 block, 2 FP32 warp), its variant

@@ -72,6 +72,7 @@ struct BatchArgs {
   size_t smem_bytes;       // FP32 kernel: dynamic shared memory per block
   unsigned long long* phase_cycles = nullptr;  // optional: SM cycles per solve phase, summed
   int items = 1;           // FP32 warp kernel: items per solve (1: whole solves)
+  int fwd_items = 0;       // FP32 warp kernel with items: forward items (0: the default)
   int* sstate = nullptr;   // FP32 warp kernel with items > 1: per-solve state records
   // Test hooks of the bounded item wait (FP32 warp kernel with items; off by
   // default): the first item of solve hold_solve (>= 0) is skipped without
@@ -137,6 +138,9 @@ bool fp32w_variant_strips(int variant);
 // Threads per block of the row kernel for `bands` bands.
 int fp32w_block(int bands, int variant);
 int fp32w_items_for_mode(int mode);
+// Forward items per solve of a variant with items (the rest: one item per
+// adjoint field): the strip variant keeps each forward whole.
+int fp32w_fwd_items(int variant);
 constexpr int kSolveStateInts = 5;
 // Per-solve state record (ints) of a solve cut into items: items done (-1:
 // failed), forward iterations, forward status, running status, adjoint

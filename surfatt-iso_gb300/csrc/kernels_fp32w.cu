@@ -813,8 +813,8 @@ constexpr int kSplitIter = 2;
 constexpr int kFwdItems = 3;
 
 // Items per solve for `mode` when solves are cut.
-__host__ __device__ inline int w_items_for_mode(int mode) {
-  return kFwdItems + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
+__host__ __device__ inline int w_items_for_mode(int mode, int fwd_items = kFwdItems) {
+  return fwd_items + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
 }
 
 template <int MB, int PF, int MINW, int NW, bool ST>
@@ -911,7 +911,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
     const int nf = A.mode == 3 ? 2 : 1;
-    const int nitems_mode = w_items_for_mode(A.mode);
+    const int nfwd = cut && A.fwd_items > 0 ? A.fwd_items : kFwdItems;  // forward items
+    const int nitems_mode = w_items_for_mode(A.mode, nfwd);
     const int first = cut ? item : 0;                 // first item done here
     const int lastit = cut ? item : nitems_mode - 1;  // last item done here
     int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0;
@@ -958,15 +959,15 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
       w_t0<NW>(P, x0, y0, w, V, T);
       mark(PH_SETUP);
     }
-    if (first < kFwdItems && (first == 0 || (fst != ST_OK && fit < MAXITER_UW))) {
+    if (first < nfwd && (first == 0 || (fst != ST_OK && fit < MAXITER_UW))) {
       const int it0 = first == 0 ? 1 : fit + 1;
-      const int it1 = (cut && first < kFwdItems - 1) ? (first + 1) * kSplitIter : MAXITER_UW;
+      const int it1 = (cut && first < nfwd - 1) ? (first + 1) * kSplitIter : MAXITER_UW;
       int n = 0;
       w_fwd_sweeps<MB, PF, NW, ST>(P, V, w, T, it0, it1, &fst, &n);
       fit = n;
       mark(PH_FWD);
     }
-    if (cut && first < kFwdItems - 1) {
+    if (cut && first < nfwd - 1) {
       if (T.tid == 0) {
         ss[SS_FIT] = fit;
         ss[SS_FST] = fst;
@@ -974,7 +975,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
       finish_item(first + 1);
       continue;
     }
-    if (first <= kFwdItems - 1) {
+    if (first <= nfwd - 1) {
       if (A.fwd_updates && T.tid == 0) {
         const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
         A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
@@ -990,13 +991,13 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
           ss[SS_FIT] = fit;
           ss[SS_ST] = st;
         }
-        finish_item(kFwdItems);
+        finish_item(nfwd);
         continue;
       }
     }
     // adjoint field(s) f0 .. f1
-    const int f0 = cut ? (first > kFwdItems ? first - kFwdItems : 0) : 0;
-    const int f1 = A.mode >= 2 ? (cut ? lastit - kFwdItems : nf - 1) : -1;
+    const int f0 = cut ? (first > nfwd ? first - nfwd : 0) : 0;
+    const int f1 = A.mode >= 2 ? (cut ? lastit - nfwd : nf - 1) : -1;
     for (int f = f0; f <= f1; ++f) {
       int ast = ST_OK, n = 0;
       w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(P, V, f ? V.src[1] : V.src[0], T,
@@ -1035,14 +1036,17 @@ int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 //   1: the same, whole solves
 //   2: cell constants loaded at the visit, 12 warps per SM, items
 //   3: cell constants loaded at the visit, 8 warps per SM, whole solves
-//   4: as 0, grids of more than 128 rows swept in strips by one warp
-//   5: as 1, the same strips
+//   4: grids of more than 128 rows swept in strips by one warp; items: the
+//      whole forward, then one item per adjoint field, one resident warp
+//      per solve
+//   5: the same strips, whole solves
 // On grids of at most 128 rows variants 4 and 5 are variants 0 and 1.
 constexpr int kFp32wVariants = 6;
 int fp32w_variant_count() { return kFp32wVariants; }
 bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2 || variant == 4; }
 bool fp32w_variant_strips(int variant) { return variant >= 4; }
 int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
+int fp32w_fwd_items(int variant) { return fp32w_variant_strips(variant) ? 1 : kFwdItems; }
 
 template <int MB, int PF, int MINW, int NW, bool ST>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {

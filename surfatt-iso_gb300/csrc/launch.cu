@@ -94,8 +94,15 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.ws_doubles = batch_fp32_ws_doubles(sh.max_cells);
   }
   if (p.per_sm < 1) p.per_sm = 1;
+  // Resident units: one per work item, except for the strip variants' items,
+  // which get one warp per solve: a solve's items then run as soon as its
+  // previous item ends (its two adjoint fields side by side), and no warp
+  // holds a slot waiting for a forward another warp has only begun -- slots
+  // the other team classes' launches need.
   const int units_per_solve =
-      p.cut ? (p.kind == KK_FP64 ? kFp64Items : fp32w_items_for_mode(3)) : 1;
+      p.cut ? (p.kind == KK_FP64 ? kFp64Items
+                                 : (fp32w_variant_strips(p.pf) ? 1 : fp32w_items_for_mode(3)))
+            : 1;
   auto grid_for = [&](int per_sm, int nsolve) {
     int g = nsm * std::max(1, per_sm);
     if (max_grid > 0) g = std::min(g, max_grid);
@@ -193,7 +200,8 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   A.sstate = nullptr;
   if (plan.kind == KK_FP32_WARP && plan.cut) {
     const long long n = std::max(1, sh.nsolve);
-    A.items = fp32w_items_for_mode(mode);
+    A.fwd_items = fp32w_fwd_items(plan.pf);
+    A.items = A.fwd_items + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
     A.sstate = reinterpret_cast<int*>(ws + n * plan.ws_doubles);
     if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
       return -ST_CUDA_ERROR;
