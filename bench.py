@@ -29,6 +29,13 @@ import time
 
 import numpy as np
 
+# Up to 32 hardware work queues for the process's streams (CUDA's default is
+# 8): the drop-in workload's 16 caller threads each have their own stream,
+# and two streams sharing a queue serialise their launches (a short launch
+# waits behind another thread's forward solve).  Read when the CUDA context
+# is created, so set before anything initialises CUDA.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "surfatt-iso_gb300"))
 

@@ -87,6 +87,7 @@ struct PeriodBufs {
 struct ThreadCtx {
   bool init = false;
   cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;  // blocking-sync event: the end of a call's work
   PeriodBufs pb;
   DBuf ws, T, Ta, rx, ry, sa, out, si;
   DBuf sm_lon, sm_lat, sm_in, sm_out, sm_tab, sm_nyw, sm_per;  // kernel smoothing
@@ -120,14 +121,25 @@ struct ThreadCtx {
       d->release();
     if (si_host) cudaFreeHost(si_host);
     if (hst) cudaFreeHost(hst);
+    if (done) cudaEventDestroy(done);
     if (st) cudaStreamDestroy(st);
   }
   int setup() {
     if (init) return SURFATT_OK;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SURFATT_CUDA_ERROR;
     if (cudaMallocHost(&si_host, 4 * sizeof(int)) != cudaSuccess) return SURFATT_CUDA_ERROR;
+    if (cudaEventCreateWithFlags(&done, cudaEventBlockingSync | cudaEventDisableTiming) !=
+        cudaSuccess)
+      return SURFATT_CUDA_ERROR;
     init = true;
     return SURFATT_OK;
+  }
+  // Waits for the thread's stream, the calling thread sleeping rather than
+  // spinning: callers on every host core (the reference's one MPI rank per
+  // core) would otherwise keep each other's finished calls off the cores.
+  cudaError_t wait() {
+    const cudaError_t e = cudaEventRecord(done, st);
+    return e != cudaSuccess ? e : cudaEventSynchronize(done);
   }
   // start of a call: room for `doubles` staged doubles
   int stage_begin(size_t doubles) {
@@ -246,7 +258,7 @@ int finish_single(ThreadCtx& c, const DBuf& out_dev, size_t n, double** staged) 
     *staged = c.stage(nullptr, n);
     CK(cudaMemcpyAsync(*staged, out_dev.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.st));
   }
-  CK(cudaStreamSynchronize(c.st));
+  CK(c.wait());
   return SURFATT_OK;
 }
 
@@ -371,7 +383,7 @@ int mask_dropin(const double* xx, const double* yy, int nx, int ny, double* tab,
   double* staged = c.stage(nullptr, N);
   if (cudaGetLastError() != cudaSuccess ||
       cudaMemcpyAsync(staged, c.out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
-      cudaStreamSynchronize(c.st))
+      c.wait())
     return record(SURFATT_CUDA_ERROR, 0);
   std::memcpy(tab, staged, N * sizeof(double));
   c.ok.assign(staged, staged + N);
@@ -487,7 +499,7 @@ surfatt_status_t surfatt_measadj_run_forward(const double* xgrids, const double*
   if (cudaMemcpyAsync(c.si_host, c.si.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, c.st) ||
       cudaMemcpyAsync(st_T, c.T.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st) ||
       (nrec > 0 && cudaMemcpyAsync(st_k, c.sa.p, nrec * sizeof(double), cudaMemcpyDeviceToHost, c.st)) ||
-      cudaStreamSynchronize(c.st))
+      c.wait())
     return (surfatt_status_t)record(SURFATT_CUDA_ERROR, 0);
   std::memcpy(timetable, st_T, N * sizeof(double));
   if (nrec > 0) std::memcpy(tekio, st_k, nrec * sizeof(double));
@@ -603,7 +615,7 @@ surfatt_status_t surfatt_gaussian_smooth_geo_2(const double* data, int nx, int n
   launch_smooth_apply(A, plan, c.st);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(smdata, c.sm_out.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.st));
-  CK(cudaStreamSynchronize(c.st));
+  CK(c.wait());
   c.sm_key.swap(key);
   return (surfatt_status_t)record(SURFATT_OK, 0);
 }
