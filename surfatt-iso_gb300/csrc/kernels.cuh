@@ -141,11 +141,14 @@ int fp32w_items_for_mode(int mode);
 // Forward items per solve of a variant with items (the rest: one item per
 // adjoint field): the strip variant keeps each forward whole.
 int fp32w_fwd_items(int variant);
-constexpr int kSolveStateInts = 5;
+constexpr int kSolveStateInts = 9;
 // Per-solve state record (ints) of a solve cut into items: items done (-1:
 // failed), forward iterations, forward status, running status, adjoint
 // iterations of field 0.
-enum SolveStateSlot { SS_DONE = 0, SS_FIT, SS_FST, SS_ST, SS_ITS0 };
+// (FP32 row kernel: the adjoint items' per-field iterations and statuses and
+// the count of fields finished)
+enum SolveStateSlot { SS_DONE = 0, SS_FIT, SS_FST, SS_ST, SS_ITS0, SS_ITS1, SS_AST0, SS_AST1,
+                      SS_ADJ };
 // Bounded wait for a solve's previous item (polls, each followed by a short
 // sleep).
 constexpr int kItemWaitLimit = 1 << 24;
@@ -173,9 +176,10 @@ void launch_chi_reduce(const double* chi_s, int nsolve, double* chi_out, cudaStr
 // Single-solve kernels of the drop-in symbols (one block).
 void launch_uw_single(const PeriodDev& P, double x0, double y0, double* ws, double* T,
                       int* status_iters, cudaStream_t st);
-// The same solve on a cluster of four blocks (one per SM), each evaluating
-// one case of the update; false (nothing launched) when the grid's tau does
-// not fit one block's shared memory or the cluster cannot be launched.
+// The same solve on a cluster of six blocks (one per SM), each evaluating
+// its share of the update's cases; false (nothing launched) when the grid's
+// tau does not fit one block's shared memory or the cluster cannot be
+// launched.
 bool launch_uw_cluster(const PeriodDev& P, double x0, double y0, double* ws, double* T,
                        int* status_iters, cudaStream_t st);
 void launch_weno_single(const PeriodDev& P, double x0, double y0, int multiplicative, double* ws,

@@ -490,7 +490,8 @@ struct WAdj {
 // the visit); otherwise only the value the lanes exchange.
 template <bool HEAVY>
 __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, int nx, int xdir,
-                                        int ydir, const WSlot& V, const float* src, bool last) {
+                                        int ydir, const WSlot& V, const float* fld,
+                                        const float* fold, const float* src, bool last) {
   const int u = t - v;
   o.on = v < nv && u >= 0 && u < nu;
   if (!o.on) {
@@ -500,15 +501,26 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
   const int i = xdir > 0 ? 1 + u : nu - u;  // interior [1, nx-2]
   const int j = ydir > 0 ? 1 + v : nv - v;
   const int k = i + nx * j;
-  o.own = V.tau[k];
+  o.own = fld[k];
   if (HEAVY) {
     o.w = V.W[k];
     o.src = src[k];
-    if (last) o.old = V.old[k];
+    if (last) o.old = fold[k];
   }
 }
 
-// Sweeps one adjoint field (held in V.tau) to convergence: the reference's
+// Storage of adjoint field f during the adjoint: field 0 in tau / old, field
+// 1 in the T0 gradient's array (dead once the adjoint coefficients are set),
+// so that a solve's two fields can be swept side by side.
+__device__ __forceinline__ float* w_field(const WSlot& V, int f, size_t N) {
+  return f ? reinterpret_cast<float*>(V.G) : V.tau;
+}
+__device__ __forceinline__ float* w_field_old(const WSlot& V, int f, size_t N) {
+  return f ? reinterpret_cast<float*>(V.G) + N : V.old;
+}
+
+// Sweeps one adjoint field (held in fld, iteration-start values in fold) to
+// convergence: the reference's
 // absolute rule (:1429) or no change beyond the FP32 resolution of the field.
 // Neighbours outside the interior are the boundary's zeros.
 //
@@ -520,8 +532,9 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
 // affords D = 2 for a single warp (its forward sweeps hold the register
 // file: deeper rings spill) and D = 3 for teams.
 template <int MB, int NW, int D, bool ST>
-__device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const float* src,
-                                    const Tm<NW>& T, int* status_out, int* iters_out) {
+__device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* fld, float* fold,
+                                    const float* src, const Tm<NW>& T, int* status_out,
+                                    int* iters_out) {
   static_assert(!ST || NW == 1, "strips are swept by one warp");
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   const int nu = nx - 2, nv = ny - 2;
@@ -529,7 +542,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
   for (int j = T.wid; j < ny; j += NW)
     for (int i = lane; i < nx; i += 32) {
       const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
-      V.tau[i + (size_t)nx * j] = in ? 100.f : 0.f;
+      fld[i + (size_t)nx * j] = in ? 100.f : 0.f;
     }
   tsync<NW>();
   // Teams: as in the forward sweeps, the first row's south value comes
@@ -559,13 +572,13 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
       auto north_of_top = [&](int tau) {
         const int u = tau - vtop;
         if (u < 0 || u >= nu || vtop + 1 >= nv) return 0.f;
-        return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
+        return fld[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
       };
       // strips: the new value south of the bottom row at step tau
       auto south_of_bot = [&](int tau) {
         const int u = tau - vb;
         if (u < 0 || u >= nu || vb < 1) return 0.f;
-        return V.tau[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? vb : nv + 1 - vb)];
+        return fld[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? vb : nv + 1 - vb)];
       };
       // A cell is written only at its own visit and the weights, sources and
       // iteration-start values are fixed within a sweep, so operands loaded
@@ -577,8 +590,8 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
         res[m] = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d)
-          wa_load<true>(ring[d][m], tbeg + d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
-                        last);
+          wa_load<true>(ring[d][m], tbeg + d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, fld,
+                        fold, src, last);
       }
       float pn = top ? north_of_top(tbeg) : 0.f;
       float ps = (ST && bot) ? south_of_bot(tbeg) : 0.f;
@@ -613,8 +626,8 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
               const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
               const float ts = ydir > 0 ? sth : nth, tn = ydir > 0 ? nth : sth;
               const float val = adj_update(cur[m].src, cur[m].w, tw, te, ts, tn);
-              V.tau[k] = val;
-              if (s == 0) V.old[k] = cur[m].own;
+              fld[k] = val;
+              if (s == 0) fold[k] = cur[m].own;
               if (last) {
                 const float dd = fabsf(val - cur[m].old);
                 l1 += dd;
@@ -627,8 +640,8 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, const fl
           // this slot now takes the operands of step t + D
 #pragma unroll
           for (int m = 0; m < MB; ++m)
-            wa_load<true>(ring[d][m], t + D, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, src,
-                          last);
+            wa_load<true>(ring[d][m], t + D, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, fld,
+                          fold, src, last);
           if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
           pn = qn;
           ps = qs;
@@ -762,7 +775,7 @@ __device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, cons
 // (src/acqui.f90:314-315) of adjoint field f, FP32 here, summed per period
 // in FP64.
 template <int NW>
-__device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlot& V,
+__device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const float* field,
                               const WSolve& w, int s, int f, const Tm<NW>& T) {
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   float* out = reinterpret_cast<float*>(f == 0 ? A.kcontrib : A.kcontrib_den) + A.kslot[s];
@@ -780,7 +793,7 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const WSlo
           const size_t k = i + (size_t)nx * j;
           const float4 pb = P.p4b[k];
           isv[g] = A.mode == 3 ? pb.w : pb.z;
-          ta[g] = V.tau[k];
+          ta[g] = field[k];
         }
       }
 #pragma unroll
@@ -825,27 +838,38 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
   const int nitem = cut ? A.items : 1;
   float* kf = reinterpret_cast<float*>(A.kcontrib);
   float* kdf = reinterpret_cast<float*>(A.kcontrib_den);
+  const int nf = A.mode == 3 ? 2 : 1;
+  const int nfwd = cut && A.fwd_items > 0 ? A.fwd_items : kFwdItems;  // forward items
   for (;;) {
     int q = 0;
     if (T.tid == 0) q = atomicAdd(A.queue, 1);
     q = tbcast<NW>(q);
     if (q >= A.nsolve * nitem) break;
-    const int item = q / A.nsolve;
-    const int s = A.order[q % A.nsolve];
+    // queue order: every solve's forward item 0, then every item 1, ...;
+    // then the adjoint items solve by solve (a solve's fields side by side)
+    int item = q / A.nsolve, si = q % A.nsolve;
+    if (cut && item >= nfwd) {
+      const int r = q - nfwd * A.nsolve, nadj = nitem - nfwd;
+      item = nfwd + r % nadj;
+      si = r / nadj;
+    }
+    const int s = A.order[si];
     int* const ss = cut ? A.sstate + (size_t)kSolveStateInts * s : nullptr;
     if (cut && item == 0 && s == A.hold_solve) continue;  // test hook: never done
     if (cut && item > 0) {
-      // the previous item of this solve (taken earlier by a resident warp)
+      // the previous forward item of this solve, or for an adjoint item the
+      // whole forward (taken earlier by a resident warp)
+      const int need = item < nfwd ? item : nfwd;
       const int limit =
           (s == A.hold_solve && A.item_wait_limit > 0) ? A.item_wait_limit : kItemWaitLimit;
       int d = ld_acquire(ss + SS_DONE), it = 0;
-      while (d >= 0 && d < item && it < limit) {
+      while (d >= 0 && d < need && it < limit) {
         __nanosleep(128);
         d = ld_acquire(ss + SS_DONE);
         ++it;
       }
       // every thread acquired the state itself; the team takes one decision
-      bool failed = d < 0, late = d >= 0 && d < item;
+      bool failed = d < 0, late = d >= 0 && d < need;
       if (NW > 1) {
         failed = __syncthreads_or(failed);
         late = !failed && __syncthreads_or(late);
@@ -910,24 +934,20 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
       tsync<NW>();
     };
     const WSolve w = w_locate(P, x0, y0, xd0, yd0, lane);
-    const int nf = A.mode == 3 ? 2 : 1;
-    const int nfwd = cut && A.fwd_items > 0 ? A.fwd_items : kFwdItems;  // forward items
     const int nitems_mode = w_items_for_mode(A.mode, nfwd);
     const int first = cut ? item : 0;                 // first item done here
     const int lastit = cut ? item : nitems_mode - 1;  // last item done here
-    int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0;
+    int fst = ST_OK, fit = 0, st = ST_OK, its0 = 0, its1 = 0, ast0 = ST_OK, ast1 = ST_OK;
     if (cut && first > 0) {
-      int v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+      int v0 = 0, v1 = 0, v2 = 0;
       if (T.tid == 0) {
         v0 = ss[SS_FIT];
         v1 = ss[SS_FST];
         v2 = ss[SS_ST];
-        v3 = ss[SS_ITS0];
       }
       fit = tbcast<NW>(v0);
       fst = tbcast<NW>(v1);
       st = tbcast<NW>(v2);
-      its0 = tbcast<NW>(v3);
     }
     if (first == 0 && w.status != ST_OK) {
       for (int r = T.tid; r < nr; r += 32 * NW) {
@@ -995,27 +1015,53 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
         continue;
       }
     }
-    // adjoint field(s) f0 .. f1
+    // adjoint field(s) f0 .. f1 (an adjoint item: one field)
     const int f0 = cut ? (first > nfwd ? first - nfwd : 0) : 0;
     const int f1 = A.mode >= 2 ? (cut ? lastit - nfwd : nf - 1) : -1;
     for (int f = f0; f <= f1; ++f) {
       int ast = ST_OK, n = 0;
-      w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(P, V, f ? V.src[1] : V.src[0], T,
-                                                            &ast, &n);
+      float* const fld = f ? w_field(V, 1, N) : w_field(V, 0, N);
+      float* const fold = f ? w_field_old(V, 1, N) : w_field_old(V, 0, N);
+      w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(P, V, fld, fold,
+                                                            f ? V.src[1] : V.src[0], T, &ast, &n);
       mark(PH_ADJ);
-      if (f == 0) its0 = n; else its1 = n;
-      if (ast != ST_OK && st == ST_OK) st = ast;
-      w_slot<NW>(A, P, V, w, s, f, T);
+      if (f == 0) { its0 = n; ast0 = ast; } else { its1 = n; ast1 = ast; }
+      w_slot<NW>(A, P, fld, w, s, f, T);
       mark(PH_SLOT);
     }
-    if (cut && lastit < nitems_mode - 1) {
+    if (cut && f1 >= 0) {
+      // one field of several items: its iterations and status into the
+      // solve's record, then the count of finished fields; the item that
+      // finishes the solve's last field reports the solve
       if (T.tid == 0) {
-        ss[SS_ST] = st;
-        ss[SS_ITS0] = its0;
+        ss[f0 ? SS_ITS1 : SS_ITS0] = f0 ? its1 : its0;
+        ss[f0 ? SS_AST1 : SS_AST0] = f0 ? ast1 : ast0;
       }
-      finish_item(lastit + 1);
-      continue;
+      __threadfence();
+      tsync<NW>();
+      int nprev = 0;
+      if (T.tid == 0) nprev = atomicAdd(ss + SS_ADJ, 1);
+      nprev = tbcast<NW>(nprev);
+      if (nprev < nf - 1) {
+        tsync<NW>();
+        continue;
+      }
+      __threadfence();
+      int v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+      if (T.tid == 0) {
+        v0 = ld_acquire(ss + SS_ITS0);
+        v1 = ld_acquire(ss + SS_AST0);
+        v2 = nf > 1 ? ld_acquire(ss + SS_ITS1) : 0;
+        v3 = nf > 1 ? ld_acquire(ss + SS_AST1) : ST_OK;
+      }
+      its0 = tbcast<NW>(v0);
+      ast0 = tbcast<NW>(v1);
+      its1 = tbcast<NW>(v2);
+      ast1 = tbcast<NW>(v3);
     }
+    // field statuses in field order, as one warp sweeping them in turn
+    if (A.mode >= 2 && ast0 != ST_OK && st == ST_OK) st = ast0;
+    if (A.mode == 3 && ast1 != ST_OK && st == ST_OK) st = ast1;
     // the solve's last item: its outputs
     if (T.tid == 0) {
       A.status[s] = st;
