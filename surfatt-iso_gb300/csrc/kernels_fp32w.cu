@@ -813,15 +813,21 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const floa
 // per scheduler) allow 255 registers a thread and 12 warps (three) 168.
 //
 // Work items.  With A.items == 1 a warp takes whole solves.  With A.items > 1
-// each solve is cut into consecutive items -- kFwdItems forward items of
+// each solve is cut into items -- A.fwd_items consecutive forward items of
 // kSplitIter iterations each (the first also computes T0, the last runs to
 // convergence and adds receivers, misfit, adjoint coefficients and
 // sources), then one item per adjoint field and its kernel slot -- each
-// solve has its own workspace slot and state record, and the queue hands out
-// every solve's item 0, then every item 1, and so on, so that the last round
-// of a batch is a short item rather than a whole solve.  An item waits
-// (bounded) for the previous item of its solve, which a resident warp took
-// earlier, so the waits cannot form a cycle.
+// solve has its own workspace slot and state record.  The queue hands out
+// every solve's forward item 0, then every item 1, and so on, so that the
+// last round of a batch is a short item rather than a whole solve, and then
+// the adjoint items solve by solve, a solve's two fields one after the
+// other, so that two warps sweep them side by side (field 1 lives in the
+// T0 gradient's array, dead by then).  A forward item waits (bounded) for
+// the previous item of its solve, an adjoint item for the last forward
+// item; both were taken earlier by a resident warp, so the waits cannot form
+// a cycle.  Each adjoint item records its field's iterations and status and
+// counts itself; the item that finishes a solve's last field reports the
+// solve (its fields' statuses taken in field order).
 constexpr int kSplitIter = 2;
 constexpr int kFwdItems = 3;
 
