@@ -36,6 +36,20 @@ def test_forward_lonlat_dropin(sg, oracle, nx, ny, src):
     assert rel_pointwise(T, Tr) <= TT_TOL
 
 
+@pytest.mark.parametrize("nx,ny,src", [(200, 150, (103.1, 24.3)), (270, 40, (105.2, 22.9))])
+def test_forward_lonlat_dropin_large_grids(sg, oracle, nx, ny, src):
+    """A grid whose tau does not fit one block's shared memory (200 x 150)
+    runs on the one-block kernel, a long thin one (270 x 40) on the cluster
+    forward; both within the tolerance and with the oracle's iteration
+    count."""
+    xx, yy, a, b, c, fun = _flat(nx, ny, d=0.04)
+    T, st, it = sg.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, *src)
+    Tr, sr, ir = oracle.fsm_uw_ps_lonlat_2d(xx, yy, a, b, c, fun, *src)
+    assert st == sr == 0
+    assert it == ir
+    assert rel_pointwise(T, Tr) <= TT_TOL
+
+
 def test_forward_lonlat_topography_metric(sg, oracle):
     xx, yy, topo, m11, m12, m22 = W.config5_model(n_lon=60, n_lat=50, d=0.02)
     sv = 3.2 * W.checkerboard_2d(60, 50, 2, 2, 0.05)
