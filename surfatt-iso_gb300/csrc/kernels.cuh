@@ -73,6 +73,7 @@ struct BatchArgs {
   unsigned long long* phase_cycles = nullptr;  // optional: SM cycles per solve phase, summed
   int items = 1;           // FP32 warp kernel: items per solve (1: whole solves)
   int fwd_items = 0;       // FP32 warp kernel with items: forward items (0: the default)
+  int adj_parts = 0;       // FP32 warp kernel with items: items per adjoint field (0: one)
   int* sstate = nullptr;   // FP32 warp kernel with items > 1: per-solve state records
   // Test hooks of the bounded item wait (FP32 warp kernel with items; off by
   // default): the first item of solve hold_solve (>= 0) is skipped without
@@ -141,14 +142,16 @@ int fp32w_items_for_mode(int mode);
 // Forward items per solve of a variant with items (the rest: one item per
 // adjoint field): the strip variant keeps each forward whole.
 int fp32w_fwd_items(int variant);
-constexpr int kSolveStateInts = 9;
+// Items per adjoint field of a variant with items (iteration ranges).
+int fp32w_adj_parts(int variant);
+constexpr int kSolveStateInts = 11;
 // Per-solve state record (ints) of a solve cut into items: items done (-1:
 // failed), forward iterations, forward status, running status, adjoint
 // iterations of field 0.
-// (FP32 row kernel: the adjoint items' per-field iterations and statuses and
-// the count of fields finished)
+// (FP32 row kernel: the adjoint items' per-field iterations and statuses,
+// the count of fields finished and each field's parts done)
 enum SolveStateSlot { SS_DONE = 0, SS_FIT, SS_FST, SS_ST, SS_ITS0, SS_ITS1, SS_AST0, SS_AST1,
-                      SS_ADJ };
+                      SS_ADJ, SS_AD0, SS_AD1 };
 // Bounded wait for a solve's previous item (polls, each followed by a short
 // sleep).
 constexpr int kItemWaitLimit = 1 << 24;

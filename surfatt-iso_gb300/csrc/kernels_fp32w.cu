@@ -531,20 +531,26 @@ __device__ __forceinline__ float* w_field_old(const WSlot& V, int f, size_t N) {
 // a fixed set of registers and no operand is ever copied.  The solve kernel
 // affords D = 2 for a single warp (its forward sweeps hold the register
 // file: deeper rings spill) and D = 3 for teams.
+//
+// Iterations it0 .. it1 (the field is initialised when it0 == 1; a later
+// range resumes from the field in fld): ST_OK and the iteration that
+// converged, or ST_NOT_CONVERGED and it1.
 template <int MB, int NW, int D, bool ST>
 __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* fld, float* fold,
-                                    const float* src, const Tm<NW>& T, int* status_out,
-                                    int* iters_out) {
+                                    const float* src, const Tm<NW>& T, int it0, int it1,
+                                    int* status_out, int* iters_out) {
   static_assert(!ST || NW == 1, "strips are swept by one warp");
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   const int nu = nx - 2, nv = ny - 2;
   const int nsteps = nu + nv - 1;
-  for (int j = T.wid; j < ny; j += NW)
-    for (int i = lane; i < nx; i += 32) {
-      const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
-      fld[i + (size_t)nx * j] = in ? 100.f : 0.f;
-    }
-  tsync<NW>();
+  if (it0 == 1) {
+    for (int j = T.wid; j < ny; j += NW)
+      for (int i = lane; i < nx; i += 32) {
+        const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
+        fld[i + (size_t)nx * j] = in ? 100.f : 0.f;
+      }
+    tsync<NW>();
+  }
   // Teams: as in the forward sweeps, the first row's south value comes
   // through a shared slot from the warp below, the last row's north value
   // from memory a step ahead.  Strips (ST): as in the forward sweeps, both
@@ -552,7 +558,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
   const int nstrip = ST ? (nv + 32 * MB - 1) / (32 * MB) : 1;
   __shared__ float xs_val[2][NW > 1 ? NW : 1];
   int iter, status = ST_NOT_CONVERGED;
-  for (iter = 1; iter <= MAXITER_JSE; ++iter) {
+  for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f, vmax = 0.f;
     float l1s[kMaxStrips];  // strips, last sweep: strip p's partial sums
 #pragma unroll
@@ -667,7 +673,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
     }
   }
   *status_out = status;
-  *iters_out = iter > MAXITER_JSE ? MAXITER_JSE : iter;
+  *iters_out = iter > it1 ? it1 : iter;
 }
 
 // T = tau*T0 at a node (FP64 product of the FP32 factors)
@@ -830,6 +836,10 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const floa
 // solve (its fields' statuses taken in field order).
 constexpr int kSplitIter = 2;
 constexpr int kFwdItems = 3;
+// adjoint iterations per part of a field cut into A.adj_parts items (the
+// last part runs to convergence)
+constexpr int kAdjSplitIter = 1;
+constexpr int kAdjParts = 3;
 
 // Items per solve for `mode` when solves are cut.
 __host__ __device__ inline int w_items_for_mode(int mode, int fwd_items = kFwdItems) {
@@ -845,37 +855,45 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
   float* kf = reinterpret_cast<float*>(A.kcontrib);
   float* kdf = reinterpret_cast<float*>(A.kcontrib_den);
   const int nf = A.mode == 3 ? 2 : 1;
-  const int nfwd = cut && A.fwd_items > 0 ? A.fwd_items : kFwdItems;  // forward items
+  const int nfwd = cut && A.fwd_items > 0 ? A.fwd_items : kFwdItems;   // forward items
+  const int nparts = cut && A.adj_parts > 0 ? A.adj_parts : 1;         // items per field
   for (;;) {
     int q = 0;
     if (T.tid == 0) q = atomicAdd(A.queue, 1);
     q = tbcast<NW>(q);
     if (q >= A.nsolve * nitem) break;
     // queue order: every solve's forward item 0, then every item 1, ...;
-    // then the adjoint items solve by solve (a solve's fields side by side)
-    int item = q / A.nsolve, si = q % A.nsolve;
+    // then every solve's first part of each adjoint field (a solve's fields
+    // next to each other), then every second part, ...
+    int item = q / A.nsolve, si = q % A.nsolve, part = 0, fi = 0;
     if (cut && item >= nfwd) {
-      const int r = q - nfwd * A.nsolve, nadj = nitem - nfwd;
-      item = nfwd + r % nadj;
-      si = r / nadj;
+      const int r = q - nfwd * A.nsolve;
+      part = r / (A.nsolve * nf);
+      si = (r % (A.nsolve * nf)) / nf;
+      fi = r % nf;
+      item = nfwd + part * nf + fi;
     }
     const int s = A.order[si];
     int* const ss = cut ? A.sstate + (size_t)kSolveStateInts * s : nullptr;
     if (cut && item == 0 && s == A.hold_solve) continue;  // test hook: never done
     if (cut && item > 0) {
-      // the previous forward item of this solve, or for an adjoint item the
-      // whole forward (taken earlier by a resident warp)
-      const int need = item < nfwd ? item : nfwd;
+      // a forward item: the previous forward item of this solve; an adjoint
+      // field's first part: the whole forward; a later part: the field's
+      // previous part (each taken earlier by a resident warp)
+      const bool onfield = item >= nfwd && part > 0;
+      const int need = item < nfwd ? item : (part == 0 ? nfwd : part);
       const int limit =
           (s == A.hold_solve && A.item_wait_limit > 0) ? A.item_wait_limit : kItemWaitLimit;
       int d = ld_acquire(ss + SS_DONE), it = 0;
-      while (d >= 0 && d < need && it < limit) {
+      int g = onfield ? ld_acquire(ss + (fi ? SS_AD1 : SS_AD0)) : d;
+      while (d >= 0 && g < need && it < limit) {
         __nanosleep(128);
         d = ld_acquire(ss + SS_DONE);
+        g = onfield ? ld_acquire(ss + (fi ? SS_AD1 : SS_AD0)) : d;
         ++it;
       }
       // every thread acquired the state itself; the team takes one decision
-      bool failed = d < 0, late = d >= 0 && d < need;
+      bool failed = d < 0, late = d >= 0 && g < need;
       if (NW > 1) {
         failed = __syncthreads_or(failed);
         late = !failed && __syncthreads_or(late);
@@ -1021,30 +1039,55 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
         continue;
       }
     }
-    // adjoint field(s) f0 .. f1 (an adjoint item: one field)
-    const int f0 = cut ? (first > nfwd ? first - nfwd : 0) : 0;
-    const int f1 = A.mode >= 2 ? (cut ? lastit - nfwd : nf - 1) : -1;
+    // adjoint field(s) f0 .. f1 (an adjoint item: one part of one field)
+    const int f0 = cut ? fi : 0;
+    const int f1 = A.mode >= 2 ? (cut ? fi : nf - 1) : -1;
+    bool field_done = true;
     for (int f = f0; f <= f1; ++f) {
-      int ast = ST_OK, n = 0;
+      int ast = ST_OK, n = 0, it0 = 1, it1 = MAXITER_JSE;
+      if (cut && part > 0) {
+        // this field's earlier parts: converged (nothing left) or not
+        int v0 = 0, v1 = 0;
+        if (T.tid == 0) {
+          v0 = ss[f ? SS_ITS1 : SS_ITS0];
+          v1 = ss[f ? SS_AST1 : SS_AST0];
+        }
+        n = tbcast<NW>(v0);
+        ast = tbcast<NW>(v1);
+        it0 = n + 1;
+      }
+      if (cut && part < nparts - 1) it1 = (part + 1) * kAdjSplitIter;
       float* const fld = f ? w_field(V, 1, N) : w_field(V, 0, N);
       float* const fold = f ? w_field_old(V, 1, N) : w_field_old(V, 0, N);
-      w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(P, V, fld, fold,
-                                                            f ? V.src[1] : V.src[0], T, &ast, &n);
-      mark(PH_ADJ);
+      const bool earlier = cut && part > 0 && ast == ST_OK;  // converged in an earlier part
+      if (!earlier) {
+        w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(
+            P, V, fld, fold, f ? V.src[1] : V.src[0], T, it0, it1, &ast, &n);
+        mark(PH_ADJ);
+      }
       if (f == 0) { its0 = n; ast0 = ast; } else { its1 = n; ast1 = ast; }
-      w_slot<NW>(A, P, fld, w, s, f, T);
-      mark(PH_SLOT);
+      field_done = !earlier && (ast == ST_OK || !cut || part == nparts - 1);
+      if (field_done) {
+        w_slot<NW>(A, P, fld, w, s, f, T);
+        mark(PH_SLOT);
+      }
     }
     if (cut && f1 >= 0) {
-      // one field of several items: its iterations and status into the
-      // solve's record, then the count of finished fields; the item that
-      // finishes the solve's last field reports the solve
+      // one part of one field: the field's iterations and status into the
+      // solve's record, then the part is done; the part that finishes the
+      // field counts it, and the one that finishes the solve's last field
+      // reports the solve
       if (T.tid == 0) {
         ss[f0 ? SS_ITS1 : SS_ITS0] = f0 ? its1 : its0;
         ss[f0 ? SS_AST1 : SS_AST0] = f0 ? ast1 : ast0;
       }
       __threadfence();
       tsync<NW>();
+      if (T.tid == 0) st_release(ss + (f0 ? SS_AD1 : SS_AD0), part + 1);
+      if (!field_done) {
+        tsync<NW>();
+        continue;
+      }
       int nprev = 0;
       if (T.tid == 0) nprev = atomicAdd(ss + SS_ADJ, 1);
       nprev = tbcast<NW>(nprev);
@@ -1099,6 +1142,7 @@ bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2 || v
 bool fp32w_variant_strips(int variant) { return variant >= 4; }
 int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
 int fp32w_fwd_items(int variant) { return fp32w_variant_strips(variant) ? 1 : kFwdItems; }
+int fp32w_adj_parts(int variant) { return fp32w_variant_items(variant) ? kAdjParts : 1; }
 
 template <int MB, int PF, int MINW, int NW, bool ST>
 static void launch_w(const BatchArgs& a, int grid, cudaStream_t st) {

@@ -201,7 +201,8 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   if (plan.kind == KK_FP32_WARP && plan.cut) {
     const long long n = std::max(1, sh.nsolve);
     A.fwd_items = fp32w_fwd_items(plan.pf);
-    A.items = A.fwd_items + (mode == 3 ? 2 : (mode == 2 ? 1 : 0));
+    A.adj_parts = fp32w_adj_parts(plan.pf);
+    A.items = A.fwd_items + (mode == 3 ? 2 : (mode == 2 ? 1 : 0)) * A.adj_parts;
     A.sstate = reinterpret_cast<int*>(ws + n * plan.ws_doubles);
     if (cudaMemsetAsync(A.sstate, 0, (size_t)n * kSolveStateInts * sizeof(int), st) != cudaSuccess)
       return -ST_CUDA_ERROR;
