@@ -822,18 +822,22 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const floa
 // each solve is cut into items -- A.fwd_items consecutive forward items of
 // kSplitIter iterations each (the first also computes T0, the last runs to
 // convergence and adds receivers, misfit, adjoint coefficients and
-// sources), then one item per adjoint field and its kernel slot -- each
-// solve has its own workspace slot and state record.  The queue hands out
-// every solve's forward item 0, then every item 1, and so on, so that the
-// last round of a batch is a short item rather than a whole solve, and then
-// the adjoint items solve by solve, a solve's two fields one after the
-// other, so that two warps sweep them side by side (field 1 lives in the
-// T0 gradient's array, dead by then).  A forward item waits (bounded) for
-// the previous item of its solve, an adjoint item for the last forward
-// item; both were taken earlier by a resident warp, so the waits cannot form
-// a cycle.  Each adjoint item records its field's iterations and status and
-// counts itself; the item that finishes a solve's last field reports the
-// solve (its fields' statuses taken in field order).
+// sources), then A.adj_parts items per adjoint field (iteration ranges of
+// kAdjSplitIter, the last to convergence, then the field's kernel slot) --
+// each solve has its own workspace slot and state record.  The queue hands
+// out every solve's forward item 0, then every item 1, and so on, so that
+// the last round of a batch is a short item rather than a whole solve, then
+// every solve's first part of each field (a solve's two fields next to each
+// other, so that two warps sweep them side by side; field 1 lives in the T0
+// gradient's array, dead by then), then every second part, and so on.  A
+// forward item waits (bounded) for the previous item of its solve, a
+// field's first part for the last forward item, a later part for the
+// field's previous part; each was taken earlier by a resident warp, so the
+// waits cannot form a cycle.  A part records the field's iterations and
+// status; the part that finishes a field (it converged, or it is the last)
+// writes the kernel slot and counts the field, and the one that finishes a
+// solve's last field reports the solve (its fields' statuses taken in field
+// order); parts after convergence only mark themselves done.
 constexpr int kSplitIter = 2;
 constexpr int kFwdItems = 3;
 // adjoint iterations per part of a field cut into A.adj_parts items (the
