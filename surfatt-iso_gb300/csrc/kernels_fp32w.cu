@@ -838,8 +838,11 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const floa
 // writes the kernel slot and counts the field, and the one that finishes a
 // solve's last field reports the solve (its fields' statuses taken in field
 // order); parts after convergence only mark themselves done.
-constexpr int kSplitIter = 2;
-constexpr int kFwdItems = 3;
+// (measured on the 1280-solve, 120 x 120 evaluation: forward items of one
+// iteration, five of them, and three parts per adjoint field, 17.6 ms,
+// against 18.0 with three forward items of two iterations)
+constexpr int kSplitIter = 1;
+constexpr int kFwdItems = 5;
 // adjoint iterations per part of a field cut into A.adj_parts items (the
 // last part runs to convergence)
 constexpr int kAdjSplitIter = 1;
