@@ -169,6 +169,8 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 // Plain FP64 kernel cut into work items (BatchArgs::items = kFp64Items):
 // items 0 .. kFp64Items - 2 run kFp64SplitIter forward iterations each, the
 // last runs the forward sweeps to convergence and the rest of the solve.
+// (measured on the 1280-solve, 120 x 120 evaluation: 207 - 210 ms, against
+// 209 - 212 ms with four to six one-iteration items)
 constexpr int kFp64Items = 3;
 constexpr int kFp64SplitIter = 2;
 long long batch_fp32w_ws_doubles(long long N);
