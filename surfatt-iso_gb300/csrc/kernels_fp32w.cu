@@ -93,28 +93,17 @@ __device__ __forceinline__ void tsum_max2(double& a, double& b, double& c) {
 }
 
 
-// Strips of one warp (at most a team's warps): the partial sum of strip p
-// kept apart (selects: a run-time index would put the array in local memory)
-// and the strips reduced as a team reduces its warps: each over the lanes by
-// the xor tree, then in strip order.
+// Strips of one warp (at most a team's warps): each strip's partial sums
+// reduced as a team reduces a warp's (over the lanes by the xor tree, in
+// FP64) and added to the iteration's total in strip order, as the team adds
+// its warps' -- the same bits as a team's reduction.
 constexpr int kMaxStrips = 4;
 
-__device__ __forceinline__ void w_strip_put(float (&l1s)[kMaxStrips], int p, float v) {
+__device__ __forceinline__ void w_strip_add(double& acc, float v) {
+  double x = (double)v;
 #pragma unroll
-  for (int q = 0; q < kMaxStrips; ++q)
-    if (q == p) l1s[q] = v;
-}
-
-__device__ __forceinline__ double w_strip_sum(const float (&l1s)[kMaxStrips], int nstrip) {
-  double a = 0.0;
-#pragma unroll
-  for (int q = 0; q < kMaxStrips; ++q) {
-    double x = (double)l1s[q];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
-    if (q < nstrip) a += x;
-  }
-  return a;
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+  acc += x;
 }
 
 __device__ __forceinline__ double w_warp_max(double b) {
@@ -261,9 +250,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
   int iter, status = ST_NOT_CONVERGED;
   for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f;
-    float l1s[kMaxStrips];  // strips, last sweep: strip p's partial sums
-#pragma unroll
-    for (int p = 0; p < kMaxStrips; ++p) l1s[p] = 0.f;
+    double l1acc = 0.0;  // strips, last sweep: the strips' reduced sums so far
     for (int s = 0; s < 4; ++s) {
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
@@ -423,13 +410,13 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
         ps_t0 = qs_t0;
         tsync<NW>();
       }
-      if (ST && last) w_strip_put(l1s, sp, l1);
+      if (ST && last) w_strip_add(l1acc, l1);
      }
     }
     // FP64 decision over the lanes' partial sums (:1091-1115)
     double sl1, smax = (double)lmax, unused = 0.0;
     if (ST) {
-      sl1 = w_strip_sum(l1s, nstrip);
+      sl1 = l1acc;
       smax = w_warp_max(smax);
     } else {
       sl1 = (double)l1;
@@ -560,9 +547,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
   int iter, status = ST_NOT_CONVERGED;
   for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f, vmax = 0.f;
-    float l1s[kMaxStrips];  // strips, last sweep: strip p's partial sums
-#pragma unroll
-    for (int p = 0; p < kMaxStrips; ++p) l1s[p] = 0.f;
+    double l1acc = 0.0;  // strips, last sweep: the strips' reduced sums so far
     for (int s = 0; s < 4; ++s) {
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
@@ -654,12 +639,12 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
           tsync<NW>();
         }
       }
-      if (ST && last) w_strip_put(l1s, sp, l1);
+      if (ST && last) w_strip_add(l1acc, l1);
      }
     }
     double sl1, smax = (double)lmax, svmax = (double)vmax;
     if (ST) {
-      sl1 = w_strip_sum(l1s, nstrip);
+      sl1 = l1acc;
       smax = w_warp_max(smax);
       svmax = w_warp_max(svmax);
     } else {
