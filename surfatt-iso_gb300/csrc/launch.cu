@@ -78,7 +78,11 @@ int plan_evaluation(const EvalShape& sh, int prec, int device, int max_grid, Lau
     p.kind = KK_FP32_WARP;
     p.slots_per_block = 1;
     p.bands = fp32w_bands(sh.max_ny);
-    p.pf = force.variant >= 0 && force.variant < fp32w_variant_count() ? force.variant : 0;
+    // automatic: work items, grids of more than 128 rows in strips (the
+    // faster on every measured batch of tall grids and in the serving loop)
+    p.pf = force.variant >= 0 && force.variant < fp32w_variant_count()
+               ? force.variant
+               : (sh.max_ny > 128 ? 4 : 0);
     p.block = fp32w_block(p.bands, p.pf);
     p.per_sm = batch_fp32w_max_blocks_per_sm(p.bands, p.pf);
     p.ws_doubles = batch_fp32w_ws_doubles(sh.max_cells);

@@ -375,6 +375,7 @@ def test_fp32_single_class_ignores_periods_without_solves(sg):
     full = eng.evaluate(pb, mode=3, precision=sg.PREC_FP32)
     sub = pb.subset(sel)
     eng.load(sub)
+    eng.set_kernel(sg.PREC_FP32, kind=2, variant=0)  # teams (automatic: strips)
     eng.run(3, sg.PREC_FP32)
     assert eng.sync() == sg.OK
     assert eng.launch_config()["block"] == 64
