@@ -139,9 +139,9 @@ bool fp32w_variant_strips(int variant);
 // Threads per block of the row kernel for `bands` bands.
 int fp32w_block(int bands, int variant);
 int fp32w_items_for_mode(int mode);
-// Forward items per solve of a variant with items (the rest: one item per
-// adjoint field): the strip variant keeps each forward whole.
-int fp32w_fwd_items(int variant);
+// Forward items per solve of a variant with items on grids of `bands` bands
+// (the rest: the adjoint fields' parts): strips keep each forward whole.
+int fp32w_fwd_items(int variant, int bands);
 // Items per adjoint field of a variant with items (iteration ranges).
 int fp32w_adj_parts(int variant);
 constexpr int kSolveStateInts = 11;

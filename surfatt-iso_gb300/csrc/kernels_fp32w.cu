@@ -1123,9 +1123,8 @@ int fp32w_bands(int max_ny) { return (max_ny + 31) / 32; }
 //   1: the same, whole solves
 //   2: cell constants loaded at the visit, 12 warps per SM, items
 //   3: cell constants loaded at the visit, 8 warps per SM, whole solves
-//   4: grids of more than 128 rows swept in strips by one warp; items: the
-//      whole forward, then one item per adjoint field, one resident warp
-//      per solve
+//   4: grids of more than 128 rows swept in strips by one warp; items (their
+//      forward whole, one resident warp per solve)
 //   5: the same strips, whole solves
 // On grids of at most 128 rows variants 4 and 5 are variants 0 and 1.
 constexpr int kFp32wVariants = 6;
@@ -1133,7 +1132,9 @@ int fp32w_variant_count() { return kFp32wVariants; }
 bool fp32w_variant_items(int variant) { return variant == 0 || variant == 2 || variant == 4; }
 bool fp32w_variant_strips(int variant) { return variant >= 4; }
 int fp32w_items_for_mode(int mode) { return w_items_for_mode(mode); }
-int fp32w_fwd_items(int variant) { return fp32w_variant_strips(variant) ? 1 : kFwdItems; }
+int fp32w_fwd_items(int variant, int bands) {
+  return fp32w_variant_strips(variant) && bands > 4 ? 1 : kFwdItems;
+}
 int fp32w_adj_parts(int variant) { return fp32w_variant_items(variant) ? kAdjParts : 1; }
 
 template <int MB, int PF, int MINW, int NW, bool ST>

@@ -204,7 +204,7 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   A.sstate = nullptr;
   if (plan.kind == KK_FP32_WARP && plan.cut) {
     const long long n = std::max(1, sh.nsolve);
-    A.fwd_items = fp32w_fwd_items(plan.pf);
+    A.fwd_items = fp32w_fwd_items(plan.pf, plan.bands);
     A.adj_parts = fp32w_adj_parts(plan.pf);
     A.items = A.fwd_items + (mode == 3 ? 2 : (mode == 2 ? 1 : 0)) * A.adj_parts;
     A.sstate = reinterpret_cast<int*>(ws + n * plan.ws_doubles);
@@ -250,6 +250,10 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
       C.order = A.order + plan.class_off[k];
       C.nsolve = plan.class_solves[k];
       C.queue = queue + k;
+      if (plan.cut && plan.kind == KK_FP32_WARP) {  // the class's own forward items
+        C.fwd_items = fp32w_fwd_items(plan.pf, plan.class_bands[k]);
+        C.items = C.fwd_items + (mode == 3 ? 2 : (mode == 2 ? 1 : 0)) * C.adj_parts;
+      }
       if (!plan.cut) C.ws = ws + slot0 * plan.ws_doubles;  // disjoint block slots
       slot0 += plan.class_grid[k];
       cudaStream_t sk = st;
