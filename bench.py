@@ -103,7 +103,7 @@ def _workload(name):
         desc = "config1: 2-D, 81x81 grid, 25 stations (600 paths), 1 period"
     elif name == "config2s":
         pb = W.config2(nsta=20)
-        desc = ("config2s: config 2 with 20 stations (16 periods, 380 solves, 120x120), "
+        desc = ("config2s: config 2 with 20 stations (16 periods, 320 solves, 120x120), "
                 "a bounded case for profiler captures")
     elif name == "config4":
         pb = W.config4()
