@@ -291,27 +291,53 @@ void launch_kernel_reduce(const PeriodDev* /*periods_host*/, int nperiod, const 
                                         goff_dev, nx_dev, ny_dev);
 }
 
+// Per period and cell: the sum over the period's solves, in solve order, of
+// the FP32 kernel slots of one or two fields (c1 null: one), in FP64.  The
+// loads of eight solves are issued before their in-order additions, so the
+// chain waits for memory once per eight solves, not once per solve.
 __global__ void k_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plist,
-                                    const long long* kslot, const float* contrib, double* out,
-                                    const long long* goff, const int* nxs, const int* nys) {
+                                    const long long* kslot, const float* c0, double* o0,
+                                    const float* c1, double* o1, const long long* goff,
+                                    const int* nxs, const int* nys) {
   const int p = blockIdx.y;
   if (p >= nperiod) return;
   const long long N = (long long)nxs[p] * nys[p];
   const int s0 = plist_off[p], s1 = plist_off[p + 1];
+  constexpr int U = 8;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < N;
        k += (long long)gridDim.x * blockDim.x) {
-    double acc = 0.0;
-    for (int q = s0; q < s1; ++q) acc = acc + (double)contrib[kslot[plist[q]] + k];
-    out[goff[p] + k] = acc;
+    double a0 = 0.0, a1 = 0.0;
+    int q = s0;
+    for (; q + U <= s1; q += U) {
+      float v0[U], v1[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long off = kslot[plist[q + u]] + k;
+        v0[u] = c0[off];
+        v1[u] = c1 ? c1[off] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        a0 = a0 + (double)v0[u];
+        a1 = a1 + (double)v1[u];
+      }
+    }
+    for (; q < s1; ++q) {
+      const long long off = kslot[plist[q]] + k;
+      a0 = a0 + (double)c0[off];
+      if (c1) a1 = a1 + (double)c1[off];
+    }
+    o0[goff[p] + k] = a0;
+    if (c1) o1[goff[p] + k] = a1;
   }
 }
 
 void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plist,
-                              const long long* kslot, const float* contrib, double* out,
-                              const long long* goff_dev, const int* nx_dev, const int* ny_dev,
-                              cudaStream_t st) {
+                              const long long* kslot, const float* c0, double* o0,
+                              const float* c1, double* o1, const long long* goff_dev,
+                              const int* nx_dev, const int* ny_dev, cudaStream_t st) {
   dim3 grid(64, nperiod);
-  k_kernel_reduce_f32<<<grid, 256, 0, st>>>(nperiod, plist_off, plist, kslot, contrib, out,
+  k_kernel_reduce_f32<<<grid, 256, 0, st>>>(nperiod, plist_off, plist, kslot, c0, o0, c1, o1,
                                             goff_dev, nx_dev, ny_dev);
 }
 

@@ -123,9 +123,9 @@ void launch_kernel_reduce(const PeriodDev* periods_host, int nperiod, const int*
                           const int* nx_dev, const int* ny_dev, cudaStream_t st);
 // Same with FP32 per-solve slots, summed in FP64.
 void launch_kernel_reduce_f32(int nperiod, const int* plist_off, const int* plist,
-                              const long long* kslot, const float* contrib, double* out,
-                              const long long* goff_dev, const int* nx_dev, const int* ny_dev,
-                              cudaStream_t st);
+                              const long long* kslot, const float* c0, double* o0,
+                              const float* c1, double* o1, const long long* goff_dev,
+                              const int* nx_dev, const int* ny_dev, cudaStream_t st);
 // Warp-per-solve FP32 kernel (grids of at most 32*bands rows), one warp per
 // block; `variant` < fp32w_variant_count() selects prefetch and register cap.
 void launch_batch_fp32w(const BatchArgs& a, int grid, int bands, int variant, cudaStream_t st);

@@ -276,17 +276,20 @@ int enqueue_evaluation(const EvalShape& sh, const EvalDev& dev, const LaunchPlan
   if (ev_k1) cudaEventRecordWithFlags(ev_k1, st, ev_flags);
   if (mode >= 2) {
     const int nf = mode == 3 ? 2 : 1;
-    for (int f = 0; f < nf; ++f) {
-      double* kc = f == 0 ? A.kcontrib : A.kcontrib_den;
-      double* out = f == 0 ? dev.adj_s : dev.adj_density;
-      if (plan.kind == KK_FP32_WARP)
-        launch_kernel_reduce_f32(sh.nperiod, dev.plist_off, dev.plist, A.kslot,
-                                 reinterpret_cast<const float*>(kc), out, dev.goff, dev.nx,
-                                 dev.ny, st);
-      else
+    if (plan.kind == KK_FP32_WARP) {  // both fields in one pass
+      launch_kernel_reduce_f32(sh.nperiod, dev.plist_off, dev.plist, A.kslot,
+                               reinterpret_cast<const float*>(A.kcontrib), dev.adj_s,
+                               nf == 2 ? reinterpret_cast<const float*>(A.kcontrib_den) : nullptr,
+                               nf == 2 ? dev.adj_density : nullptr, dev.goff, dev.nx, dev.ny, st);
+      ++launches;
+    } else {
+      for (int f = 0; f < nf; ++f) {
+        double* kc = f == 0 ? A.kcontrib : A.kcontrib_den;
+        double* out = f == 0 ? dev.adj_s : dev.adj_density;
         launch_kernel_reduce(nullptr, sh.nperiod, dev.plist_off, dev.plist, A.kslot, kc, out,
                              sh.ncell, dev.goff, dev.nx, dev.ny, st);
-      ++launches;
+        ++launches;
+      }
     }
   }
   launch_chi_reduce(A.chi, sh.nsolve, dev.chi_total, st);
