@@ -496,6 +496,11 @@ __device__ __forceinline__ void wa_load(WAdj& o, int t, int v, int nu, int nv, i
   }
 }
 
+// Buffer holding an adjoint field after `iters` iterations of w_adj_sweeps.
+__device__ __forceinline__ float* w_adj_result(float* fld, float* fold, int iters) {
+  return (iters & 1) ? fold : fld;
+}
+
 // Storage of adjoint field f during the adjoint: field 0 in tau / old, field
 // 1 in the T0 gradient's array (dead once the adjoint coefficients are set),
 // so that a solve's two fields can be swept side by side.
@@ -520,8 +525,13 @@ __device__ __forceinline__ float* w_field_old(const WSlot& V, int f, size_t N) {
 // file: deeper rings spill) and D = 3 for teams.
 //
 // Iterations it0 .. it1 (the field is initialised when it0 == 1; a later
-// range resumes from the field in fld): ST_OK and the iteration that
-// converged, or ST_NOT_CONVERGED and it1.
+// range resumes from where the previous one left it): ST_OK and the
+// iteration that converged, or ST_NOT_CONVERGED and it1.  The two buffers
+// alternate: iteration i starts from fld (i odd) or fold (i even), its
+// first sweep writes the other, which the other three sweeps update in
+// place, so the start values stay for the convergence test without a store
+// of their own; after iteration i the field is in fold (i odd) or fld (i
+// even) -- w_adj_result.
 template <int MB, int NW, int D, bool ST>
 __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* fld, float* fold,
                                     const float* src, const Tm<NW>& T, int it0, int it1,
@@ -535,6 +545,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
       for (int i = lane; i < nx; i += 32) {
         const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
         fld[i + (size_t)nx * j] = in ? 100.f : 0.f;
+        fold[i + (size_t)nx * j] = 0.f;
       }
     tsync<NW>();
   }
@@ -547,11 +558,17 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
   int iter, status = ST_NOT_CONVERGED;
   for (iter = it0; iter <= it1; ++iter) {
     float l1 = 0.f, lmax = 0.f, vmax = 0.f;
+    // iteration start values in xs (read by the first sweep, kept for the
+    // convergence test), the sweeps' field in ys: odd iterations start in
+    // fld, even ones in fold
+    float* const xs = (iter & 1) ? fld : fold;
+    float* const ys = (iter & 1) ? fold : fld;
     double l1acc = 0.0;  // strips, last sweep: the strips' reduced sums so far
     for (int s = 0; s < 4; ++s) {
       int xdir, ydir;
       sweep_dirs(s, xdir, ydir);
       const bool last = s == 3;
+      const float* const rd = s == 0 ? xs : ys;
      for (int sp = 0; sp < nstrip; ++sp) {
       const int vb = 32 * MB * (ST ? sp : T.wid);
       const int vtop = vb + 32 * MB - 1;
@@ -563,13 +580,14 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
       auto north_of_top = [&](int tau) {
         const int u = tau - vtop;
         if (u < 0 || u >= nu || vtop + 1 >= nv) return 0.f;
-        return fld[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
+        return rd[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? 2 + vtop : nv - 1 - vtop)];
       };
-      // strips: the new value south of the bottom row at step tau
+      // strips: the new value south of the bottom row at step tau (the strip
+      // below wrote it in this sweep: the buffer the sweep writes)
       auto south_of_bot = [&](int tau) {
         const int u = tau - vb;
         if (u < 0 || u >= nu || vb < 1) return 0.f;
-        return fld[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? vb : nv + 1 - vb)];
+        return ys[(xdir > 0 ? 1 + u : nu - u) + nx * (ydir > 0 ? vb : nv + 1 - vb)];
       };
       // A cell is written only at its own visit and the weights, sources and
       // iteration-start values are fixed within a sweep, so operands loaded
@@ -581,8 +599,8 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
         res[m] = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d)
-          wa_load<true>(ring[d][m], tbeg + d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, fld,
-                        fold, src, last);
+          wa_load<true>(ring[d][m], tbeg + d, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, rd,
+                        xs, src, last);
       }
       float pn = top ? north_of_top(tbeg) : 0.f;
       float ps = (ST && bot) ? south_of_bot(tbeg) : 0.f;
@@ -617,8 +635,7 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
               const float tw = xdir > 0 ? west : east, te = xdir > 0 ? east : west;
               const float ts = ydir > 0 ? sth : nth, tn = ydir > 0 ? nth : sth;
               const float val = adj_update(cur[m].src, cur[m].w, tw, te, ts, tn);
-              fld[k] = val;
-              if (s == 0) fold[k] = cur[m].own;
+              ys[k] = val;
               if (last) {
                 const float dd = fabsf(val - cur[m].old);
                 l1 += dd;
@@ -631,8 +648,8 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
           // this slot now takes the operands of step t + D
 #pragma unroll
           for (int m = 0; m < MB; ++m)
-            wa_load<true>(ring[d][m], t + D, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, fld,
-                          fold, src, last);
+            wa_load<true>(ring[d][m], t + D, vb + lane + 32 * m, nu, nv, nx, xdir, ydir, V, rd,
+                          xs, src, last);
           if (NW > 1 && top) xs_val[t & 1][T.wid] = res[MB - 1];
           pn = qn;
           ps = qs;
@@ -1060,7 +1077,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
       if (f == 0) { its0 = n; ast0 = ast; } else { its1 = n; ast1 = ast; }
       field_done = !earlier && (ast == ST_OK || !cut || part == nparts - 1);
       if (field_done) {
-        w_slot<NW>(A, P, fld, w, s, f, T);
+        w_slot<NW>(A, P, w_adj_result(fld, fold, n), w, s, f, T);
         mark(PH_SLOT);
       }
     }

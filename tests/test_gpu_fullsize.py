@@ -115,6 +115,29 @@ def test_config4_sampled(sg, oracle, prec):
     eng.close()
 
 
+def test_config4_every_fp32_variant_same_bits(sg):
+    """Config 4's uneven grids (six sources x all 25 periods, 64^2 ... 384^2)
+    through every variant of the FP32 row kernel -- teams or strips, work
+    items or whole solves, operands a step ahead or at the visit: the same
+    bits everywhere (travel times, kernels, misfit, iteration counts)."""
+    pb = W.config4(nsrc=6)
+    eng = sg.Engine(0)
+    eng.load(pb)
+    outs = {}
+    for v in range(6):
+        eng.set_kernel(sg.PREC_FP32, kind=2, variant=v)
+        eng.run(3, sg.PREC_FP32)
+        assert eng.sync() == sg.OK
+        outs[v] = eng.results()
+    eng.close()
+    base = outs[0]
+    assert int(np.max(base["status"])) == 0
+    for v in range(1, 6):
+        for k in ("tt_fwd", "adj_s", "adj_density", "fwd_iters", "adj_iters", "status"):
+            assert np.array_equal(outs[v][k], base[k]), (v, k)
+        assert outs[v]["chi"] == base["chi"], v
+
+
 def test_serving_request_on_curved_surface(sg, oracle):
     """One gradient request (3-D mode) over the surface metric of the
     config-5 island (resampled to 128^2) through the serving loop, FP64 and
