@@ -126,13 +126,22 @@ struct ThreadCtx {
   }
   int setup() {
     if (init) return SURFATT_OK;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return SURFATT_CUDA_ERROR;
-    if (cudaMallocHost(&si_host, 4 * sizeof(int)) != cudaSuccess) return SURFATT_CUDA_ERROR;
-    if (cudaEventCreateWithFlags(&done, cudaEventBlockingSync | cudaEventDisableTiming) !=
-        cudaSuccess)
-      return SURFATT_CUDA_ERROR;
-    init = true;
-    return SURFATT_OK;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+        cudaMallocHost(&si_host, 4 * sizeof(int)) == cudaSuccess &&
+        cudaEventCreateWithFlags(&done, cudaEventBlockingSync | cudaEventDisableTiming) ==
+            cudaSuccess) {
+      init = true;
+      return SURFATT_OK;
+    }
+    // a partial setup is undone, so that the next call starts afresh
+    if (done) cudaEventDestroy(done);
+    if (si_host) cudaFreeHost(si_host);
+    if (st) cudaStreamDestroy(st);
+    done = nullptr;
+    si_host = nullptr;
+    st = nullptr;
+    cudaGetLastError();
+    return SURFATT_CUDA_ERROR;
   }
   // Waits for the thread's stream, the calling thread sleeping rather than
   // spinning: callers on every host core (the reference's one MPI rank per
@@ -752,6 +761,10 @@ surfatt_status_t surfatt_engine_create(surfatt_engine_t** out, int device, size_
       cudaEventCreate(&e->evs0) != cudaSuccess || cudaEventCreate(&e->evs1) != cudaSuccess ||
       e->cs.create() != ST_OK) {
     e->cs.destroy();
+    for (cudaEvent_t ev : {e->ev0, e->ev1, e->evk0, e->evk1, e->evs0, e->evs1})
+      if (ev) cudaEventDestroy(ev);
+    if (e->st) cudaStreamDestroy(e->st);
+    cudaGetLastError();
     delete e;
     return SURFATT_CUDA_ERROR;
   }

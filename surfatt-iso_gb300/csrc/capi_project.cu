@@ -35,6 +35,12 @@ struct ProjCtx {
     if (init) return SURFATT_OK;
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ev0) != cudaSuccess || cudaEventCreate(&ev1) != cudaSuccess) {
+      // a partial setup is undone, so that the next call starts afresh
+      if (ev0) cudaEventDestroy(ev0);
+      if (ev1) cudaEventDestroy(ev1);
+      if (st) cudaStreamDestroy(st);
+      ev0 = ev1 = nullptr;
+      st = nullptr;
       cudaGetLastError();
       return SURFATT_CUDA_ERROR;
     }

@@ -244,11 +244,16 @@ surfatt_status_t surfatt_srcrec_build_worklist(surfatt_srcrec_t* h, int device, 
   SrcRecTable& t = h->t;
   const int n = t.npath(), S = (int)t.sta_name.size(), P = (int)t.periods.size();
   CK(cudaSetDevice(device));
-  cudaStream_t st;
-  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    cudaGetLastError();
+    return SURFATT_CUDA_ERROR;
+  }
   std::vector<unsigned char> pz(P);
   for (int p = 0; p < P; ++p) pz[p] = t.periods[p] == 0.0;
   const size_t SP = (size_t)S * P, nI = sizeof(int), nD = sizeof(double);

@@ -414,6 +414,13 @@ void finish_request(surfatt_server* S, Request& r) {
     if (!ok) r.status = ST_CUDA_ERROR;
     for (int s = 0; s < L.nsolve && r.status == ST_OK; ++s)
       if (r.h_status[s] != ST_OK) r.status = r.h_status[s];
+  } else if (r.st) {
+    // a request that failed part-way may still have work queued: none of
+    // it may write into the chunk once the arena hands it out again
+    cudaStreamSynchronize(r.st);
+    for (cudaStream_t s : r.cs.side)
+      if (s) cudaStreamSynchronize(s);
+    cudaGetLastError();
   }
   if (r.st) cudaStreamDestroy(r.st);
   if (r.done) cudaEventDestroy(r.done);
