@@ -58,7 +58,9 @@ struct PeriodDev {
   const float* f32;
   // 1/svel**2 and 1/svel**3 (isv, isv + N) for the FP32 path's kernel slots
   const double* isv;
-  // per-cell FP32 records: {a, b, c, fun**2} and {disx, disy, 1/svel**2, 1/svel**3}
+  // per-cell FP32 records: p4a[k] = {a, b, c, fun**2}; p4b holds N float4 of
+  // storage read as 2N float2: {disx, disy} at k, {1/svel**2, 1/svel**3} at
+  // N + k (the forward sweeps read the first half only, densely)
   const float4* p4a;
   const float4* p4b;
 };

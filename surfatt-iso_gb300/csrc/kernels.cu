@@ -81,7 +81,9 @@ __global__ void k_prep(PrepIn in, PrepOut out) {
         i2 = (float)(1.0 / (v * v));
         i3 = (float)(1.0 / (v * v * v));
       }
-      out.p4b[k] = make_float4((float)out.disx[k], (float)out.disy[k], i2, i3);
+      float2* const q = reinterpret_cast<float2*>(out.p4b);
+      q[k] = make_float2((float)out.disx[k], (float)out.disy[k]);
+      q[N + k] = make_float2(i2, i3);
     }
   }
 }

@@ -27,7 +27,7 @@ struct PrepOut {
   float* f32;   // optional (6N): FP32 a, b, c, fun**2, disx, disy
   double* isv;  // optional (2N): 1/svel**2, 1/svel**3 (model inputs only)
   float4* p4a;  // optional (N): {a, b, c, fun**2}
-  float4* p4b;  // optional (N): {disx, disy, 1/svel**2, 1/svel**3}
+  float4* p4b;  // optional (N float4 as 2N float2): {disx, disy} at k, {1/svel**2, 1/svel**3} at N + k
 };
 
 // Batched evaluation arguments (all device pointers).

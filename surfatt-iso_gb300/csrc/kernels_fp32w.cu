@@ -228,7 +228,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
   const float* const tau = V.tau;
   const float2* const G = V.G;
   const float4* const PA = P.p4a;
-  const float2* const PB = reinterpret_cast<const float2*>(P.p4b);  // {disx, disy} at 2k
+  const float2* const PB = reinterpret_cast<const float2*>(P.p4b);  // {disx, disy} at k
   const int flen = w.box.i1 > w.box.i0 ? w.box.i1 - w.box.i0 : 0;
   // Teams: warp w owns the rows vb .. vb + 32 MB - 1.  The south neighbour
   // of its first row is the last row of warp w-1, visited a step earlier:
@@ -287,7 +287,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
           gx[m] = g.x;
           gy[m] = g.y;
           pa[m] = PA[k];
-          const float2 d = PB[2 * k];
+          const float2 d = PB[k];
           dsx[m] = d.x;
           dsy[m] = d.y;
           if (last) old[m] = V.old[k];
@@ -799,8 +799,8 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const floa
         ta[g] = 0.f;
         if (i < nx) {
           const size_t k = i + (size_t)nx * j;
-          const float4 pb = P.p4b[k];
-          isv[g] = A.mode == 3 ? pb.w : pb.z;
+          const float2 iv = reinterpret_cast<const float2*>(P.p4b)[(size_t)nx * ny + k];
+          isv[g] = A.mode == 3 ? iv.y : iv.x;
           ta[g] = field[k];
         }
       }
