@@ -48,12 +48,12 @@ KERNEL_NAMES = {0: "k_batch_fp64", 1: "k_batch_fp32", 2: "k_batch_fp32w"}
 # DRAM bytes (read + write) per launch of the FP32 row kernel
 # (k_batch_fp32w, variant 0) on the full 1280-solve workload, from one ncu
 # capture of the first launch of this bench command (dram__bytes_read.sum
-# 14.36 GB + dram__bytes_write.sum 4.58 GB in 17.34 ms):
+# 14.28 GB + dram__bytes_write.sum 4.57 GB in 17.43 ms):
 # profiles/k_batch_fp32w_config3.md.  The per-solve workspaces of the 1216
 # resident solves (about 1 GB) do not fit in L2, so operands are re-read
 # from DRAM every sweep.  Reported only when the autotuner picked that
 # kernel.
-DRAM_BYTES_PER_LAUNCH = {"config2": 18.93e9}
+DRAM_BYTES_PER_LAUNCH = {"config2": 18.85e9}
 METRIC = "eikonal+adjoint solves/s (batched FP32-factored, rel err<=1e-5 vs FP64)"
 
 
