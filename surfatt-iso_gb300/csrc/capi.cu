@@ -652,7 +652,7 @@ struct surfatt_engine {
   std::vector<long long> kslot;
   // device buffers
   DBuf d_periods, d_xdeg, d_ydeg, d_xs, d_ys, d_cosy, d_siny, d_A, d_B, d_C, d_V, d_a, d_b, d_c,
-      d_fun, d_f2, d_disx, d_disy, d_f32, d_isv, d_p4a, d_p4b, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
+      d_fun, d_f2, d_disx, d_disy, d_f32, d_isv, d_p4a, d_pidx, d_srcx, d_srcy, d_rec_off, d_nrec, d_recx, d_recy,
       d_tt, d_weight, d_path, d_order, d_plist_off, d_plist, d_kslot, d_goff, d_nx, d_ny;
   DBuf d_tekio, d_wgt, d_ttfwd, d_chis, d_chi, d_kc, d_kcd, d_adj, d_adjd, d_status, d_fit, d_ait,
       d_fupd, d_aupd, d_ws, d_queue, d_phase;
@@ -693,7 +693,7 @@ struct surfatt_engine {
   }
   std::vector<DBuf*> all() {
     return {&d_periods, &d_xdeg, &d_ydeg, &d_xs, &d_ys, &d_cosy, &d_siny, &d_A, &d_B, &d_C,
-            &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_f32, &d_isv, &d_p4a, &d_p4b, &d_pidx, &d_srcx, &d_srcy,
+            &d_V, &d_a, &d_b, &d_c, &d_fun, &d_f2, &d_disx, &d_disy, &d_f32, &d_isv, &d_p4a, &d_pidx, &d_srcx, &d_srcy,
             &d_rec_off, &d_nrec, &d_recx, &d_recy, &d_tt, &d_weight, &d_path, &d_order,
             &d_plist_off, &d_plist, &d_kslot, &d_goff, &d_nx, &d_ny, &d_tekio, &d_wgt, &d_ttfwd,
             &d_chis, &d_chi, &d_kc, &d_kcd, &d_adj, &d_adjd, &d_status, &d_fit, &d_ait, &d_fupd,
@@ -732,7 +732,7 @@ int run_prep_all(surfatt_engine* e) {
                 e->d_fun.as<double>() + g, e->d_f2.as<double>() + g,
                 e->d_disx.as<double>() + g, e->d_disy.as<double>() + g,
                 e->d_f32.as<float>() + 6 * g, e->d_isv.as<double>() + 2 * g,
-                e->d_p4a.as<float4>() + g, e->d_p4b.as<float4>() + g};
+                e->d_p4a.as<float4>() + 2 * g, e->d_p4a.as<float4>() + 2 * g + 1};
     launch_prep(in, out, e->st);
   }
   CK(cudaGetLastError());
@@ -866,7 +866,7 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
   for (DBuf* b : {&e->d_a, &e->d_b, &e->d_c, &e->d_fun, &e->d_f2, &e->d_disx, &e->d_disy})
     r |= up(e, *b, (double*)nullptr, NC);
   r |= up(e, e->d_f32, (float*)nullptr, 6 * NC) | up(e, e->d_isv, (double*)nullptr, 2 * NC);
-  r |= up(e, e->d_p4a, (float4*)nullptr, NC) | up(e, e->d_p4b, (float4*)nullptr, NC);
+  r |= up(e, e->d_p4a, (float4*)nullptr, 2 * NC);
   r |= up(e, e->d_pidx, pb->pidx, ns) | up(e, e->d_srcx, pb->srcx, ns) |
        up(e, e->d_srcy, pb->srcy, ns) | up(e, e->d_rec_off, pb->rec_off, ns) |
        up(e, e->d_nrec, pb->nrec, ns);
@@ -918,8 +918,8 @@ surfatt_status_t surfatt_engine_load(surfatt_engine_t* e, const surfatt_problem_
     P.goff = g;
     P.f32 = e->d_f32.as<float>() + 6 * g;
     P.isv = e->d_isv.as<double>() + 2 * g;
-    P.p4a = e->d_p4a.as<float4>() + g;
-    P.p4b = e->d_p4b.as<float4>() + g;
+    P.p4a = e->d_p4a.as<float4>() + 2 * g;
+    P.p4b = P.p4a + 1;
   }
   r = up(e, e->d_periods, e->periods.data(), np);
   if (r) return (surfatt_status_t)r;

@@ -58,9 +58,8 @@ struct PeriodDev {
   const float* f32;
   // 1/svel**2 and 1/svel**3 (isv, isv + N) for the FP32 path's kernel slots
   const double* isv;
-  // per-cell FP32 records: p4a[k] = {a, b, c, fun**2}; p4b holds N float4 of
-  // storage read as 2N float2: {disx, disy} at k, {1/svel**2, 1/svel**3} at
-  // N + k (the forward sweeps read the first half only, densely)
+  // per-cell FP32 record of 32 bytes: p4a[2k] = {a, b, c, fun**2} and
+  // p4b[2k] = p4a[2k + 1] = {disx, disy, 1/svel**2, 1/svel**3} (p4b = p4a + 1)
   const float4* p4a;
   const float4* p4b;
 };

@@ -73,7 +73,7 @@ __global__ void k_prep(PrepIn in, PrepOut out) {
       out.isv[k] = 1.0 / (v * v);
       out.isv[N + k] = 1.0 / (v * v * v);
     }
-    if (out.p4a) out.p4a[k] = make_float4((float)a, (float)b, (float)c, (float)(f * f));
+    if (out.p4a) out.p4a[2 * k] = make_float4((float)a, (float)b, (float)c, (float)(f * f));
     if (out.p4b) {
       float i2 = 0.f, i3 = 0.f;
       if (in.from_model) {
@@ -81,9 +81,7 @@ __global__ void k_prep(PrepIn in, PrepOut out) {
         i2 = (float)(1.0 / (v * v));
         i3 = (float)(1.0 / (v * v * v));
       }
-      float2* const q = reinterpret_cast<float2*>(out.p4b);
-      q[k] = make_float2((float)out.disx[k], (float)out.disy[k]);
-      q[N + k] = make_float2(i2, i3);
+      out.p4b[2 * k] = make_float4((float)out.disx[k], (float)out.disy[k], i2, i3);
     }
   }
 }

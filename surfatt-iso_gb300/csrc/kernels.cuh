@@ -26,8 +26,8 @@ struct PrepOut {
   double *xs, *ys, *cosy, *siny, *a, *b, *c, *fun, *f2, *disx, *disy;
   float* f32;   // optional (6N): FP32 a, b, c, fun**2, disx, disy
   double* isv;  // optional (2N): 1/svel**2, 1/svel**3 (model inputs only)
-  float4* p4a;  // optional (N): {a, b, c, fun**2}
-  float4* p4b;  // optional (N float4 as 2N float2): {disx, disy} at k, {1/svel**2, 1/svel**3} at N + k
+  float4* p4a;  // optional (2N): cell k's 32-byte record at 2k: {a, b, c, fun**2}
+  float4* p4b;  // optional, = p4a + 1: {disx, disy, 1/svel**2, 1/svel**3} at 2k
 };
 
 // Batched evaluation arguments (all device pointers).

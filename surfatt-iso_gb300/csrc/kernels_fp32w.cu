@@ -112,33 +112,53 @@ __device__ __forceinline__ double w_warp_max(double b) {
   return b;
 }
 
-// Workspace per warp slot: W (float4 adjoint weights), G (float2: T0x,
-// T0y), T0, tau, old, 1/d, two scaled adjoint sources (4 bytes each per
-// cell), per-column half-angle sines and cosines.
+// Workspace per warp slot: W (float4 adjoint weights), 4N floats of
+// forward state from R, old, 1/d, two scaled adjoint sources (4 bytes each
+// per cell), per-column half-angle sines and cosines.  The forward state is
+// laid out one of two ways:
+//   separate (one-warp kernel):  G = {T0x, T0y} (float2), T0, tau;
+//   paired (strips and teams):   TT = {T0, tau} (float2), G.
+// A row's forward sweep reads four operand streams with the separate
+// layout and three with the paired one; a tall grid's latency-bound strips
+// gain from the fewer L1 lines (config 4: 159 -> 154 ms), the one-warp
+// kernel does not (17.2 -> 17.4 ms on config 2), so each kernel keeps the
+// layout it is faster with (all results are the same bits).
 long long batch_fp32w_ws_doubles(long long N) {
-  const long long floats = 4 * N + 2 * N + 6 * N + 2 * 4096;
+  const long long floats = 4 * N + 4 * N + 4 * N + 2 * 4096;  // W, R, old / 1/d / sources, col
   long long d = (floats + 1) / 2 + 64;
   return (d + 31) / 32 * 32;  // keep every slot 256-byte aligned
 }
 
 struct WSlot {
   float4* W;
-  float2* G;
-  float* T0;
+  float* R;    // start of the forward state (4N floats)
+  float2* TT;  // paired: {T0, tau} per cell (null when separate)
+  float2* G;   // {T0x, T0y} per cell
+  float* T0;   // separate: T0, tau per cell (null when paired)
   float* tau;
+  bool pair;
   float* old;
   float* id;
   float* src[2];
   float* col;  // per column sin and cos of half the longitude offset (2 * nx)
 };
 
-__device__ inline WSlot wcarve(double* base, size_t N) {
+__device__ inline WSlot wcarve(double* base, size_t N, bool pair) {
   WSlot V;
   V.W = reinterpret_cast<float4*>(base);
-  V.G = reinterpret_cast<float2*>(V.W + N);
-  V.T0 = reinterpret_cast<float*>(V.G + N);
-  V.tau = V.T0 + N;
-  V.old = V.tau + N;
+  V.R = reinterpret_cast<float*>(V.W + N);
+  V.pair = pair;
+  if (pair) {
+    V.TT = reinterpret_cast<float2*>(V.R);
+    V.G = V.TT + N;
+    V.T0 = V.tau = nullptr;
+  } else {
+    V.TT = nullptr;
+    V.G = reinterpret_cast<float2*>(V.R);
+    V.T0 = reinterpret_cast<float*>(V.G + N);
+    V.tau = V.T0 + N;
+  }
+  V.old = V.R + 4 * N;
   V.id = V.old + N;
   V.src[0] = V.id + N;
   V.src[1] = V.src[0] + N;
@@ -146,9 +166,16 @@ __device__ inline WSlot wcarve(double* base, size_t N) {
   return V;
 }
 
+// {T0, tau} of cell k in the kernel's layout
+template <bool PAIR>
+__device__ __forceinline__ float2 w_t0tau(const WSlot& V, size_t k) {
+  if constexpr (PAIR) return V.TT[k];
+  return make_float2(V.T0[k], V.tau[k]);
+}
+
 
 // T0 and (T0x, T0y) of every cell; tau initialised (1 in the frozen box).
-template <int NW>
+template <int NW, bool PAIR>
 __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSolve& w,
                             const WSlot& V, const Tm<NW>& T) {
   const int nx = P.nx, ny = P.ny, lane = T.lane;
@@ -164,9 +191,14 @@ __device__ inline void w_t0(const PeriodDev& P, double x0, double y0, const WSol
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
       const float4 c = t0_cell(P, src, row, i, j, V.col[i], V.col[nx + i]);
-      V.T0[k] = c.x;
+      const float tau0 = w.box.has(i, j) ? 1.0f : 10.0f;
+      if constexpr (PAIR) {
+        V.TT[k] = make_float2(c.x, tau0);
+      } else {
+        V.T0[k] = c.x;
+        V.tau[k] = tau0;
+      }
       V.G[k] = make_float2(c.y, c.z);
-      V.tau[k] = w.box.has(i, j) ? 1.0f : 10.0f;
     }
   }
   tsync<NW>();
@@ -224,11 +256,24 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
   const int nx = P.nx, ny = P.ny, lane = T.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
   const int nsteps = nx + ny - 1;
-  const float* const T0a = V.T0;
+  constexpr bool PAIR = ST || NW > 1;  // this kernel's workspace layout (wcarve)
+  const float2* const TT = V.TT;  // paired: {T0, tau}
+  const float* const T0a = V.T0;  // separate
   const float* const tau = V.tau;
-  const float2* const G = V.G;
+  const float2* const G = V.G;    // {T0x, T0y}
+  // old tau (own) and T0 of cell k
+  auto ld_pt = [&](int k, float& own, float& t0) {
+    if constexpr (PAIR) {
+      const float2 q = TT[k];
+      own = q.y;
+      t0 = q.x;
+    } else {
+      own = tau[k];
+      t0 = T0a[k];
+    }
+  };
   const float4* const PA = P.p4a;
-  const float2* const PB = reinterpret_cast<const float2*>(P.p4b);  // {disx, disy} at k
+  const float2* const PB = reinterpret_cast<const float2*>(P.p4b);  // {disx, disy} at 4k
   const int flen = w.box.i1 > w.box.i0 ? w.box.i1 - w.box.i0 : 0;
   // Teams: warp w owns the rows vb .. vb + 32 MB - 1.  The south neighbour
   // of its first row is the last row of warp w-1, visited a step earlier:
@@ -272,9 +317,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
         own = 0.f;
         t0 = 0.f;
         if ((unsigned)(tt - R[m].lo) < (unsigned)nx) {
-          const int k = R[m].kb + xdir * tt;
-          own = tau[k];
-          t0 = T0a[k];
+          ld_pt(R[m].kb + xdir * tt, own, t0);
         }
       };
       // the cell constants of band m at step tt
@@ -286,8 +329,8 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
           const float2 g = G[k];
           gx[m] = g.x;
           gy[m] = g.y;
-          pa[m] = PA[k];
-          const float2 d = PB[k];
+          pa[m] = PA[2 * k];
+          const float2 d = PB[4 * k];
           dsx[m] = d.x;
           dsy[m] = d.y;
           if (last) old[m] = V.old[k];
@@ -300,8 +343,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
         t0 = 0.f;
         if (u >= 0 && u < nx && vtop + 1 < ny) {
           const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? vtop + 1 : ny - 2 - vtop);
-          own = tau[k];
-          t0 = T0a[k];
+          ld_pt(k, own, t0);
         }
       };
       // strips: new tau and T0 of the cell south of the bottom row at step
@@ -312,8 +354,7 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
         t0 = 0.f;
         if (u >= 0 && u < nx && vb >= 1) {
           const int k = (xdir > 0 ? u : nx - 1 - u) + nx * (ydir > 0 ? vb - 1 : ny - vb);
-          own = tau[k];
-          t0 = T0a[k];
+          ld_pt(k, own, t0);
         }
       };
       // exchange ring: steps t (x0), t + 1 (x1), t + 2 (x2, in flight)
@@ -374,7 +415,10 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
               nv = wf_visit(o, res[m], x1o[m], south, north, t0prev[m], x1t[m], t0s, t0n, tl > 0,
                             R[m].hass, tl < nx - 1, R[m].hasn, xdir, ydir, idx, idy);
             }
-            V.tau[k] = nv;
+            if constexpr (PAIR)
+              reinterpret_cast<float*>(V.TT)[2 * (size_t)k + 1] = nv;
+            else
+              V.tau[k] = nv;
             if (s == 0) V.old[k] = x0o[m];
             if (last && !frz) dds[m] = fabsf(nv - old[m]) * x0t[m];
             res[m] = nv;
@@ -437,14 +481,22 @@ __device__ inline void w_fwd_sweeps(const PeriodDev& P, const WSlot& V, const WS
 // ---------------------------------------------------------------------------
 // Weights of Ta = src + ww*Ta_W + we*Ta_E + ws*Ta_S + wn*Ta_N (face fluxes of
 // :1348-1370 with T = tau*T0 in FP32) and 1/d per interior cell.
-template <int NW>
+template <int NW, bool PAIR>
 __device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, const Tm<NW>& TM) {
   const int nx = P.nx, ny = P.ny, lane = TM.lane;
   const float idx = (float)(1.0 / P.dx), idy = (float)(1.0 / P.dy);
-  const float* T0 = V.T0;
+  const float2* TT = V.TT;  // paired: {T0, tau}
+  const float* T0 = V.T0;   // separate
   const float4* PA = P.p4a;
   // T = tau*T0 rounded on its own (no contraction with the differences below)
-  auto T = [&](size_t k) { return __fmul_rn(V.tau[k], T0[k]); };
+  auto T = [&](size_t k) {
+    if constexpr (PAIR) {
+      const float2 q = TT[k];
+      return __fmul_rn(q.y, q.x);
+    } else {
+      return __fmul_rn(V.tau[k], T0[k]);
+    }
+  };
   for (int j = TM.wid; j < ny; j += NW) {  // rows by warp, columns by lane
     for (int i = lane; i < nx; i += 32) {
       const size_t k = i + (size_t)nx * j;
@@ -454,7 +506,7 @@ __device__ inline void w_adj_setup(const PeriodDev& P, const WSlot& V, const Tm<
         continue;
       }
       const size_t w = k - 1, e = k + 1, s = k - nx, n = k + nx;
-      const float4 pk = PA[k], pw = PA[w], pe = PA[e], ps = PA[s], pn = PA[n];
+      const float4 pk = PA[2 * k], pw = PA[2 * w], pe = PA[2 * e], ps = PA[2 * s], pn = PA[2 * n];
       const float Tk = T(k), Tw = T(w), Te = T(e), Ts = T(s), Tn = T(n);
       const float Twn = T(w + nx), Tws = T(w - nx), Ten = T(e + nx), Tes = T(e - nx);
       float4 W;
@@ -501,13 +553,19 @@ __device__ __forceinline__ float* w_adj_result(float* fld, float* fold, int iter
   return (iters & 1) ? fold : fld;
 }
 
-// Storage of adjoint field f during the adjoint: field 0 in tau / old, field
-// 1 in the T0 gradient's array (dead once the adjoint coefficients are set),
-// so that a solve's two fields can be swept side by side.
+// Storage of adjoint field f during the adjoint, in forward state that is
+// dead once the adjoint weights are set, so that a solve's two fields can
+// be swept side by side: paired layout, field 0 and its second buffer in
+// TT's 2N floats, field 1 and its second buffer in G's; separate layout,
+// field 0 in tau / old, field 1 in G's 2N floats.
+template <bool PAIR>
 __device__ __forceinline__ float* w_field(const WSlot& V, int f, size_t N) {
+  if constexpr (PAIR) return V.R + (f ? 2 * N : 0);
   return f ? reinterpret_cast<float*>(V.G) : V.tau;
 }
+template <bool PAIR>
 __device__ __forceinline__ float* w_field_old(const WSlot& V, int f, size_t N) {
+  if constexpr (PAIR) return V.R + (f ? 3 * N : N);
   return f ? reinterpret_cast<float*>(V.G) + N : V.old;
 }
 
@@ -679,11 +737,14 @@ __device__ inline void w_adj_sweeps(const PeriodDev& P, const WSlot& V, float* f
 }
 
 // T = tau*T0 at a node (FP64 product of the FP32 factors)
+template <bool PAIR>
 __device__ __forceinline__ double w_T(const WSlot& V, size_t k) {
-  return (double)V.tau[k] * (double)V.T0[k];
+  const float2 q = w_t0tau<PAIR>(V, k);
+  return (double)q.y * (double)q.x;
 }
 
 // interp2_0_dp on the caller's increasing degree grid (src/shared/utils.f90:917-942)
+template <bool PAIR>
 __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, double yq,
                                 double* out) {
   const int nx = P.nx, ny = P.ny;
@@ -708,10 +769,10 @@ __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, d
   const double n3 = fabs((x[x2] - xq) * (y[y1] - yq));
   const double n4 = fabs((x[x1] - xq) * (y[y1] - yq));
   double r = 0;
-  r = r + w_T(V, x1 + (size_t)nx * y1) * (n1 / vn);
-  r = r + w_T(V, x2 + (size_t)nx * y1) * (n2 / vn);
-  r = r + w_T(V, x1 + (size_t)nx * y2) * (n3 / vn);
-  r = r + w_T(V, x2 + (size_t)nx * y2) * (n4 / vn);
+  r = r + w_T<PAIR>(V, x1 + (size_t)nx * y1) * (n1 / vn);
+  r = r + w_T<PAIR>(V, x2 + (size_t)nx * y1) * (n2 / vn);
+  r = r + w_T<PAIR>(V, x1 + (size_t)nx * y2) * (n3 / vn);
+  r = r + w_T<PAIR>(V, x2 + (size_t)nx * y2) * (n4 / vn);
   *out = r;
   return true;
 }
@@ -721,13 +782,13 @@ __device__ inline bool w_interp(const PeriodDev& P, const WSlot& V, double xq, d
 // ---------------------------------------------------------------------------
 // Receiver times, misfit, outlier weights (src/measadj.f90:71-72, 82-84);
 // returns the status (ST_BAD_ARG for a receiver outside the grid).
-template <int NW>
+template <int NW, bool PAIR>
 __device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const WSlot& V, int s,
                                   int r0, int nr, const Tm<NW>& T, int st) {
   int bad = 0;
   for (int r = T.tid; r < nr; r += 32 * NW) {
     double v = 0.0;
-    if (!w_interp(P, V, A.recx[r0 + r], A.recy[r0 + r], &v)) bad = 1;
+    if (!w_interp<PAIR>(P, V, A.recx[r0 + r], A.recy[r0 + r], &v)) bad = 1;
     A.tekio[r0 + r] = v;
     A.tt_fwd[A.path[r0 + r]] = v;
   }
@@ -735,7 +796,7 @@ __device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const 
   else bad = __syncthreads_or(bad);
   if (A.Tout) {
     const size_t N = (size_t)P.nx * P.ny;
-    for (size_t k = T.tid; k < N; k += 32 * NW) A.Tout[A.kslot[s] + k] = w_T(V, k);
+    for (size_t k = T.tid; k < N; k += 32 * NW) A.Tout[A.kslot[s] + k] = w_T<PAIR>(V, k);
   }
   tsync<NW>();
   if (T.tid == 0) {
@@ -758,12 +819,12 @@ __device__ inline int w_receivers(const BatchArgs& A, const PeriodDev& P, const 
 // Adjoint coefficients and the scaled sources of nf fields: weight*(tekio-tt)
 // (src/measadj.f90:88) and -weight (:102), splat bilinearly over the cell
 // area (src/eikon_solver_2d.f90:1328-1336) and scaled by 1/d.
-template <int NW>
+template <int NW, bool PAIR>
 __device__ inline int w_adj_sources(const BatchArgs& A, const PeriodDev& P, const WSlot& V,
                                     int r0, int nr, int nf, const Tm<NW>& T, int st) {
   const int nx = P.nx, ny = P.ny;
   const size_t N = (size_t)nx * ny;
-  w_adj_setup<NW>(P, V, T);
+  w_adj_setup<NW, PAIR>(P, V, T);
   // (the fields' arrays picked by selects: an indexed V.src[f] would put
   // the whole slot descriptor in local memory)
   for (int f = 0; f < nf; ++f) {
@@ -799,8 +860,8 @@ __device__ inline void w_slot(const BatchArgs& A, const PeriodDev& P, const floa
         ta[g] = 0.f;
         if (i < nx) {
           const size_t k = i + (size_t)nx * j;
-          const float2 iv = reinterpret_cast<const float2*>(P.p4b)[(size_t)nx * ny + k];
-          isv[g] = A.mode == 3 ? iv.y : iv.x;
+          const float4 pb = P.p4b[2 * k];
+          isv[g] = A.mode == 3 ? pb.w : pb.z;
           ta[g] = field[k];
         }
       }
@@ -857,6 +918,9 @@ __host__ __device__ inline int w_items_for_mode(int mode, int fwd_items = kFwdIt
 
 template <int MB, int PF, int MINW, int NW, bool ST>
 __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A) {
+  // workspace layout: paired forward state for strips and teams, separate
+  // for the one-warp kernel (batch_fp32w_ws_doubles)
+  constexpr bool kPair = ST || NW > 1;
   const Tm<NW> T = this_team<NW>();
   const int lane = T.lane;
   const bool cut = A.items > 1;
@@ -944,7 +1008,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     const int nx = P.nx, ny = P.ny;
     const size_t N = (size_t)nx * ny;
     const int r0 = A.rec_off[s], nr = A.nrec[s];
-    const WSlot V = wcarve(A.ws + (cut ? (long long)s : (long long)blockIdx.x) * A.ws_doubles, N);
+    const WSlot V = wcarve(A.ws + (cut ? (long long)s : (long long)blockIdx.x) * A.ws_doubles, N,
+                           kPair);
     const double xd0 = A.srcx[s], yd0 = A.srcy[s];
     const double x0 = xd0 / 180.0 * PI_S, y0 = yd0 / 180.0 * PI_S;
     unsigned long long* const pc = A.phase_cycles;
@@ -1009,7 +1074,7 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
     // (k+1)*kSplitIter, the last one (a whole solve: all) up to MaxIter,
     // unless an earlier item converged
     if (first == 0) {
-      w_t0<NW>(P, x0, y0, w, V, T);
+      w_t0<NW, kPair>(P, x0, y0, w, V, T);
       mark(PH_SETUP);
     }
     if (first < nfwd && (first == 0 || (fst != ST_OK && fit < MAXITER_UW))) {
@@ -1033,10 +1098,10 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
         const double frozen = (double)(w.box.i1 - w.box.i0 + 1) * (w.box.j1 - w.box.j0 + 1);
         A.fwd_updates[s] = (double)fit * 4.0 * ((double)N - frozen);
       }
-      st = w_receivers<NW>(A, P, V, s, r0, nr, T, fst);
+      st = w_receivers<NW, kPair>(A, P, V, s, r0, nr, T, fst);
       mark(PH_RECV);
       if (A.mode >= 2) {
-        st = w_adj_sources<NW>(A, P, V, r0, nr, nf, T, st);
+        st = w_adj_sources<NW, kPair>(A, P, V, r0, nr, nf, T, st);
         mark(PH_ADJ_SETUP);
       }
       if (cut && A.mode >= 2) {
@@ -1066,8 +1131,8 @@ __global__ void __launch_bounds__(32 * NW, MINW / NW) k_batch_fp32w(BatchArgs A)
         it0 = n + 1;
       }
       if (cut && part < nparts - 1) it1 = (part + 1) * kAdjSplitIter;
-      float* const fld = f ? w_field(V, 1, N) : w_field(V, 0, N);
-      float* const fold = f ? w_field_old(V, 1, N) : w_field_old(V, 0, N);
+      float* const fld = f ? w_field<kPair>(V, 1, N) : w_field<kPair>(V, 0, N);
+      float* const fold = f ? w_field_old<kPair>(V, 1, N) : w_field_old<kPair>(V, 0, N);
       const bool earlier = cut && part > 0 && ast == ST_OK;  // converged in an earlier part
       if (!earlier) {
         w_adj_sweeps<MB, NW, (PF == 1 && NW > 1) ? 3 : 2, ST>(

@@ -143,8 +143,8 @@ void carve_periods(Carver& cv, long long nxs, long long nys, long long NC, int n
   a->disy = cv.take<double>(NC);
   a->f32 = cv.take<float>(6 * NC);
   a->isv = cv.take<double>(2 * NC);
-  a->p4a = cv.take<float4>(NC);
-  a->p4b = cv.take<float4>(NC);
+  a->p4a = cv.take<float4>(2 * NC);  // 32-byte records
+  a->p4b = a->p4a ? a->p4a + 1 : nullptr;
   a->periods = cv.take<PeriodDev>(np);
   a->goff = cv.take<long long>(np);
   a->nx = cv.take<int>(np);
@@ -238,7 +238,7 @@ int prep_periods(const Model& m, const PeriodArrays& src_axes, const PeriodArray
     PrepOut o{ax(out.xs, m.xoff[p]), ax(out.ys, m.yoff[p]), ax(out.cosy, m.yoff[p]),
               ax(out.siny, m.yoff[p]),
               out.a + g, out.b + g, out.c + g, out.fun + g, out.f2 + g, out.disx + g, out.disy + g,
-              out.f32 + 6 * g, out.isv + 2 * g, out.p4a + g, out.p4b + g};
+              out.f32 + 6 * g, out.isv + 2 * g, out.p4a + 2 * g, out.p4b + 2 * g};
     launch_prep(in, o, st);
   }
   return cudaGetLastError() == cudaSuccess ? ST_OK : ST_CUDA_ERROR;
@@ -272,8 +272,8 @@ std::vector<PeriodDev> period_descs(const Model& m, const PeriodArrays& axes,
     P.goff = g;
     P.f32 = f.f32 + 6 * g;
     P.isv = f.isv + 2 * g;
-    P.p4a = f.p4a + g;
-    P.p4b = f.p4b + g;
+    P.p4a = f.p4a + 2 * g;
+    P.p4b = f.p4b + 2 * g;
   }
   return out;
 }
