@@ -136,7 +136,6 @@ struct WSlot {
   float2* G;   // {T0x, T0y} per cell
   float* T0;   // separate: T0, tau per cell (null when paired)
   float* tau;
-  bool pair;
   float* old;
   float* id;
   float* src[2];
@@ -147,7 +146,6 @@ __device__ inline WSlot wcarve(double* base, size_t N, bool pair) {
   WSlot V;
   V.W = reinterpret_cast<float4*>(base);
   V.R = reinterpret_cast<float*>(V.W + N);
-  V.pair = pair;
   if (pair) {
     V.TT = reinterpret_cast<float2*>(V.R);
     V.G = V.TT + N;
