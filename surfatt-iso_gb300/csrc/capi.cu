@@ -721,20 +721,22 @@ int up(surfatt_engine* e, DBuf& b, const T* src, size_t n) {
 }
 
 int run_prep_all(surfatt_engine* e) {
+  std::vector<PrepIn> ins(e->nperiod);
+  std::vector<PrepOut> outs(e->nperiod);
   for (int p = 0; p < e->nperiod; ++p) {
     const long long g = e->goff[p];
-    PrepIn in{e->nx[p], e->ny[p], 1, e->d_xdeg.as<double>() + e->xoff[p],
+    ins[p] = PrepIn{e->nx[p], e->ny[p], 1, e->d_xdeg.as<double>() + e->xoff[p],
               e->d_ydeg.as<double>() + e->yoff[p], e->d_A.as<double>() + g,
               e->d_B.as<double>() + g, e->d_C.as<double>() + g, e->d_V.as<double>() + g, 1};
-    PrepOut out{e->d_xs.as<double>() + e->xoff[p], e->d_ys.as<double>() + e->yoff[p],
+    outs[p] = PrepOut{e->d_xs.as<double>() + e->xoff[p], e->d_ys.as<double>() + e->yoff[p],
                 e->d_cosy.as<double>() + e->yoff[p], e->d_siny.as<double>() + e->yoff[p],
                 e->d_a.as<double>() + g, e->d_b.as<double>() + g, e->d_c.as<double>() + g,
                 e->d_fun.as<double>() + g, e->d_f2.as<double>() + g,
                 e->d_disx.as<double>() + g, e->d_disy.as<double>() + g,
                 e->d_f32.as<float>() + 6 * g, e->d_isv.as<double>() + 2 * g,
                 e->d_p4a.as<float4>() + 2 * g, e->d_p4a.as<float4>() + 2 * g + 1};
-    launch_prep(in, out, e->st);
   }
+  launch_prep_batch(ins.data(), outs.data(), e->nperiod, e->st);
   CK(cudaGetLastError());
   return SURFATT_OK;
 }

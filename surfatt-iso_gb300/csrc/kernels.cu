@@ -19,11 +19,9 @@ namespace sgb {
 // b = sphb/R^2, c = sphc/(R^2 cos y) (:817-821).  The one-sided `dis` terms
 // (:1014, :1055) are loop invariant and evaluated here exactly as written.
 // ---------------------------------------------------------------------------
-__global__ void k_prep(PrepIn in, PrepOut out) {
+__device__ inline void prep_cells(const PrepIn& in, const PrepOut& out, size_t tid, size_t nthr) {
   const int nx = in.nx, ny = in.ny;
   const size_t N = (size_t)nx * ny;
-  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  const size_t nthr = (size_t)gridDim.x * blockDim.x;
   if (out.xs)  // axis outputs are optional (already prepared for this grid)
     for (size_t i = tid; i < (size_t)nx; i += nthr)
       out.xs[i] = in.lonlat ? in.xdeg[i] / 180.0 * PI_S : in.xdeg[i];
@@ -86,12 +84,51 @@ __global__ void k_prep(PrepIn in, PrepOut out) {
   }
 }
 
-void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st) {
-  const size_t N = (size_t)in.nx * in.ny;
+__global__ void k_prep(PrepIn in, PrepOut out) {
+  prep_cells(in, out, blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+             (size_t)gridDim.x * blockDim.x);
+}
+
+// Up to kPrepBatch periods in one launch (block row p: period p), so that a
+// load or a velocity update of many small periods is one launch, not one
+// per period.  The table travels as the kernel's parameter.
+constexpr int kPrepBatch = 32;
+struct PrepBatch {
+  int n;
+  PrepIn in[kPrepBatch];
+  PrepOut out[kPrepBatch];
+};
+
+__global__ void k_prep_batch(const __grid_constant__ PrepBatch b) {
+  const int p = blockIdx.y;
+  if (p >= b.n) return;
+  prep_cells(b.in[p], b.out[p], blockIdx.x * (size_t)blockDim.x + threadIdx.x,
+             (size_t)gridDim.x * blockDim.x);
+}
+
+static int prep_grid(size_t N) {
   int grid = (int)((N + 255) / 256);
   if (grid < 1) grid = 1;
   if (grid > 4096) grid = 4096;
-  k_prep<<<grid, 256, 0, st>>>(in, out);
+  return grid;
+}
+
+void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st) {
+  k_prep<<<prep_grid((size_t)in.nx * in.ny), 256, 0, st>>>(in, out);
+}
+
+void launch_prep_batch(const PrepIn* in, const PrepOut* out, int np, cudaStream_t st) {
+  for (int p0 = 0; p0 < np; p0 += kPrepBatch) {
+    PrepBatch b;
+    b.n = np - p0 < kPrepBatch ? np - p0 : kPrepBatch;
+    size_t nmax = 0;
+    for (int i = 0; i < b.n; ++i) {
+      b.in[i] = in[p0 + i];
+      b.out[i] = out[p0 + i];
+      nmax = std::max(nmax, (size_t)in[p0 + i].nx * in[p0 + i].ny);
+    }
+    k_prep_batch<<<dim3(prep_grid(nmax), b.n), 256, 0, st>>>(b);
+  }
 }
 
 // ---------------------------------------------------------------------------

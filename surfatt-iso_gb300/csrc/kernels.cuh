@@ -96,6 +96,8 @@ enum SolvePhase {
 };
 
 void launch_prep(const PrepIn& in, const PrepOut& out, cudaStream_t st);
+// The same for np periods, in as few launches as the parameter table allows.
+void launch_prep_batch(const PrepIn* in, const PrepOut* out, int np, cudaStream_t st);
 // Largest grid the single-warp form of the row kernel takes; its warp
 // teams take up to kTeamMaxRows.
 constexpr int kWarpMaxRows = 128;

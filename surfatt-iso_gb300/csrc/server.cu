@@ -230,17 +230,20 @@ namespace {
 // from the model's metric and the given velocity.
 int prep_periods(const Model& m, const PeriodArrays& src_axes, const PeriodArrays& out,
                  const double* V, cudaStream_t st) {
+  std::vector<PrepIn> ins(m.nperiod);
+  std::vector<PrepOut> outs(m.nperiod);
   for (int p = 0; p < m.nperiod; ++p) {
     const long long g = m.goff[p];
-    PrepIn in{m.nx[p], m.ny[p], 1, src_axes.xdeg + m.xoff[p], src_axes.ydeg + m.yoff[p],
+    ins[p] = PrepIn{m.nx[p], m.ny[p], 1, src_axes.xdeg + m.xoff[p], src_axes.ydeg + m.yoff[p],
               src_axes.A + g, src_axes.B + g, src_axes.C + g, V + g, 1};
     auto ax = [](double* b, long long o) { return b ? b + o : nullptr; };
-    PrepOut o{ax(out.xs, m.xoff[p]), ax(out.ys, m.yoff[p]), ax(out.cosy, m.yoff[p]),
-              ax(out.siny, m.yoff[p]),
-              out.a + g, out.b + g, out.c + g, out.fun + g, out.f2 + g, out.disx + g, out.disy + g,
-              out.f32 + 6 * g, out.isv + 2 * g, out.p4a + 2 * g, out.p4b + 2 * g};
-    launch_prep(in, o, st);
+    outs[p] = PrepOut{ax(out.xs, m.xoff[p]), ax(out.ys, m.yoff[p]), ax(out.cosy, m.yoff[p]),
+                      ax(out.siny, m.yoff[p]),
+                      out.a + g, out.b + g, out.c + g, out.fun + g, out.f2 + g, out.disx + g,
+                      out.disy + g, out.f32 + 6 * g, out.isv + 2 * g, out.p4a + 2 * g,
+                      out.p4b + 2 * g};
   }
+  launch_prep_batch(ins.data(), outs.data(), m.nperiod, st);
   return cudaGetLastError() == cudaSuccess ? ST_OK : ST_CUDA_ERROR;
 }
 
