@@ -451,6 +451,17 @@ def test_engine_uneven_grids(sg, oracle):
     _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_engine_many_periods(sg, oracle, prec):
+    """40 periods: the per-period precompute runs in two launches (32 + 8)."""
+    pb = W.config4(nsrc=3, nperiod=40, nmax=40, nmin=24, span_deg=2.0)
+    assert pb.nperiod == 40
+    if prec == "fp64":
+        _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP64, TT_TOL, KER_TOL)
+    else:
+        _engine_vs_oracle(sg, oracle, pb, 3, sg.PREC_FP32, TT_TOL_F32, KER_TOL_F32)
+
+
 def test_batched_equals_single_solves(sg):
     """Every solve's result is independent of the batch it runs in."""
     pb = W.flat_case(nx=40, ny=36, nsta=6, nperiod=2, mode=3)
